@@ -1,0 +1,184 @@
+// C ABI of the plain single-scene solver (include/rfmm.h).
+//
+// Each entry point replaces a piece of the reference host's dispatch
+// sequence: rfmm_create ~ rebuildSimulation buffer setup (app.js:525-607,
+// native/main.rs:290-316), rfmm_seed_galaxy ~ the `initialize` pass
+// (native/main.rs:423-434), rfmm_solve_fields ~ the digest solve
+// (native/main.rs:436-449), rfmm_step ~ encode_frame (native/main.rs:411-421),
+// rfmm_digest ~ digest() (native/main.rs:152-163), rfmm_phase_times ~ the
+// timestamp-query frame (native/main.rs:466-520), rfmm_check_finite ~ the
+// finiteness scan (native/main.rs:536-549).
+#include <cmath>
+#include <new>
+#include <vector>
+
+#include "engine.h"
+#include "rfmm.h"
+
+struct rfmm_handle {
+  rfmm::Engine *engine;
+  rfmm_params params;
+};
+
+namespace {
+
+int guard(const rfmm_handle *h) { return (h == nullptr || h->engine == nullptr) ? RFMM_ERR_INVALID : RFMM_OK; }
+
+}  // namespace
+
+extern "C" {
+
+void rfmm_default_params(rfmm_params *p) {
+  if (p == nullptr) return;
+  *p = rfmm_params{};
+  p->dt = 0.0009f;
+  p->gravity = 0.34f;
+  p->softening = 0.012f;
+  p->speed = 1.0f;
+  p->control_strength = 0.7f;
+  p->control_radius = 0.22f;
+}
+
+const char *rfmm_status_string(int status) { return rfmm::status_string(status); }
+
+int rfmm_create(uint32_t n, const rfmm_params *params, rfmm_handle **out) {
+  if (out == nullptr) return RFMM_ERR_INVALID;
+  *out = nullptr;
+  rfmm::SceneSpec spec;
+  spec.n = n;
+  if (params != nullptr) {
+    spec.params = *params;
+  } else {
+    rfmm_default_params(&spec.params);
+  }
+  rfmm::Engine *e = nullptr;
+  const int st = rfmm::Engine::create({spec}, &e);
+  if (st != RFMM_OK) return st;
+  rfmm_handle *h = new (std::nothrow) rfmm_handle{e, spec.params};
+  if (h == nullptr) {
+    delete e;
+    return RFMM_ERR_OOM;
+  }
+  *out = h;
+  return RFMM_OK;
+}
+
+int rfmm_destroy(rfmm_handle *h) {
+  if (h == nullptr) return RFMM_ERR_INVALID;
+  delete h->engine;
+  delete h;
+  return RFMM_OK;
+}
+
+int rfmm_set_stream(rfmm_handle *h, void *stream) {
+  if (guard(h)) return RFMM_ERR_INVALID;
+  return h->engine->set_stream(static_cast<cudaStream_t>(stream));
+}
+
+int rfmm_get_plan(const rfmm_handle *h, rfmm_plan *out) {
+  if (guard(h) || out == nullptr) return RFMM_ERR_INVALID;
+  const rfmm::SceneDesc &d = h->engine->scene(0);
+  out->particles = d.n;
+  out->depth = d.depth;
+  out->cells = d.cells;
+  out->fixed_point_scale = d.scale;
+  return RFMM_OK;
+}
+
+int rfmm_set_params(rfmm_handle *h, const rfmm_params *params) {
+  if (guard(h) || params == nullptr) return RFMM_ERR_INVALID;
+  const int st = h->engine->set_params(0, *params);
+  if (st == RFMM_OK) h->params = *params;
+  return st;
+}
+
+int rfmm_upload_particles(rfmm_handle *h, const void *host_aos, size_t bytes) {
+  if (guard(h)) return RFMM_ERR_INVALID;
+  int st = h->engine->upload(0, host_aos, bytes, cudaMemcpyHostToDevice);
+  if (st == RFMM_OK) st = h->engine->commit();
+  return st;
+}
+
+int rfmm_upload_particles_device(rfmm_handle *h, const void *device_aos, size_t bytes) {
+  if (guard(h)) return RFMM_ERR_INVALID;
+  int st = h->engine->upload(0, device_aos, bytes, cudaMemcpyDeviceToDevice);
+  if (st == RFMM_OK) st = h->engine->commit();
+  return st;
+}
+
+int rfmm_seed_galaxy(rfmm_handle *h) {
+  if (guard(h)) return RFMM_ERR_INVALID;
+  int st = h->engine->seed_galaxy(0);
+  if (st == RFMM_OK) st = h->engine->commit();
+  return st;
+}
+
+int rfmm_solve_fields(rfmm_handle *h) {
+  if (guard(h)) return RFMM_ERR_INVALID;
+  return h->engine->solve_fields();
+}
+
+int rfmm_step(rfmm_handle *h, uint32_t steps) {
+  if (guard(h)) return RFMM_ERR_INVALID;
+  return h->engine->step(steps);
+}
+
+int rfmm_sync(rfmm_handle *h) {
+  if (guard(h)) return RFMM_ERR_INVALID;
+  return h->engine->sync();
+}
+
+int rfmm_download(rfmm_handle *h, int which, void *host_dst, size_t bytes) {
+  if (guard(h)) return RFMM_ERR_INVALID;
+  return h->engine->download(0, which, host_dst, bytes, cudaMemcpyDeviceToHost);
+}
+
+int rfmm_download_device(rfmm_handle *h, int which, void *device_dst, size_t bytes) {
+  if (guard(h)) return RFMM_ERR_INVALID;
+  return h->engine->download(0, which, device_dst, bytes, cudaMemcpyDeviceToDevice);
+}
+
+int rfmm_digest(rfmm_handle *h, int which, uint32_t *out) {
+  if (guard(h)) return RFMM_ERR_INVALID;
+  return h->engine->digest(0, which, out);
+}
+
+int rfmm_phase_times(rfmm_handle *h, float ms[7]) {
+  if (guard(h)) return RFMM_ERR_INVALID;
+  return h->engine->phase_times(ms);
+}
+
+int rfmm_check_finite(rfmm_handle *h, uint32_t probe, uint32_t *non_finite, float *max_abs) {
+  if (guard(h) || non_finite == nullptr || max_abs == nullptr) return RFMM_ERR_INVALID;
+  const rfmm::SceneDesc &d = h->engine->scene(0);
+  std::vector<float> all((size_t)d.n * 8u);
+  const int st = h->engine->download(0, RFMM_BUF_PARTICLES, all.data(), all.size() * 4u,
+                                     cudaMemcpyDeviceToHost);
+  if (st != RFMM_OK) return st;
+  const size_t count = (size_t)(probe < d.n ? probe : d.n) * 8u;
+  uint32_t bad = 0;
+  float mx = 0.0f;
+  for (size_t i = 0; i < count; i++) {
+    const float f = all[i];
+    if (std::isfinite(f)) {
+      mx = std::fmax(mx, std::fabs(f));
+    } else {
+      bad++;
+    }
+  }
+  *non_finite = bad;
+  *max_abs = mx;
+  return RFMM_OK;
+}
+
+int rfmm_set_resort_interval(rfmm_handle *h, uint32_t steps) {
+  if (guard(h)) return RFMM_ERR_INVALID;
+  return h->engine->set_resort_interval(steps);
+}
+
+int rfmm_device_error(rfmm_handle *h, uint32_t *code, uint32_t *info) {
+  if (guard(h)) return RFMM_ERR_INVALID;
+  return h->engine->device_error(code, info);
+}
+
+}  // extern "C"

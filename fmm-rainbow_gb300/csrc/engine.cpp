@@ -1,0 +1,544 @@
+// Host engine implementation (see engine.h).
+#include "engine.h"
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "rfmm_internal.h"
+
+namespace rfmm {
+
+namespace {
+
+constexpr uint32_t kMaxGraphSteps = 16u;  // steps per captured graph
+constexpr uint32_t kMaxScenes = 1u << 14; // scene rank must fit above the 18 Morton bits
+
+uint32_t pad_tiles(uint32_t n) { return (n + kTile - 1u) / kTile; }
+
+uint32_t log2_ceil(uint32_t v) {
+  uint32_t b = 0;
+  while ((1u << b) < v) ++b;
+  return b;
+}
+
+using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                   const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                   const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn get_encode_tiled() {
+  static EncodeTiledFn fn = nullptr;
+  if (fn == nullptr) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  return fn;
+}
+
+}  // namespace
+
+int cuda_status(cudaError_t e) {
+  if (e == cudaSuccess) return RFMM_OK;
+  if (e == cudaErrorMemoryAllocation) return RFMM_ERR_OOM;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver || e == cudaErrorNoKernelImageForDevice)
+    return RFMM_ERR_NO_DEVICE;
+  return RFMM_ERR_CUDA;
+}
+
+#define RF_CK(call)                                 \
+  do {                                              \
+    cudaError_t e_ = (call);                        \
+    if (e_ != cudaSuccess) return cuda_status(e_);  \
+  } while (0)
+
+const char *status_string(int status) {
+  switch (status) {
+    case RFMM_OK: return "ok";
+    case RFMM_ERR_INVALID: return "invalid argument";
+    case RFMM_ERR_CUDA: return "CUDA runtime error";
+    case RFMM_ERR_OOM: return "device memory exhausted";
+    case RFMM_ERR_STATE: return "call out of order";
+    case RFMM_ERR_TIMEOUT: return "kernel wait timed out";
+    case RFMM_ERR_NO_DEVICE: return "no sm_103 CUDA device";
+    case RFMM_ERR_DEVICE: return "kernel reported an error";
+    case RFMM_ERR_BUDGET: return "request exceeds the memory budget";
+    default: return "unknown status";
+  }
+}
+
+int Engine::alloc(void **p, size_t bytes) {
+  bytes = std::max<size_t>(bytes, 256);
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    return cuda_status(e);
+  }
+  allocations_.push_back(*p);
+  device_bytes_ += bytes;
+  return RFMM_OK;
+}
+
+int Engine::create(const std::vector<SceneSpec> &specs, Engine **out) {
+  if (out == nullptr || specs.empty() || specs.size() > kMaxScenes) return RFMM_ERR_INVALID;
+  *out = nullptr;
+  for (const SceneSpec &s : specs) {
+    if (s.n == 0u || s.n > (1u << 23)) return RFMM_ERR_INVALID;
+    if (s.params.depth != 0u && (s.params.depth < 4u || s.params.depth > 6u)) return RFMM_ERR_INVALID;
+    if (!(s.params.fixed_point_scale >= 0.0f)) return RFMM_ERR_INVALID;
+  }
+  int dev = 0;
+  RF_CK(cudaGetDevice(&dev));
+  cudaDeviceProp prop;
+  RF_CK(cudaGetDeviceProperties(&prop, dev));
+  if (prop.major != 10 || prop.minor != 3) return RFMM_ERR_NO_DEVICE;
+  if (get_encode_tiled() == nullptr) return RFMM_ERR_NO_DEVICE;
+
+  Engine *E = new Engine();
+  E->device_ = dev;
+  E->sms_ = prop.multiProcessorCount;
+  uint32_t body_off = 0, cell_off = 0, task_off = 0;
+  for (uint32_t i = 0; i < specs.size(); ++i) {
+    const SceneSpec &sp = specs[i];
+    SceneDesc d{};
+    d.n = sp.n;
+    d.depth = sp.params.depth ? sp.params.depth : depth_for_particles(sp.n);
+    d.body_off = body_off;
+    d.tile_off = body_off / kTile;
+    d.cell_off = cell_off;
+    d.cells = total_cells(d.depth);
+    d.sub_level = d.depth - 3u;
+    d.task_off = task_off;
+    d.scale = sp.params.fixed_point_scale > 0.0f ? sp.params.fixed_point_scale : fixed_point_scale(sp.n);
+    d.gravity = sp.params.gravity;
+    d.softening = sp.params.softening;
+    d.dt_eff = sp.params.dt * sp.params.speed;
+    d.n_f = (float)sp.n;
+    d.control_strength = sp.params.control_strength;
+    d.control_radius = sp.params.control_radius;
+    d.key_base = i << 18;
+    for (int k = 0; k < 4; k++) {
+      d.control_point[k] = sp.params.control_point[k];
+      d.control_axis_mode[k] = sp.params.control_axis_mode[k];
+    }
+    const uint32_t tiles = pad_tiles(sp.n);
+    for (uint32_t t = 0; t < tiles; t++) E->tile_scene_h_.push_back(i);
+    const uint32_t ntasks = 1u << (3u * d.sub_level);
+    for (uint32_t t = 0; t < ntasks; t++) E->task_scene_h_.push_back(i);
+    E->plist_cap_ += total_cells(d.depth - 1u);
+    body_off += tiles * kTile;
+    cell_off += d.cells;
+    task_off += ntasks;
+    E->scenes_.push_back(d);
+  }
+  E->slots_ = body_off;
+  E->tiles_ = body_off / kTile;
+  E->cells_ = cell_off;
+  E->tasks_ = task_off;
+  E->key_bits_ = 18u + log2_ceil((uint32_t)specs.size());
+  E->uploaded_.assign(specs.size(), false);
+
+  int st = RFMM_OK;
+  auto A = [&](void **p, size_t bytes) {
+    if (st == RFMM_OK) st = E->alloc(p, bytes);
+  };
+  const size_t S = E->slots_, C = E->cells_;
+  A((void **)&E->d_scenes_, sizeof(SceneDesc) * specs.size());
+  A((void **)&E->d_tile_scene_, 4 * E->tiles_);
+  A((void **)&E->d_task_scene_, 4 * E->tasks_);
+  for (int b = 0; b < 2; b++) {
+    A((void **)&E->d_part_[b], 32 * S);
+    A((void **)&E->d_ids_[b], 4 * S);
+    A((void **)&E->d_mom_[b], 16 * C);
+    A((void **)&E->d_plist_[b], sizeof(WorkItem) * E->plist_cap_);
+    A((void **)&E->sort_.keys[b], 4 * S);
+    A((void **)&E->sort_.vals[b], 4 * S);
+  }
+  A((void **)&E->d_src_, 16 * C);
+  A((void **)&E->d_lfield_, 48 * C);
+  A((void **)&E->d_fields_, 48 * C);
+  A((void **)&E->d_ctr_, sizeof(Counters));
+  A((void **)&E->d_tickets_, 4 * specs.size());
+  A((void **)&E->d_tmaps_, sizeof(CUtensorMap) * 8 * specs.size());
+  A((void **)&E->sort_.hist, 4 * 256 * (size_t)sort_tiles(E->slots_));
+  A((void **)&E->sort_.totals, 4 * 256);
+  E->sort_.capacity = E->slots_;
+  if (st != RFMM_OK) {
+    delete E;
+    return st;
+  }
+  cudaError_t e = cudaStreamCreateWithFlags(&E->own_stream_, cudaStreamNonBlocking);
+  if (e == cudaSuccess) {
+    E->stream_ = E->own_stream_;
+    for (auto &ev : E->ev_)
+      if (e == cudaSuccess) e = cudaEventCreate(&ev);
+  }
+  if (e == cudaSuccess) e = configure_tree_kernels();
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(E->d_scenes_, E->scenes_.data(), sizeof(SceneDesc) * specs.size(),
+                        cudaMemcpyHostToDevice, E->stream_);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(E->d_tile_scene_, E->tile_scene_h_.data(), 4 * E->tiles_,
+                        cudaMemcpyHostToDevice, E->stream_);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(E->d_task_scene_, E->task_scene_h_.data(), 4 * E->tasks_,
+                        cudaMemcpyHostToDevice, E->stream_);
+  for (int b = 0; b < 2 && e == cudaSuccess; b++) {
+    e = cudaMemsetAsync(E->d_part_[b], 0, 32 * S, E->stream_);
+    if (e == cudaSuccess) e = cudaMemsetAsync(E->d_mom_[b], 0, 16 * C, E->stream_);
+    if (e == cudaSuccess) e = cudaMemsetAsync(E->d_ids_[b], 0, 4 * S, E->stream_);
+  }
+  if (e == cudaSuccess) e = cudaMemsetAsync(E->d_src_, 0, 16 * C, E->stream_);
+  if (e == cudaSuccess) e = cudaMemsetAsync(E->d_lfield_, 0, 48 * C, E->stream_);
+  if (e == cudaSuccess) e = cudaMemsetAsync(E->d_fields_, 0, 48 * C, E->stream_);
+  if (e == cudaSuccess) e = cudaMemsetAsync(E->d_ctr_, 0, sizeof(Counters), E->stream_);
+  if (e == cudaSuccess) e = cudaMemsetAsync(E->d_tickets_, 0, 4 * specs.size(), E->stream_);
+  if (e != cudaSuccess) {
+    delete E;
+    return cuda_status(e);
+  }
+  st = E->build_tensor_maps();
+  if (st == RFMM_OK) st = cuda_status(cudaStreamSynchronize(E->stream_));
+  if (st != RFMM_OK) {
+    delete E;
+    return st;
+  }
+  *out = E;
+  return RFMM_OK;
+}
+
+int Engine::build_tensor_maps() {
+  EncodeTiledFn encode = get_encode_tiled();
+  std::vector<CUtensorMap> maps(8 * scenes_.size());
+  std::memset(maps.data(), 0, sizeof(CUtensorMap) * maps.size());
+  for (uint32_t s = 0; s < scenes_.size(); s++) {
+    const SceneDesc &d = scenes_[s];
+    for (uint32_t l = 3; l <= d.depth; l++) {
+      const uint64_t dim = 1ull << l;
+      void *base = reinterpret_cast<char *>(d_src_) + 16ull * (d.cell_off + level_offset(l));
+      const cuuint64_t gdim[3] = {4 * dim, dim, dim};
+      const cuuint64_t gstride[2] = {16 * dim, 16 * dim * dim};
+      const cuuint32_t box[3] = {24, 6, 6};
+      const cuuint32_t estride[3] = {1, 1, 1};
+      CUresult r = encode(&maps[8 * s + l], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, gdim, gstride,
+                          box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+      if (r != CUDA_SUCCESS) return RFMM_ERR_CUDA;
+    }
+  }
+  RF_CK(cudaMemcpyAsync(d_tmaps_, maps.data(), sizeof(CUtensorMap) * maps.size(),
+                        cudaMemcpyHostToDevice, stream_));
+  return RFMM_OK;
+}
+
+Engine::~Engine() {
+  if (stream_ != nullptr) cudaStreamSynchronize(stream_);
+  for (auto &kv : graphs_) cudaGraphExecDestroy(kv.second);
+  for (auto &ev : ev_)
+    if (ev != nullptr) cudaEventDestroy(ev);
+  for (void *p : allocations_) cudaFree(p);
+  if (own_stream_ != nullptr) cudaStreamDestroy(own_stream_);
+}
+
+int Engine::set_stream(cudaStream_t s) {
+  RF_CK(cudaStreamSynchronize(stream_));
+  stream_ = s != nullptr ? s : own_stream_;
+  return RFMM_OK;
+}
+
+int Engine::set_params(uint32_t scene, const rfmm_params &p) {
+  if (scene >= scenes_.size()) return RFMM_ERR_INVALID;
+  SceneDesc &d = scenes_[scene];
+  if (p.depth != 0u && p.depth != d.depth) return RFMM_ERR_INVALID;
+  if (p.fixed_point_scale != 0.0f && p.fixed_point_scale != d.scale) return RFMM_ERR_INVALID;
+  d.gravity = p.gravity;
+  d.softening = p.softening;
+  d.dt_eff = p.dt * p.speed;
+  d.control_strength = p.control_strength;
+  d.control_radius = p.control_radius;
+  for (int k = 0; k < 4; k++) {
+    d.control_point[k] = p.control_point[k];
+    d.control_axis_mode[k] = p.control_axis_mode[k];
+  }
+  // Kernels read the scene table from device memory, so captured graphs stay valid.
+  RF_CK(cudaMemcpyAsync(d_scenes_ + scene, &d, sizeof(SceneDesc), cudaMemcpyHostToDevice, stream_));
+  RF_CK(cudaStreamSynchronize(stream_));
+  return RFMM_OK;
+}
+
+int Engine::set_resort_interval(uint32_t steps) {
+  resort_interval_ = steps;
+  since_sort_ = 0;
+  return RFMM_OK;
+}
+
+LaunchCtx Engine::ctx(uint32_t mpar, uint32_t lpar, uint32_t ppar) const {
+  LaunchCtx L;
+  L.stream = stream_;
+  L.scenes = d_scenes_;
+  L.tile_scene = d_tile_scene_;
+  L.task_scene = d_task_scene_;
+  L.part = d_part_[ppar];
+  L.mom = d_mom_[mpar];
+  L.mom_next = d_mom_[mpar ^ 1u];
+  L.src = d_src_;
+  L.lfield = d_lfield_;
+  L.fields = d_fields_;
+  L.plist = d_plist_[lpar];
+  L.plist_prev = d_plist_[lpar ^ 1u];
+  L.plist_cap = plist_cap_;
+  L.ctr = d_ctr_;
+  L.tickets = d_tickets_;
+  L.tmaps = d_tmaps_;
+  return L;
+}
+
+int Engine::upload(uint32_t scene, const void *src, size_t bytes, cudaMemcpyKind kind) {
+  if (scene >= scenes_.size() || src == nullptr) return RFMM_ERR_INVALID;
+  const SceneDesc &d = scenes_[scene];
+  if (bytes != 32ull * d.n) return RFMM_ERR_INVALID;
+  RF_CK(cudaMemcpyAsync(d_part_[pcur_] + 2ull * d.body_off, src, bytes, kind, stream_));
+  launch_iota(stream_, d_ids_[pcur_] + d.body_off, pad_tiles(d.n) * kTile);
+  RF_CK(cudaGetLastError());
+  uploaded_[scene] = true;
+  committed_ = false;
+  return RFMM_OK;
+}
+
+int Engine::seed_galaxy(uint32_t scene) {
+  if (scene >= scenes_.size()) return RFMM_ERR_INVALID;
+  const SceneDesc &d = scenes_[scene];
+  LaunchCtx L = ctx(mcur_, lpar_, pcur_);
+  launch_initialize(L, d_part_[pcur_], d.tile_off, pad_tiles(d.n));
+  launch_iota(stream_, d_ids_[pcur_] + d.body_off, pad_tiles(d.n) * kTile);
+  RF_CK(cudaGetLastError());
+  uploaded_[scene] = true;
+  committed_ = false;
+  return RFMM_OK;
+}
+
+void Engine::enqueue_resort(uint32_t ppar) {
+  LaunchCtx L = ctx(mcur_, lpar_, ppar);
+  launch_keys(L, sort_.keys[0], sort_.vals[0], nullptr, 0, tiles_);
+  const int r = radix_sort(stream_, sort_, slots_, key_bits_);
+  launch_gather(L, sort_.vals[r], d_part_[ppar], d_ids_[ppar], d_part_[ppar ^ 1u], d_ids_[ppar ^ 1u],
+                nullptr, tiles_);
+}
+
+int Engine::commit() {
+  for (bool u : uploaded_)
+    if (!u) return RFMM_ERR_STATE;
+  LaunchCtx L = ctx(mcur_, lpar_, pcur_);
+  launch_keys(L, sort_.keys[0], sort_.vals[0], nullptr, 0, tiles_);
+  const int r = radix_sort(stream_, sort_, slots_, key_bits_);
+  RF_CK(cudaMemsetAsync(d_mom_[mcur_], 0, 16ull * cells_, stream_));
+  launch_gather(L, sort_.vals[r], d_part_[pcur_], d_ids_[pcur_], d_part_[pcur_ ^ 1u],
+                d_ids_[pcur_ ^ 1u], d_mom_[mcur_], tiles_);
+  RF_CK(cudaGetLastError());
+  pcur_ ^= 1u;
+  committed_ = true;
+  solved_ = false;
+  tree_buf_ = -1;
+  since_sort_ = 0;
+  return RFMM_OK;
+}
+
+void Engine::enqueue_step(uint32_t mpar, uint32_t lpar, uint32_t ppar) {
+  LaunchCtx L = ctx(mpar, lpar, ppar);
+  launch_upward(L, lpar, tasks_);
+  launch_m2l(L, lpar, (uint32_t)sms_ * 3u);
+  launch_l2l_near(L, lpar, (uint32_t)sms_ * 8u);
+  launch_integrate(L, tiles_);
+}
+
+int Engine::solve_fields() {
+  if (!committed_) return RFMM_ERR_STATE;
+  LaunchCtx L = ctx(mcur_, lpar_, pcur_);
+  launch_upward(L, lpar_, tasks_);
+  launch_m2l(L, lpar_, (uint32_t)sms_ * 3u);
+  launch_l2l_near(L, lpar_, (uint32_t)sms_ * 8u);
+  RF_CK(cudaGetLastError());
+  lpar_ ^= 1u;
+  tree_buf_ = (int)mcur_;
+  solved_ = true;
+  return RFMM_OK;
+}
+
+int Engine::launch_chunk(uint32_t len, bool sort_at_end) {
+  const auto key = std::make_tuple(len, mcur_, lpar_, pcur_, sort_at_end);
+  auto it = graphs_.find(key);
+  if (it == graphs_.end()) {
+    cudaGraph_t g = nullptr;
+    RF_CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+    for (uint32_t j = 0; j < len; j++) enqueue_step(mcur_ ^ (j & 1u), lpar_ ^ (j & 1u), pcur_);
+    if (sort_at_end) enqueue_resort(pcur_);
+    cudaError_t e = cudaStreamEndCapture(stream_, &g);
+    if (e != cudaSuccess) {
+      if (g != nullptr) cudaGraphDestroy(g);
+      return cuda_status(e);
+    }
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_status(e);
+    it = graphs_.emplace(key, exec).first;
+  }
+  RF_CK(cudaGraphLaunch(it->second, stream_));
+  const uint32_t flip = len & 1u;
+  tree_buf_ = (int)(mcur_ ^ ((len - 1u) & 1u));
+  mcur_ ^= flip;
+  lpar_ ^= flip;
+  if (sort_at_end) pcur_ ^= 1u;
+  return RFMM_OK;
+}
+
+int Engine::step(uint32_t steps) {
+  if (!committed_) return RFMM_ERR_STATE;
+  while (steps > 0) {
+    if (resort_interval_ > 0 && since_sort_ >= resort_interval_) {
+      enqueue_resort(pcur_);
+      RF_CK(cudaGetLastError());
+      pcur_ ^= 1u;
+      since_sort_ = 0;
+    }
+    uint32_t len = std::min(steps, kMaxGraphSteps);
+    bool sort_at_end = false;
+    if (resort_interval_ > 0) {
+      const uint32_t until = resort_interval_ - since_sort_;
+      if (len >= until) {
+        len = until;
+        sort_at_end = true;
+      }
+    }
+    const int st = launch_chunk(len, sort_at_end);
+    if (st != RFMM_OK) return st;
+    since_sort_ = sort_at_end ? 0u : since_sort_ + len;
+    steps -= len;
+  }
+  solved_ = true;
+  return RFMM_OK;
+}
+
+int Engine::check_device_error() {
+  Counters c;
+  RF_CK(cudaMemcpyAsync(&c, d_ctr_, sizeof(Counters), cudaMemcpyDeviceToHost, stream_));
+  RF_CK(cudaStreamSynchronize(stream_));
+  if (c.error == kDevErrTmaTimeout) return RFMM_ERR_TIMEOUT;
+  if (c.error != 0u) return RFMM_ERR_DEVICE;
+  return RFMM_OK;
+}
+
+int Engine::sync() {
+  RF_CK(cudaStreamSynchronize(stream_));
+  return check_device_error();
+}
+
+int Engine::device_error(uint32_t *code, uint32_t *info) {
+  Counters c;
+  RF_CK(cudaMemcpyAsync(&c, d_ctr_, sizeof(Counters), cudaMemcpyDeviceToHost, stream_));
+  RF_CK(cudaStreamSynchronize(stream_));
+  if (code) *code = c.error;
+  if (info) *info = c.error_info;
+  return RFMM_OK;
+}
+
+size_t Engine::buffer_bytes(uint32_t scene, int which) const {
+  const SceneDesc &d = scenes_[scene];
+  switch (which) {
+    case RFMM_BUF_PARTICLES: return 32ull * d.n;
+    case RFMM_BUF_MOMENTS: return 16ull * d.cells;
+    case RFMM_BUF_FIELDS: return 48ull * d.cells;
+    default: return 0;
+  }
+}
+
+int Engine::download(uint32_t scene, int which, void *dst, size_t bytes, cudaMemcpyKind kind) {
+  if (scene >= scenes_.size() || dst == nullptr) return RFMM_ERR_INVALID;
+  const size_t need = buffer_bytes(scene, which);
+  if (need == 0 || bytes != need) return RFMM_ERR_INVALID;
+  const SceneDesc &d = scenes_[scene];
+  const void *from = nullptr;
+  if (which == RFMM_BUF_PARTICLES) {
+    if (!committed_) return RFMM_ERR_STATE;
+    LaunchCtx L = ctx(mcur_, lpar_, pcur_);
+    launch_unpermute(L, d_ids_[pcur_], d_part_[pcur_ ^ 1u], d.tile_off, pad_tiles(d.n));
+    RF_CK(cudaGetLastError());
+    from = d_part_[pcur_ ^ 1u] + 2ull * d.body_off;
+  } else if (which == RFMM_BUF_MOMENTS) {
+    if (tree_buf_ < 0) return RFMM_ERR_STATE;
+    from = d_mom_[tree_buf_] + d.cell_off;
+  } else {
+    if (!solved_) return RFMM_ERR_STATE;
+    from = d_fields_ + 12ull * d.cell_off;
+  }
+  RF_CK(cudaMemcpyAsync(dst, from, bytes, kind, stream_));
+  return sync();
+}
+
+int Engine::digest(uint32_t scene, int which, uint32_t *out) {
+  if (scene >= scenes_.size() || out == nullptr) return RFMM_ERR_INVALID;
+  const size_t bytes = buffer_bytes(scene, which);
+  if (bytes == 0) return RFMM_ERR_INVALID;
+  std::vector<uint8_t> host(bytes);
+  const int st = download(scene, which, host.data(), bytes, cudaMemcpyDeviceToHost);
+  if (st != RFMM_OK) return st;
+  uint32_t h = 2166136261u;  // FNV-1a, native/main.rs:152-163
+  for (uint8_t b : host) {
+    h ^= b;
+    h *= 16777619u;
+  }
+  *out = h;
+  return RFMM_OK;
+}
+
+int Engine::phase_times(float ms[7]) {
+  if (!committed_ || ms == nullptr) return RFMM_ERR_INVALID;
+  if (d_mom_scratch_ == nullptr) {
+    const int st = alloc((void **)&d_mom_scratch_, 16ull * cells_);
+    if (st != RFMM_OK) return st;
+  }
+  LaunchCtx L = ctx(mcur_, lpar_, pcur_);
+  // Standalone P2M on a scratch tree, timed for the phase breakdown only.
+  RF_CK(cudaMemsetAsync(d_mom_scratch_, 0, 16ull * cells_, stream_));
+  RF_CK(cudaEventRecord(ev_[5], stream_));
+  launch_deposit(L, d_mom_scratch_, tiles_);
+  RF_CK(cudaEventRecord(ev_[6], stream_));
+  // One instrumented frame.
+  RF_CK(cudaEventRecord(ev_[0], stream_));
+  launch_upward(L, lpar_, tasks_);
+  RF_CK(cudaEventRecord(ev_[1], stream_));
+  launch_m2l(L, lpar_, (uint32_t)sms_ * 3u);
+  RF_CK(cudaEventRecord(ev_[2], stream_));
+  launch_l2l_near(L, lpar_, (uint32_t)sms_ * 8u);
+  RF_CK(cudaEventRecord(ev_[3], stream_));
+  launch_integrate(L, tiles_);
+  RF_CK(cudaEventRecord(ev_[4], stream_));
+  RF_CK(cudaGetLastError());
+  tree_buf_ = (int)mcur_;
+  mcur_ ^= 1u;
+  lpar_ ^= 1u;
+  solved_ = true;
+  since_sort_++;
+  const int st = sync();
+  if (st != RFMM_OK) return st;
+  float t[5];
+  RF_CK(cudaEventElapsedTime(&t[0], ev_[5], ev_[6]));
+  RF_CK(cudaEventElapsedTime(&t[1], ev_[0], ev_[1]));
+  RF_CK(cudaEventElapsedTime(&t[2], ev_[1], ev_[2]));
+  RF_CK(cudaEventElapsedTime(&t[3], ev_[2], ev_[3]));
+  RF_CK(cudaEventElapsedTime(&t[4], ev_[3], ev_[4]));
+  ms[0] = 0.0f;   // clear: folded into upward
+  ms[1] = t[0];   // deposit (standalone P2M; fused into integrate in the step)
+  ms[2] = t[1];   // upward
+  ms[3] = t[2];   // m2l
+  ms[4] = t[3];   // downward (L2L fused with near)
+  ms[5] = 0.0f;   // near: fused into downward
+  ms[6] = t[4];   // integrate (+ next deposit)
+  return RFMM_OK;
+}
+
+}  // namespace rfmm

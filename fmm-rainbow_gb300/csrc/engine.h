@@ -1,0 +1,116 @@
+// Host engine: device buffers, scene table, step sequencing and CUDA graphs
+// for one or more independent scenes on one GPU.
+//
+// A plain solve is an engine with one scene; the batched form packs many
+// scenes into the same buffers so every kernel covers all of them in one
+// launch (per-scene slot ranges aligned to body tiles, per-scene tree cell
+// ranges, and one parent work list shared by all scenes).
+#pragma once
+
+#include <cstdint>
+#include <map>
+#include <tuple>
+#include <vector>
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include "rfmm.h"
+#include "rfmm_kernels.h"
+#include "rfmm_shared.h"
+
+namespace rfmm {
+
+struct SceneSpec {
+  uint32_t n;
+  rfmm_params params;
+};
+
+class Engine {
+ public:
+  // Allocates every buffer for `specs`; returns an RFMM status.
+  static int create(const std::vector<SceneSpec> &specs, Engine **out);
+  ~Engine();
+
+  int set_stream(cudaStream_t s);
+  cudaStream_t stream() const { return stream_; }
+  int set_params(uint32_t scene, const rfmm_params &p);
+  int set_resort_interval(uint32_t steps);
+
+  // Copy a scene's bodies (caller order) into the resident buffer; the new
+  // bodies take effect at the next commit().
+  int upload(uint32_t scene, const void *src, size_t bytes, cudaMemcpyKind kind);
+  int seed_galaxy(uint32_t scene);
+  // Sort every scene into leaf order and deposit the leaf moments.
+  int commit();
+
+  int solve_fields();
+  int step(uint32_t steps);
+  int sync();
+
+  int download(uint32_t scene, int which, void *dst, size_t bytes, cudaMemcpyKind kind);
+  int digest(uint32_t scene, int which, uint32_t *out);
+  int phase_times(float ms[7]);
+  int device_error(uint32_t *code, uint32_t *info);
+
+  uint32_t num_scenes() const { return (uint32_t)scenes_.size(); }
+  const SceneDesc &scene(uint32_t s) const { return scenes_[s]; }
+  size_t buffer_bytes(uint32_t scene, int which) const;
+  size_t device_bytes() const { return device_bytes_; }
+  uint32_t kernels_per_step() const { return 4u; }
+  uint32_t total_tiles() const { return tiles_; }
+
+ private:
+  Engine() = default;
+  int alloc(void **p, size_t bytes);
+  int build_tensor_maps();
+  LaunchCtx ctx(uint32_t mpar, uint32_t lpar, uint32_t ppar) const;
+  void enqueue_step(uint32_t mpar, uint32_t lpar, uint32_t ppar);
+  void enqueue_resort(uint32_t ppar);
+  int launch_chunk(uint32_t len, bool sort_at_end);
+  int check_device_error();
+
+  int device_ = 0;
+  int sms_ = 0;
+  cudaStream_t stream_ = nullptr;
+  cudaStream_t own_stream_ = nullptr;
+
+  std::vector<SceneDesc> scenes_;
+  std::vector<uint32_t> tile_scene_h_;
+  std::vector<uint32_t> task_scene_h_;
+  uint32_t slots_ = 0, tiles_ = 0, cells_ = 0, tasks_ = 0, plist_cap_ = 0, key_bits_ = 18;
+
+  SceneDesc *d_scenes_ = nullptr;
+  uint32_t *d_tile_scene_ = nullptr, *d_task_scene_ = nullptr;
+  float4 *d_part_[2] = {nullptr, nullptr};
+  uint32_t *d_ids_[2] = {nullptr, nullptr};
+  uint4 *d_mom_[2] = {nullptr, nullptr};
+  uint4 *d_mom_scratch_ = nullptr;
+  float4 *d_src_ = nullptr;
+  float *d_lfield_ = nullptr, *d_fields_ = nullptr;
+  WorkItem *d_plist_[2] = {nullptr, nullptr};
+  Counters *d_ctr_ = nullptr;
+  uint32_t *d_tickets_ = nullptr;
+  CUtensorMap *d_tmaps_ = nullptr;
+  SortScratch sort_{};
+  std::vector<void *> allocations_;
+  size_t device_bytes_ = 0;
+
+  // Host-side sequencing state.
+  uint32_t pcur_ = 0;    // particle buffer holding the resident bodies
+  uint32_t mcur_ = 0;    // moment buffer whose leaf level holds the current deposit
+  uint32_t lpar_ = 0;    // parent list to write next
+  int tree_buf_ = -1;    // moment buffer holding the last complete tree
+  bool committed_ = false;
+  bool solved_ = false;  // fields hold a solution
+  uint32_t resort_interval_ = 16, since_sort_ = 0;
+  std::vector<bool> uploaded_;
+
+  std::map<std::tuple<uint32_t, uint32_t, uint32_t, uint32_t, bool>, cudaGraphExec_t> graphs_;
+  cudaEvent_t ev_[8] = {};
+};
+
+const char *status_string(int status);
+int cuda_status(cudaError_t e);
+
+}  // namespace rfmm

@@ -1,0 +1,447 @@
+// Body passes: integrate (L2P + self leaf + kick/drift) fused with the next
+// step's deposit, the sort-key and gather passes that keep bodies resident in
+// leaf (Morton) order, the standalone deposit, and the galaxy seed.
+//
+// Reference passes (iskamag/fmm-rainbow src/rainbow_fmm.wgsl):
+//   deposit     408-422   leaf cell + i32(round(pos * scale)) atomics
+//   integrate   613-771   adaptive descent, local expansion, self leaf,
+//                         control field, symplectic Euler, soft wall, hue
+//   initialize  232-374   seeded galaxy
+//
+// Bodies live in HBM in leaf-key order (a permutation of the caller's order,
+// undone on download).  Every result is independent of that order: each
+// body's update reads only its own state and the tree, and the moment sums
+// are exact integers.  Sorted order makes a warp's bodies share leaves, so
+// the tree gathers broadcast and the deposit is one reduction per run.
+#include <cuda_runtime.h>
+
+#include "rfmm_device.cuh"
+#include "rfmm_kernels.h"
+
+namespace rfmm {
+
+// Leaf (level `depth`) cell of a position, local to the scene's tree.
+__device__ __forceinline__ uint32_t leaf_cell(float x, float y, float z, uint32_t depth) {
+  const uint32_t dim = 1u << depth;
+  return level_offset_d(depth) + lin3(cell_of_unit(unit_coord(x), dim), cell_of_unit(unit_coord(y), dim),
+                                      cell_of_unit(unit_coord(z), dim), dim);
+}
+
+__device__ __forceinline__ float length3(float x, float y, float z) {
+  return sqrtf((x * x + y * y) + z * z);
+}
+
+// Soft absorbing band and last-resort clamp for one axis (wgsl:740-751).
+__device__ __forceinline__ void soft_wall(float &p, float &v, float world_edge, float edge_band) {
+  const float over = fabsf(p) - (world_edge - edge_band);
+  if (over > 0.0f) {
+    const float absorb = clampf_d(over / edge_band, 0.0f, 1.0f);
+    v = v * (1.0f - absorb * 0.16f);
+  }
+  if (fabsf(p) > world_edge) {
+    p = clampf_d(p, -world_edge, world_edge);
+    v = v * -0.55f;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_integrate(const SceneDesc *__restrict__ scenes,
+                                                   const uint32_t *__restrict__ tile_scene,
+                                                   float4 *__restrict__ part,
+                                                   const uint4 *__restrict__ mom,
+                                                   const float4 *__restrict__ src,
+                                                   const float *__restrict__ fields,
+                                                   uint4 *__restrict__ mom_next) {
+  const uint32_t tile = blockIdx.x;
+  const SceneDesc &S = scenes[tile_scene[tile]];
+  const uint32_t slot = tile * kTile + threadIdx.x;
+  const bool active = slot - S.body_off < S.n;
+  uint32_t key = 0xFFFFFFFFu;
+  int32_t qx = 0, qy = 0, qz = 0;
+  if (active) {
+    const float4 p0 = part[2u * slot], p1 = part[2u * slot + 1u];
+    float px = p0.x, py = p0.y, pz = p0.z;
+    float vx = p1.x, vy = p1.y, vz = p1.z;
+    const uint32_t D = S.depth;
+    const float ux = unit_coord(px), uy = unit_coord(py), uz = unit_coord(pz);
+
+    // Adaptive descent (wgsl:625-639): first level whose cell holds at most
+    // 16 bodies, else the leaf level.  The level loads are independent.
+    uint32_t chosen = D, cell_index = 0u, count = 0u;
+#pragma unroll
+    for (uint32_t l = 6u; l >= 1u; l--) {
+      if (l <= D) {
+        const uint32_t dim = 1u << l;
+        const uint32_t idx = S.cell_off + level_offset_d(l) +
+                             lin3(cell_of_unit(ux, dim), cell_of_unit(uy, dim), cell_of_unit(uz, dim), dim);
+        const uint32_t c = __ldg(&mom[idx].x);
+        if ((int32_t)c <= (int32_t)kAdaptive || l == D) {
+          chosen = l;
+          cell_index = idx;
+          count = c;
+        }
+      }
+    }
+    const uint32_t cdim = 1u << chosen;
+    const float cx = cell_center_axis(cell_of_unit(ux, cdim), cdim);
+    const float cy = cell_center_axis(cell_of_unit(uy, cdim), cdim);
+    const float cz = cell_center_axis(cell_of_unit(uz, cdim), cdim);
+
+    const float4 *fp = reinterpret_cast<const float4 *>(fields + (size_t)cell_index * 12u);
+    const float4 fa = __ldg(fp), fj0 = __ldg(fp + 1), fj1 = __ldg(fp + 2);
+    const float rx = px - cx, ry = py - cy, rz = pz - cz;
+    float ax = fa.x + (fj0.x * rx + fj0.y * ry + fj0.z * rz);
+    float ay = fa.y + (fj0.y * rx + fj0.w * ry + fj1.x * rz);
+    float az = fa.z + (fj0.z * rx + fj1.x * ry + fj1.y * rz);
+
+    // Self leaf: softened monopole of the other count-1 bodies (wgsl:646-657).
+    if (count > 1u) {
+      const float4 s = __ldg(&src[cell_index]);
+      const float dx = s.x - px, dy = s.y - py, dz = s.z - pz;
+      const float eps = fmaxf(S.softening, 0.62f * kHalf / (float)cdim);
+      const float inv_r = 1.0f / sqrtf((dx * dx + dy * dy) + dz * dz + eps * eps);
+      const float self_mass = (float)(count - 1u) / S.n_f;
+      const float gsm = S.gravity * self_mass;
+      ax = ax + gsm * dx * inv_r * inv_r * inv_r;
+      ay = ay + gsm * dy * inv_r * inv_r * inv_r;
+      az = az + gsm * dz * inv_r * inv_r * inv_r;
+    }
+
+    // Interactive control field (wgsl:659-689); off unless control_point.w > 0.5.
+    float control_influence = 0.0f;
+    if (S.control_point[3] > 0.5f) {
+      const float cdx = S.control_point[0] - px, cdy = S.control_point[1] - py,
+                  cdz = S.control_point[2] - pz;
+      const float d2 = (cdx * cdx + cdy * cdy) + cdz * cdz;
+      const float cr = fmaxf(S.control_radius, 0.02f);
+      control_influence = expf(-2.0f * d2 / (cr * cr));
+      const float strength = S.control_strength;
+      const float inv = 1.0f / sqrtf(d2 + cr * cr * 0.018f);
+      const float dirx = cdx * inv, diry = cdy * inv, dirz = cdz * inv;
+      const float mode = S.control_axis_mode[3];
+      if (mode < 1.5f) {
+        ax = ax + dirx * strength * control_influence;
+        ay = ay + diry * strength * control_influence;
+        az = az + dirz * strength * control_influence;
+      } else if (mode < 2.5f) {
+        ax = ax - dirx * strength * control_influence;
+        ay = ay - diry * strength * control_influence;
+        az = az - dirz * strength * control_influence;
+      } else {
+        const float al = length3(S.control_axis_mode[0], S.control_axis_mode[1], S.control_axis_mode[2]);
+        const float nx = S.control_axis_mode[0] / al, ny = S.control_axis_mode[1] / al,
+                    nz = S.control_axis_mode[2] / al;
+        const float tx = ny * cdz - nz * cdy, ty = nz * cdx - nx * cdz, tz = nx * cdy - ny * cdx;
+        const float tl = length3(tx, ty, tz);
+        if (tl > 0.00001f) {
+          ax = ax + tx / tl * strength * control_influence;
+          ay = ay + ty / tl * strength * control_influence;
+          az = az + tz / tl * strength * control_influence;
+        }
+      }
+    }
+
+    // Symplectic Euler with excitation and hue state (wgsl:691-769).
+    const float dt = S.dt_eff;
+    const float radius = fmaxf(length3(px, py, pz), 0.0001f);
+    const float vlen = fmaxf(length3(vx, vy, vz), 0.0001f);
+    const float pv = (px * vx + py * vy) + pz * vz;
+    const float signed_radial = clampf_d(pv / (radius * vlen), -1.0f, 1.0f);
+    const float rf = fabsf(signed_radial);
+    const float radial_shock = rf * rf * rf;
+    const float density_pulse = clampf_d(((float)count - (float)kAdaptive) / 72.0f, 0.0f, 1.0f);
+    const float field_strength = clampf_d(length3(ax, ay, az) * (radius + 0.12f) * 0.58f, 0.0f, 1.0f);
+    const float target_exc = clampf_d(0.025f + radial_shock * 0.56f + density_pulse * 0.26f +
+                                          field_strength * 0.13f + control_influence * 0.42f,
+                                      0.0f, 1.0f);
+    float exc = p1.w;
+    const float response = target_exc > exc ? 10.0f : 1.05f;
+    const float t = clampf_d(dt * response, 0.0f, 1.0f);
+    exc = exc * (1.0f - t) + target_exc * t;
+
+    vx = vx + ax * dt;
+    vy = vy + ay * dt;
+    vz = vz + az * dt;
+    px = px + vx * dt;
+    py = py + vy * dt;
+    pz = pz + vz * dt;
+
+    const float world_edge = kHalf * 0.985f;
+    const float edge_band = 0.12f * kHalf;
+    soft_wall(px, vx, world_edge, edge_band);
+    soft_wall(py, vy, world_edge, edge_band);
+    soft_wall(pz, vz, world_edge, edge_band);
+    const float st = clampf_d((exc - 0.30f) / (0.70f - 0.30f), 0.0f, 1.0f);
+    const float hue_drift = 1.0f - st * st * (3.0f - 2.0f * st);
+    const float hsum = p0.w + dt * hue_drift *
+                                  (0.012f + signed_radial * 0.030f + exc * 0.036f +
+                                   control_influence * 0.080f);
+    const float hue = hsum - floorf(hsum);
+    part[2u * slot] = make_float4(px, py, pz, hue);
+    part[2u * slot + 1u] = make_float4(vx, vy, vz, exc);
+
+    // The next step's deposit (wgsl:414-421 on the new position).
+    key = S.cell_off + leaf_cell(px, py, pz, D);
+    qx = f2i_rn_sat(px * S.scale);
+    qy = f2i_rn_sat(py * S.scale);
+    qz = f2i_rn_sat(pz * S.scale);
+  }
+  deposit_segmented(key, active, qx, qy, qz, mom_next);
+}
+
+// Standalone P2M: deposit the current positions into `moments` (leaf level
+// must be zero).
+__global__ void __launch_bounds__(256) k_deposit(const SceneDesc *__restrict__ scenes,
+                                                 const uint32_t *__restrict__ tile_scene,
+                                                 const float4 *__restrict__ part,
+                                                 uint4 *__restrict__ moments) {
+  const uint32_t tile = blockIdx.x;
+  const SceneDesc &S = scenes[tile_scene[tile]];
+  const uint32_t slot = tile * kTile + threadIdx.x;
+  const bool active = slot - S.body_off < S.n;
+  uint32_t key = 0xFFFFFFFFu;
+  int32_t qx = 0, qy = 0, qz = 0;
+  if (active) {
+    const float4 p = part[2u * slot];
+    key = S.cell_off + leaf_cell(p.x, p.y, p.z, S.depth);
+    qx = f2i_rn_sat(p.x * S.scale);
+    qy = f2i_rn_sat(p.y * S.scale);
+    qz = f2i_rn_sat(p.z * S.scale);
+  }
+  deposit_segmented(key, active, qx, qy, qz, moments);
+}
+
+// 3-D Morton interleave of leaf coordinates (x in bit 0).
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {
+  v &= 0x3FFu;
+  v = (v | (v << 16)) & 0x030000FFu;
+  v = (v | (v << 8)) & 0x0300F00Fu;
+  v = (v | (v << 4)) & 0x030C30C3u;
+  v = (v | (v << 2)) & 0x09249249u;
+  return v;
+}
+
+__global__ void __launch_bounds__(256) k_keys(const SceneDesc *__restrict__ scenes,
+                                              const uint32_t *__restrict__ tile_scene,
+                                              const float4 *__restrict__ part,
+                                              uint32_t *__restrict__ keys, uint32_t *__restrict__ vals,
+                                              uint32_t *__restrict__ ids, int fresh_ids) {
+  const uint32_t tile = blockIdx.x;
+  const SceneDesc &S = scenes[tile_scene[tile]];
+  const uint32_t slot = tile * kTile + threadIdx.x;
+  const uint32_t local = slot - S.body_off;
+  uint32_t key = S.key_base | 0x3FFFFu;  // padding sorts after every body of its scene
+  if (local < S.n) {
+    const float4 p = part[2u * slot];
+    const uint32_t dim = 1u << S.depth;
+    key = S.key_base | (spread3(cell_of_unit(unit_coord(p.x), dim)) |
+                        (spread3(cell_of_unit(unit_coord(p.y), dim)) << 1) |
+                        (spread3(cell_of_unit(unit_coord(p.z), dim)) << 2));
+  }
+  keys[slot] = key;
+  vals[slot] = slot;
+  if (fresh_ids) ids[slot] = local;
+}
+
+__global__ void __launch_bounds__(256) k_gather(const SceneDesc *__restrict__ scenes,
+                                                const uint32_t *__restrict__ tile_scene,
+                                                const uint32_t *__restrict__ perm,
+                                                const float4 *__restrict__ part_in,
+                                                const uint32_t *__restrict__ ids_in,
+                                                float4 *__restrict__ part_out,
+                                                uint32_t *__restrict__ ids_out,
+                                                uint4 *__restrict__ deposit_into, uint32_t nslots) {
+  const uint32_t tile = blockIdx.x;
+  const uint32_t slot = tile * kTile + threadIdx.x;
+  uint32_t from = perm[slot];
+  if (from >= nslots) from = slot;  // defensive: a permutation never leaves the buffer
+  const float4 p0 = part_in[2u * from], p1 = part_in[2u * from + 1u];
+  part_out[2u * slot] = p0;
+  part_out[2u * slot + 1u] = p1;
+  ids_out[slot] = ids_in[from];
+  if (deposit_into != nullptr) {
+    const SceneDesc &S = scenes[tile_scene[tile]];
+    const bool active = slot - S.body_off < S.n;
+    uint32_t key = 0xFFFFFFFFu;
+    int32_t qx = 0, qy = 0, qz = 0;
+    if (active) {
+      key = S.cell_off + leaf_cell(p0.x, p0.y, p0.z, S.depth);
+      qx = f2i_rn_sat(p0.x * S.scale);
+      qy = f2i_rn_sat(p0.y * S.scale);
+      qz = f2i_rn_sat(p0.z * S.scale);
+    }
+    deposit_segmented(key, active, qx, qy, qz, deposit_into);
+  }
+}
+
+// Scatter bodies back to the caller's order: out[body_off + id] = part[slot].
+__global__ void __launch_bounds__(256) k_unpermute(const SceneDesc *__restrict__ scenes,
+                                                   const uint32_t *__restrict__ tile_scene,
+                                                   const float4 *__restrict__ part,
+                                                   const uint32_t *__restrict__ ids,
+                                                   float4 *__restrict__ out, uint32_t tile_base) {
+  const uint32_t tile = tile_base + blockIdx.x;
+  const SceneDesc &S = scenes[tile_scene[tile]];
+  const uint32_t slot = tile * kTile + threadIdx.x;
+  if (slot - S.body_off >= S.n) return;
+  const uint32_t id = ids[slot];
+  if (id >= S.n) return;  // defensive: ids are a permutation of 0..n-1
+  const uint32_t dst = S.body_off + id;
+  out[2u * dst] = part[2u * slot];
+  out[2u * dst + 1u] = part[2u * slot + 1u];
+}
+
+// ------------------------------------------------------ galaxy seeding
+
+__device__ __forceinline__ uint32_t hash32(uint32_t x) {  // wgsl:205-210
+  x = ((x >> 16) ^ x) * 0x45d9f3bu;
+  x = ((x >> 16) ^ x) * 0x45d9f3bu;
+  return (x >> 16) ^ x;
+}
+
+__device__ __forceinline__ float random01(uint32_t seed) {
+  return (float)hash32(seed) * (1.0f / 4294967296.0f);
+}
+
+__device__ float seeded_enclosed_mass(float radius) {  // wgsl:216-230
+  const float bulge = 0.05f * powf(clampf_d(radius / 0.11f, 0.0f, 1.0f), 3.0f);
+  const float halo = 0.70f * powf(clampf_d(radius / 0.70f, 0.0f, 1.0f), 3.0f);
+  const float disc = 0.18f * powf(clampf_d((radius - 0.055f) / 0.60f, 0.0f, 1.0f), 1.0f / 0.72f);
+  const float polar = 0.07f * powf(clampf_d((radius - 0.22f) / 0.31f, 0.0f, 1.0f), 1.0f / 0.86f);
+  return fmaxf(bulge + halo + disc + polar, 0.0001f);
+}
+
+__device__ __forceinline__ void cross3(const float a[3], const float b[3], float o[3]) {
+  o[0] = a[1] * b[2] - a[2] * b[1];
+  o[1] = a[2] * b[0] - a[0] * b[2];
+  o[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+__global__ void __launch_bounds__(256) k_initialize(const SceneDesc *__restrict__ scenes,
+                                                    const uint32_t *__restrict__ tile_scene,
+                                                    float4 *__restrict__ out, uint32_t tile_base) {
+  constexpr float kTau = 6.28318530718f;
+  const uint32_t tile = tile_base + blockIdx.x;
+  const SceneDesc &S = scenes[tile_scene[tile]];
+  const uint32_t slot = tile * kTile + threadIdx.x;
+  const uint32_t i = slot - S.body_off;
+  if (i >= S.n) return;
+  const float u0 = random01(i * 11u + 1u), u1 = random01(i * 11u + 2u), u2 = random01(i * 11u + 3u);
+  const float u3 = random01(i * 11u + 4u), u4 = random01(i * 11u + 5u), u5 = random01(i * 11u + 6u);
+  float pos[3], vel[3], excitation;
+  if (u5 < 0.75f) {
+    const float z = u0 * 2.0f - 1.0f, phi = kTau * u1;
+    const float outer = u5 < 0.05f ? 0.11f : 0.70f;
+    const float radius = outer * powf(u2, 0.3333333f);
+    const float ring = sqrtf(fmaxf(0.0f, 1.0f - z * z));
+    const float rd[3] = {ring * cosf(phi), z, ring * sinf(phi)};
+    for (int k = 0; k < 3; k++) pos[k] = radius * rd[k];
+    const float tz = u3 * 2.0f - 1.0f, tphi = kTau * u4;
+    const float tring = sqrtf(fmaxf(0.0f, 1.0f - tz * tz));
+    const float rnd[3] = {tring * cosf(tphi), tz, tring * sinf(tphi)};
+    float tangent[3];
+    cross3(rd, rnd, tangent);
+    if (length3(tangent[0], tangent[1], tangent[2]) < 0.001f) {
+      const float up[3] = {0.0f, 1.0f, 0.0f};
+      cross3(rd, up, tangent);
+    }
+    if (length3(tangent[0], tangent[1], tangent[2]) < 0.001f) {
+      const float ex[3] = {1.0f, 0.0f, 0.0f};
+      cross3(rd, ex, tangent);
+    }
+    const float orbital = 0.985f * sqrtf(S.gravity * seeded_enclosed_mass(radius) / (radius + 0.018f));
+    const float tl = length3(tangent[0], tangent[1], tangent[2]);
+    for (int k = 0; k < 3; k++) vel[k] = orbital * (tangent[k] / tl);
+    excitation = u5 < 0.05f ? 0.09f : 0.025f + u4 * 0.025f;
+  } else if (u5 < 0.93f) {
+    const float radius = 0.055f + 0.60f * powf(u0, 0.72f);
+    const float arm = (float)(i & 3u) * (kTau / 4.0f);
+    const float angle = arm + radius * 7.8f + (u1 - 0.5f) * (0.045f + radius * 0.055f);
+    const float thickness = (u2 + u3 + u4 - 1.5f) * (0.0035f + radius * 0.010f);
+    const float flat[3] = {radius * cosf(angle), radius * sinf(angle) * 0.72f, thickness};
+    const float tilt = 0.20f;
+    pos[0] = flat[0];
+    pos[1] = flat[1] * cosf(tilt) - flat[2] * sinf(tilt);
+    pos[2] = flat[1] * sinf(tilt) + flat[2] * cosf(tilt);
+    const float orbital = 0.99f * sqrtf(S.gravity * seeded_enclosed_mass(radius) / (radius + 0.018f));
+    const float tangent[3] = {-sinf(angle), cosf(angle) * 0.72f * cosf(tilt),
+                              cosf(angle) * 0.72f * sinf(tilt)};
+    const float pl = length3(pos[0], pos[1], pos[2]);
+    const float tl = length3(tangent[0], tangent[1], tangent[2]);
+    const float sw = sinf(angle * 3.0f - radius * 13.0f);
+    for (int k = 0; k < 3; k++) vel[k] = orbital * (tangent[k] / tl) + (pos[k] / pl) * orbital * 0.035f * sw;
+    excitation = 0.08f + u3 * 0.05f;
+  } else {
+    const float lineage = (float)(i & 3u);
+    const float radius = 0.22f + 0.31f * powf(u0, 0.86f) + (lineage - 1.5f) * 0.007f;
+    const float angle = kTau * u1 + radius * 3.5f;
+    const float thickness = (u2 + u3 + u4 - 1.5f) * (0.004f + radius * 0.009f);
+    const float flat[3] = {radius * cosf(angle), thickness, radius * sinf(angle)};
+    const float tilt = -0.54f + lineage * 0.36f;
+    pos[0] = flat[0] * cosf(tilt) - flat[1] * sinf(tilt);
+    pos[1] = flat[0] * sinf(tilt) + flat[1] * cosf(tilt);
+    pos[2] = flat[2];
+    const float tangent[3] = {-sinf(angle) * cosf(tilt), -sinf(angle) * sinf(tilt), cosf(angle)};
+    const float orbital = 0.99f * sqrtf(S.gravity * seeded_enclosed_mass(radius) / (radius + 0.018f));
+    const float tl = length3(tangent[0], tangent[1], tangent[2]);
+    for (int k = 0; k < 3; k++) vel[k] = -orbital * (tangent[k] / tl);
+    excitation = 0.20f + u4 * 0.08f;
+  }
+  float hue = 0.0f;
+  if (u5 >= 0.75f) {
+    const float speed = fmaxf(length3(vel[0], vel[1], vel[2]), 0.0001f);
+    const float radius = fmaxf(length3(pos[0], pos[1], pos[2]), 0.0001f);
+    const float pv = (pos[0] * vel[0] + pos[1] * vel[1]) + pos[2] * vel[2];
+    const float radial_motion = clampf_d(pv / (radius * speed), -1.0f, 1.0f);
+    float am[3];
+    cross3(pos, vel, am);
+    const float spin = am[1] / fmaxf(length3(am[0], am[1], am[2]), 0.0001f);
+    const float h = atan2f(vel[1], vel[0]) / kTau + (vel[2] / speed) * 0.14f + spin * 0.075f +
+                    radial_motion * 0.065f + excitation * 0.085f + (float)(i & 3u) * 0.018f;
+    hue = h - floorf(h);
+  }
+  out[2u * slot] = make_float4(pos[0], pos[1], pos[2], hue);
+  out[2u * slot + 1u] = make_float4(vel[0], vel[1], vel[2], excitation);
+}
+
+// --------------------------------------------------------------- launches
+
+void launch_integrate(const LaunchCtx &L, uint32_t tiles) {
+  k_integrate<<<tiles, kTile, 0, L.stream>>>(L.scenes, L.tile_scene, L.part, L.mom, L.src, L.fields,
+                                             L.mom_next);
+}
+
+void launch_deposit(const LaunchCtx &L, uint4 *moments, uint32_t tiles) {
+  k_deposit<<<tiles, kTile, 0, L.stream>>>(L.scenes, L.tile_scene, L.part, moments);
+}
+
+void launch_keys(const LaunchCtx &L, uint32_t *keys, uint32_t *vals, uint32_t *ids, int fresh_ids,
+                 uint32_t tiles) {
+  k_keys<<<tiles, kTile, 0, L.stream>>>(L.scenes, L.tile_scene, L.part, keys, vals, ids, fresh_ids);
+}
+
+void launch_gather(const LaunchCtx &L, const uint32_t *perm, const float4 *part_in,
+                   const uint32_t *ids_in, float4 *part_out, uint32_t *ids_out, uint4 *deposit_into,
+                   uint32_t tiles) {
+  k_gather<<<tiles, kTile, 0, L.stream>>>(L.scenes, L.tile_scene, perm, part_in, ids_in, part_out,
+                                          ids_out, deposit_into, tiles * kTile);
+}
+
+void launch_unpermute(const LaunchCtx &L, const uint32_t *ids, float4 *out, uint32_t tile_base,
+                      uint32_t tiles) {
+  k_unpermute<<<tiles, kTile, 0, L.stream>>>(L.scenes, L.tile_scene, L.part, ids, out, tile_base);
+}
+
+void launch_initialize(const LaunchCtx &L, float4 *part_out, uint32_t tile_base, uint32_t tiles) {
+  k_initialize<<<tiles, kTile, 0, L.stream>>>(L.scenes, L.tile_scene, part_out, tile_base);
+}
+
+__global__ void k_iota(uint32_t *__restrict__ ids, uint32_t count) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) ids[i] = i;
+}
+
+void launch_iota(cudaStream_t stream, uint32_t *ids, uint32_t count) {
+  k_iota<<<(count + 255u) / 256u, 256, 0, stream>>>(ids, count);
+}
+
+}  // namespace rfmm

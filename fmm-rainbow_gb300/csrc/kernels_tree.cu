@@ -1,0 +1,493 @@
+// Tree passes of the FMM step: upward (M2M), M2L, and L2L fused with the
+// adaptive-leaf near field.
+//
+// Reference passes (iskamag/fmm-rainbow src/rainbow_fmm.wgsl):
+//   upward   424-455   one dispatch per level, 8-child integer sums
+//   m2l_all  457-519   <= 189 pair_field terms per on-path cell
+//   downward 574-611   parent field translated to the child centre
+//   near_all 521-572   26 neighbour cell monopoles per adaptive leaf
+//
+// GB300 structure:
+//   k_upward     one 512-thread CTA per 8x8x8-leaf subtree reduces four levels
+//                in shared memory; the last CTA of a scene (ticket counter)
+//                finishes the top levels.  It also writes each cell's source
+//                record (centre of mass, G*m), appends every parent with more
+//                than 16 bodies to the work list, zeroes the leaf level the
+//                next integrate deposits into, and clears the fields of the
+//                previous step's targets (fields are zero off the M2L path).
+//   k_m2l        one CTA per listed parent: the 6x6x6 source tile of the
+//                parent's 3x3x3 neighbourhood is staged in shared memory by a
+//                TMA tensor copy; warp w evaluates child w's 216 stencil slots
+//                in parallel and 10 lanes then sum them in the reference's
+//                loop order (excluded and empty slots contribute +0, which
+//                leaves an accumulation that starts at +0 unchanged).
+//   k_l2l_near   one warp per target: the top-down L2L chain is recomputed
+//                from the M2L results of the target's ancestors (so levels
+//                need no ordering), then adaptive leaves add their 26 near
+//                terms in loop order.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include "rfmm_device.cuh"
+#include "rfmm_kernels.h"
+
+namespace rfmm {
+
+// ----------------------------------------------------------------- upward
+
+__device__ __forceinline__ uint4 add_moment(uint4 a, uint4 b) {
+  return make_uint4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+}
+
+__device__ __forceinline__ void store_cell(const SceneDesc &S, uint32_t local_cell, uint4 m,
+                                           uint4 *mom, float4 *src) {
+  const uint32_t g = S.cell_off + local_cell;
+  mom[g] = m;
+  src[g] = make_source(m, S.scale, S.gravity, S.n_f);
+}
+
+__global__ void __launch_bounds__(512) k_upward(const SceneDesc *__restrict__ scenes,
+                                                const uint32_t *__restrict__ task_scene,
+                                                uint4 *__restrict__ mom, uint4 *__restrict__ mom_next,
+                                                float4 *__restrict__ src, float *__restrict__ fields,
+                                                WorkItem *__restrict__ plist, uint32_t plist_cap,
+                                                const WorkItem *__restrict__ plist_prev,
+                                                Counters *__restrict__ ctr, uint32_t list_par,
+                                                uint32_t *__restrict__ tickets) {
+  __shared__ uint4 s0[512];
+  __shared__ uint4 s1[64];
+  __shared__ uint4 s2[8];
+  __shared__ WorkItem s_items[80];
+  __shared__ uint32_t s_nitems, s_base, s_last;
+
+  const uint32_t tid = threadIdx.x;
+  const uint32_t scene = task_scene[blockIdx.x];
+  const SceneDesc S = scenes[scene];
+  const uint32_t D = S.depth, r = S.sub_level;
+  const uint32_t sub = blockIdx.x - S.task_off;
+  const uint32_t rdim = 1u << r;
+  const uint32_t sx = sub % rdim, sy = (sub / rdim) % rdim, sz = sub / (rdim * rdim);
+
+  // Clear the fields of the previous step's targets (children of listed parents).
+  {
+    const uint32_t prev_n = min(ctr->parents[list_par ^ 1u], plist_cap);
+    const uint32_t warp = blockIdx.x * 16u + (tid >> 5), lane = tid & 31u;
+    for (uint32_t i = warp; i < prev_n; i += gridDim.x * 16u) {
+      const WorkItem w = plist_prev[i];
+      const SceneDesc &P = scenes[w.scene];
+      const uint32_t lp = w.cell == 0u ? 0u : level_of_d(w.cell);
+      const uint32_t pdim = 1u << lp, dim = pdim << 1;
+      const uint32_t pl = w.cell - level_offset_d(lp);
+      const uint32_t px = pl % pdim, py = (pl / pdim) % pdim, pz = pl / (pdim * pdim);
+      for (uint32_t e = lane; e < 96u; e += 32u) {
+        const uint32_t ch = e / 12u, comp = e % 12u;
+        const uint32_t c = P.cell_off + level_offset_d(lp + 1u) +
+                           lin3(2u * px + (ch & 1u), 2u * py + ((ch >> 1) & 1u),
+                                2u * pz + (ch >> 2), dim);
+        fields[(size_t)c * 12u + comp] = 0.0f;
+      }
+    }
+  }
+
+  if (tid == 0) s_nitems = 0;
+  // Leaves of this subtree: 8x8x8 block, x fastest (rows of 128 B).
+  {
+    const uint32_t lx = tid & 7u, ly = (tid >> 3) & 7u, lz = tid >> 6;
+    const uint32_t dim = 1u << D;
+    const uint32_t leaf = level_offset_d(D) + lin3(sx * 8u + lx, sy * 8u + ly, sz * 8u + lz, dim);
+    const uint4 m = mom[S.cell_off + leaf];
+    s0[tid] = m;
+    src[S.cell_off + leaf] = make_source(m, S.scale, S.gravity, S.n_f);
+    mom_next[S.cell_off + leaf] = make_uint4(0u, 0u, 0u, 0u);
+  }
+  __syncthreads();
+  // Level D-1 (4x4x4 per subtree).
+  if (tid < 64u) {
+    const uint32_t x = tid & 3u, y = (tid >> 2) & 3u, z = tid >> 4;
+    uint4 acc = make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+    for (uint32_t dz = 0; dz < 2u; dz++)
+#pragma unroll
+      for (uint32_t dy = 0; dy < 2u; dy++)
+#pragma unroll
+        for (uint32_t dx = 0; dx < 2u; dx++)
+          acc = add_moment(acc, s0[(2u * x + dx) + 8u * ((2u * y + dy) + 8u * (2u * z + dz))]);
+    s1[tid] = acc;
+    const uint32_t dim = 1u << (D - 1u);
+    const uint32_t cell = level_offset_d(D - 1u) + lin3(sx * 4u + x, sy * 4u + y, sz * 4u + z, dim);
+    store_cell(S, cell, acc, mom, src);
+    if ((int32_t)acc.x > (int32_t)kAdaptive) s_items[atomicAdd(&s_nitems, 1u)] = {scene, cell};
+  }
+  __syncthreads();
+  if (tid < 8u) {
+    const uint32_t x = tid & 1u, y = (tid >> 1) & 1u, z = tid >> 2;
+    uint4 acc = make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+    for (uint32_t dz = 0; dz < 2u; dz++)
+#pragma unroll
+      for (uint32_t dy = 0; dy < 2u; dy++)
+#pragma unroll
+        for (uint32_t dx = 0; dx < 2u; dx++)
+          acc = add_moment(acc, s1[(2u * x + dx) + 4u * ((2u * y + dy) + 4u * (2u * z + dz))]);
+    s2[tid] = acc;
+    const uint32_t dim = 1u << (D - 2u);
+    const uint32_t cell = level_offset_d(D - 2u) + lin3(sx * 2u + x, sy * 2u + y, sz * 2u + z, dim);
+    store_cell(S, cell, acc, mom, src);
+    if ((int32_t)acc.x > (int32_t)kAdaptive) s_items[atomicAdd(&s_nitems, 1u)] = {scene, cell};
+  }
+  __syncthreads();
+  if (tid == 0) {
+    uint4 acc = make_uint4(0u, 0u, 0u, 0u);
+    for (uint32_t k = 0; k < 8u; k++) acc = add_moment(acc, s2[k]);
+    const uint32_t cell = level_offset_d(r) + lin3(sx, sy, sz, rdim);
+    store_cell(S, cell, acc, mom, src);
+    if ((int32_t)acc.x > (int32_t)kAdaptive) s_items[atomicAdd(&s_nitems, 1u)] = {scene, cell};
+  }
+  __syncthreads();
+  // Publish this subtree's parents.
+  if (tid == 0) {
+    uint32_t base = atomicAdd(&ctr->parents[list_par], s_nitems);
+    if (base + s_nitems > plist_cap) {
+      atomicCAS(&ctr->error, 0u, (uint32_t)kDevErrListOverflow);
+      s_nitems = base < plist_cap ? plist_cap - base : 0u;
+    }
+    s_base = base;
+  }
+  __syncthreads();
+  for (uint32_t i = tid; i < s_nitems; i += blockDim.x) plist[s_base + i] = s_items[i];
+
+  // The last subtree CTA of the scene reduces levels r-1 .. 0.
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) {
+    const uint32_t ntasks = 1u << (3u * r);
+    const uint32_t done = atomicAdd(&tickets[scene], 1u);
+    s_last = (done == ntasks - 1u) ? 1u : 0u;
+    if (s_last) tickets[scene] = 0u;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  if (tid == 0) s_nitems = 0;
+  // Level r has at most 512 cells: stage it (written by other CTAs) via L2.
+  const uint32_t nr = 1u << (3u * r);
+  for (uint32_t i = tid; i < nr; i += blockDim.x) s0[i] = __ldcg(&mom[S.cell_off + level_offset_d(r) + i]);
+  __syncthreads();
+  for (int l = (int)r - 1; l >= 0; l--) {
+    const uint32_t dim = 1u << l, cdim = dim << 1, nl = 1u << (3u * l);
+    uint4 acc = make_uint4(0u, 0u, 0u, 0u);
+    if (tid < nl) {
+      const uint32_t x = tid % dim, y = (tid / dim) % dim, z = tid / (dim * dim);
+      for (uint32_t dz = 0; dz < 2u; dz++)
+        for (uint32_t dy = 0; dy < 2u; dy++)
+          for (uint32_t dx = 0; dx < 2u; dx++)
+            acc = add_moment(acc, s0[lin3(2u * x + dx, 2u * y + dy, 2u * z + dz, cdim)]);
+      const uint32_t cell = level_offset_d((uint32_t)l) + tid;
+      store_cell(S, cell, acc, mom, src);
+      if ((int32_t)acc.x > (int32_t)kAdaptive) s_items[atomicAdd(&s_nitems, 1u)] = {scene, cell};
+    }
+    __syncthreads();
+    if (tid < nl) s0[tid] = acc;
+    __syncthreads();
+  }
+  if (tid == 0) {
+    uint32_t base = atomicAdd(&ctr->parents[list_par], s_nitems);
+    if (base + s_nitems > plist_cap) {
+      atomicCAS(&ctr->error, 0u, (uint32_t)kDevErrListOverflow);
+      s_nitems = base < plist_cap ? plist_cap - base : 0u;
+    }
+    s_base = base;
+  }
+  __syncthreads();
+  for (uint32_t i = tid; i < s_nitems; i += blockDim.x) plist[s_base + i] = s_items[i];
+}
+
+// -------------------------------------------------------------------- M2L
+
+constexpr uint32_t kTileCells = 216u;   // 6x6x6 children of a 3x3x3 parent block
+constexpr uint32_t kSlotStride = 217u;  // padded so the 10 summing lanes hit distinct banks
+constexpr uint32_t kTmaBytes = kTileCells * 16u;
+
+struct M2LShared {
+  float4 tile[kTileCells];  // first member: 128-byte aligned by the launch
+  unsigned long long mbar;
+  uint32_t stop;
+  float vals[8][10][kSlotStride];
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+// Bounded wait on an mbarrier phase; returns false when it gave up.
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, uint32_t parity) {
+  const uint32_t addr = smem_u32(bar);
+  for (uint32_t it = 0; it < (1u << 22); ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z,
+                                            unsigned long long *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__global__ void __launch_bounds__(256) k_m2l(const SceneDesc *__restrict__ scenes,
+                                             const WorkItem *__restrict__ plist, uint32_t plist_cap,
+                                             Counters *__restrict__ ctr, uint32_t list_par,
+                                             const uint4 *__restrict__ mom,
+                                             const float4 *__restrict__ src,
+                                             float *__restrict__ lfield,
+                                             const CUtensorMap *__restrict__ tmaps) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  // The TMA destination must be 128-byte aligned: align the carve-out by hand
+  // (the launch reserves 128 spare bytes).
+  const uint32_t pad = (128u - (smem_u32(smem_raw) & 127u)) & 127u;
+  M2LShared &sh = *reinterpret_cast<M2LShared *>(smem_raw + pad);
+  const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
+  const uint32_t count = min(ctr->parents[list_par], plist_cap);
+  if (blockIdx.x == 0 && tid == 0) ctr->parents[list_par ^ 1u] = 0u;  // reset for the next step
+  if (tid == 0) {
+    mbar_init(&sh.mbar, 1u);
+    sh.stop = 0u;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  uint32_t phase = 0u;
+
+  for (uint32_t item = blockIdx.x; item < count; item += gridDim.x) {
+    const WorkItem w = plist[item];
+    const SceneDesc &S = scenes[w.scene];
+    const uint32_t lp = w.cell == 0u ? 0u : level_of_d(w.cell);
+    const uint32_t l = lp + 1u, pdim = 1u << lp, dim = pdim << 1;
+    const uint32_t pl = w.cell - level_offset_d(lp);
+    const int pcx = (int)(pl % pdim), pcy = (int)((pl / pdim) % pdim), pcz = (int)(pl / (pdim * pdim));
+    const int bx = 2 * pcx - 2, by = 2 * pcy - 2, bz = 2 * pcz - 2;
+    const uint32_t lvl_base = S.cell_off + level_offset_d(l);
+
+    // Stage the 6x6x6 source tile (out-of-range cells read as zero).
+    if (l >= 3u) {
+      if (tid == 0) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(&sh.mbar, kTmaBytes);
+        tma_load_3d(sh.tile, &tmaps[w.scene * 8u + l], 4 * bx, by, bz, &sh.mbar);
+      }
+      if (!mbar_wait(&sh.mbar, phase)) {
+        if (atomicCAS(&ctr->error, 0u, (uint32_t)kDevErrTmaTimeout) == 0u) ctr->error_info = item;
+        sh.stop = 1u;
+      }
+      phase ^= 1u;
+    } else {
+      for (uint32_t t = tid; t < kTileCells; t += blockDim.x) {
+        const int x = bx + (int)(t % 6u), y = by + (int)((t / 6u) % 6u), z = bz + (int)(t / 36u);
+        float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (x >= 0 && y >= 0 && z >= 0 && x < (int)dim && y < (int)dim && z < (int)dim)
+          v = src[lvl_base + lin3((uint32_t)x, (uint32_t)y, (uint32_t)z, dim)];
+        sh.tile[t] = v;
+      }
+    }
+    __syncthreads();
+    if (sh.stop) return;
+
+    // Warp w handles child w of the parent.
+    const int cx = (int)(warp & 1u), cy = (int)((warp >> 1) & 1u), cz = (int)(warp >> 2);
+    const uint32_t tx = (uint32_t)(2 * pcx + cx), ty = (uint32_t)(2 * pcy + cy), tz = (uint32_t)(2 * pcz + cz);
+    const uint32_t target = lvl_base + lin3(tx, ty, tz, dim);
+    const bool live = mom[target].x != 0u;  // empty children are not targets
+    if (live) {
+      const float ctx = cell_center_axis(tx, dim), cty = cell_center_axis(ty, dim),
+                  ctz = cell_center_axis(tz, dim);
+      const float eps = 0.06f * kHalf / (float)dim;  // wgsl:507
+      for (uint32_t k = lane; k < kTileCells; k += 32u) {
+        // Reference loop order: source parent (pz, py, px) then child (cz, cy, cx).
+        const uint32_t pidx = k >> 3, ch = k & 7u;
+        const int ux = 2 * (int)(pidx % 3u) + (int)(ch & 1u);
+        const int uy = 2 * (int)((pidx / 3u) % 3u) + (int)((ch >> 1) & 1u);
+        const int uz = 2 * (int)(pidx / 9u) + (int)(ch >> 2);
+        // Source child coordinate minus target coordinate = u - 2 - child.
+        const int sx = ux - 2 - cx, sy = uy - 2 - cy, sz = uz - 2 - cz;
+        const bool near = sx >= -1 && sx <= 1 && sy >= -1 && sy <= 1 && sz >= -1 && sz <= 1;
+        const float4 s = sh.tile[ux + 6 * (uy + 6 * uz)];
+        float out[10];
+        if (!near && s.w != 0.0f) {
+          pair_field_d(s, ctx, cty, ctz, eps, out);
+        } else {
+#pragma unroll
+          for (int c = 0; c < 10; c++) out[c] = 0.0f;
+        }
+#pragma unroll
+        for (int c = 0; c < 10; c++) sh.vals[warp][c][k] = out[c];
+      }
+      __syncwarp();
+      if (lane < 12u) {
+        float acc = 0.0f;
+        if (lane < 10u) {
+          const float *row = sh.vals[warp][lane];
+          for (uint32_t k = 0; k < kTileCells; k++) acc = acc + row[k];
+        }
+        lfield[(size_t)target * 12u + lane] = acc;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------ L2L + near
+
+struct L2LShared {
+  float vals[8][10][27];
+};
+
+__global__ void __launch_bounds__(256) k_l2l_near(const SceneDesc *__restrict__ scenes,
+                                                  const WorkItem *__restrict__ plist,
+                                                  uint32_t plist_cap,
+                                                  const Counters *__restrict__ ctr,
+                                                  uint32_t list_par, const uint4 *__restrict__ mom,
+                                                  const float4 *__restrict__ src,
+                                                  const float *__restrict__ lfield,
+                                                  float *__restrict__ fields) {
+  __shared__ L2LShared sh;
+  const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
+  const uint32_t count = min(ctr->parents[list_par], plist_cap);
+  for (uint32_t item = blockIdx.x; item < count; item += gridDim.x) {
+    const WorkItem w = plist[item];
+    const SceneDesc &S = scenes[w.scene];
+    const uint32_t lp = w.cell == 0u ? 0u : level_of_d(w.cell);
+    const uint32_t l = lp + 1u, pdim = 1u << lp, dim = pdim << 1;
+    const uint32_t pl = w.cell - level_offset_d(lp);
+    const uint32_t tx = 2u * (pl % pdim) + (warp & 1u);
+    const uint32_t ty = 2u * ((pl / pdim) % pdim) + ((warp >> 1) & 1u);
+    const uint32_t tz = 2u * (pl / (pdim * pdim)) + (warp >> 2);
+    const uint32_t lvl_base = S.cell_off + level_offset_d(l);
+    const uint32_t target = lvl_base + lin3(tx, ty, tz, dim);
+    const uint32_t tcount = mom[target].x;
+    if (tcount == 0u) continue;  // warp-uniform
+
+    // Top-down chain: f_level = m2l(level) + translate(f_parent), root field 0
+    // (the reference never writes cell 0's field, wgsl:459).
+    float f[12];
+#pragma unroll
+    for (int c = 0; c < 12; c++) f[c] = 0.0f;
+    for (uint32_t a = 1u; a <= l; a++) {
+      const uint32_t sh_ = l - a, adim = 1u << a, padim = adim >> 1;
+      const uint32_t ax = tx >> sh_, ay = ty >> sh_, az = tz >> sh_;
+      const uint32_t pax = ax >> 1, pay = ay >> 1, paz = az >> 1;
+      const float dx = cell_center_axis(ax, adim) - cell_center_axis(pax, padim);
+      const float dy = cell_center_axis(ay, adim) - cell_center_axis(pay, padim);
+      const float dz = cell_center_axis(az, adim) - cell_center_axis(paz, padim);
+      // inherited (wgsl:603-609): a += J . delta, phi -= a . delta, J unchanged.
+      float inh[12];
+      inh[0] = f[0] + (f[4] * dx + f[5] * dy + f[6] * dz);
+      inh[1] = f[1] + (f[5] * dx + f[7] * dy + f[8] * dz);
+      inh[2] = f[2] + (f[6] * dx + f[8] * dy + f[9] * dz);
+      inh[3] = f[3] - ((f[0] * dx + f[1] * dy) + f[2] * dz);
+#pragma unroll
+      for (int c = 4; c < 12; c++) inh[c] = f[c];
+      const uint32_t anc = S.cell_off + level_offset_d(a) + lin3(ax, ay, az, adim);
+      const float4 *lf = reinterpret_cast<const float4 *>(lfield + (size_t)anc * 12u);
+      const float4 g0 = __ldg(lf), g1 = __ldg(lf + 1), g2 = __ldg(lf + 2);
+      f[0] = g0.x + inh[0];
+      f[1] = g0.y + inh[1];
+      f[2] = g0.z + inh[2];
+      f[3] = g0.w + inh[3];
+      f[4] = g1.x + inh[4];
+      f[5] = g1.y + inh[5];
+      f[6] = g1.z + inh[6];
+      f[7] = g1.w + inh[7];
+      f[8] = g2.x + inh[8];
+      f[9] = g2.y + inh[9];
+      f[10] = g2.z + inh[10];
+      f[11] = g2.w + inh[11];
+    }
+
+    const bool leaf = tcount <= kAdaptive || l == S.depth;  // wgsl:537-541
+    if (leaf) {
+      const float ctx = cell_center_axis(tx, dim), cty = cell_center_axis(ty, dim),
+                  ctz = cell_center_axis(tz, dim);
+      const float near_eps = fmaxf(S.softening, 0.72f * kHalf / (float)dim);
+      if (lane < 26u) {
+        const uint32_t j = lane < 13u ? lane : lane + 1u;  // skip the centre (13)
+        const int dx = (int)(j % 3u) - 1, dy = (int)((j / 3u) % 3u) - 1, dz = (int)(j / 9u) - 1;
+        const int sx = (int)tx + dx, sy = (int)ty + dy, sz = (int)tz + dz;
+        float out[10];
+#pragma unroll
+        for (int c = 0; c < 10; c++) out[c] = 0.0f;
+        if (sx >= 0 && sy >= 0 && sz >= 0 && sx < (int)dim && sy < (int)dim && sz < (int)dim) {
+          const float4 s = __ldg(&src[lvl_base + lin3((uint32_t)sx, (uint32_t)sy, (uint32_t)sz, dim)]);
+          if (s.w != 0.0f) pair_field_d(s, ctx, cty, ctz, near_eps, out);
+        }
+#pragma unroll
+        for (int c = 0; c < 10; c++) sh.vals[warp][c][lane] = out[c];
+      }
+      __syncwarp();
+      if (lane < 10u) {
+        float acc = f[0];
+#pragma unroll
+        for (int c = 1; c < 10; c++)
+          if ((int)lane == c) acc = f[c];
+        const float *row = sh.vals[warp][lane];
+        for (uint32_t k = 0; k < 26u; k++) acc = acc + row[k];
+        fields[(size_t)target * 12u + lane] = acc;
+      } else if (lane < 12u) {
+        fields[(size_t)target * 12u + lane] = f[lane == 10u ? 10 : 11];
+      }
+      __syncwarp();
+    } else if (lane < 12u) {
+      float v = f[0];
+#pragma unroll
+      for (int c = 1; c < 12; c++)
+        if ((int)lane == c) v = f[c];
+      fields[(size_t)target * 12u + lane] = v;
+    }
+  }
+}
+
+// --------------------------------------------------------------- launches
+
+void launch_upward(const LaunchCtx &L, uint32_t list_par, uint32_t tasks) {
+  k_upward<<<tasks, 512, 0, L.stream>>>(L.scenes, L.task_scene, L.mom, L.mom_next, L.src, L.fields,
+                                        L.plist, L.plist_cap, L.plist_prev, L.ctr, list_par,
+                                        L.tickets);
+}
+
+size_t m2l_smem_bytes() { return sizeof(M2LShared) + 128; }
+
+void launch_m2l(const LaunchCtx &L, uint32_t list_par, uint32_t grid) {
+  k_m2l<<<grid, 256, m2l_smem_bytes(), L.stream>>>(L.scenes, L.plist, L.plist_cap, L.ctr, list_par,
+                                                    L.mom, L.src, L.lfield, L.tmaps);
+}
+
+void launch_l2l_near(const LaunchCtx &L, uint32_t list_par, uint32_t grid) {
+  k_l2l_near<<<grid, 256, 0, L.stream>>>(L.scenes, L.plist, L.plist_cap, L.ctr, list_par, L.mom,
+                                         L.src, L.lfield, L.fields);
+}
+
+cudaError_t configure_tree_kernels() {
+  return cudaFuncSetAttribute(k_m2l, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)m2l_smem_bytes());
+}
+
+}  // namespace rfmm

@@ -1,0 +1,65 @@
+// Kernel launch interface used by the host engine.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include "rfmm_shared.h"
+
+namespace rfmm {
+
+// Device pointers one launch needs; filled by the engine for each step parity.
+struct LaunchCtx {
+  cudaStream_t stream;
+  const SceneDesc *scenes;
+  const uint32_t *tile_scene;  // body tile -> scene
+  const uint32_t *task_scene;  // upward task -> scene
+  float4 *part;                // current particle slots (2 float4 per body)
+  uint4 *mom;                  // moments of the current positions (leaf level valid)
+  uint4 *mom_next;             // leaf level receives the integrate deposit
+  float4 *src;                 // per-cell (com, G*m)
+  float *lfield;               // per-cell M2L result (12 floats)
+  float *fields;               // per-cell final field (12 floats, reference layout)
+  WorkItem *plist;             // parent list written this step
+  const WorkItem *plist_prev;  // parent list of the previous step
+  uint32_t plist_cap;
+  Counters *ctr;
+  uint32_t *tickets;
+  const CUtensorMap *tmaps;    // 8 per scene (levels 0..7; 3..6 used)
+};
+
+// Tree passes (kernels_tree.cu).
+void launch_upward(const LaunchCtx &L, uint32_t list_par, uint32_t tasks);
+void launch_m2l(const LaunchCtx &L, uint32_t list_par, uint32_t grid);
+void launch_l2l_near(const LaunchCtx &L, uint32_t list_par, uint32_t grid);
+cudaError_t configure_tree_kernels();
+
+// Body passes (kernels_body.cu).
+void launch_integrate(const LaunchCtx &L, uint32_t tiles);
+void launch_deposit(const LaunchCtx &L, uint4 *moments, uint32_t tiles);
+void launch_keys(const LaunchCtx &L, uint32_t *keys, uint32_t *vals, uint32_t *ids, int fresh_ids,
+                 uint32_t tiles);
+void launch_gather(const LaunchCtx &L, const uint32_t *perm, const float4 *part_in,
+                   const uint32_t *ids_in, float4 *part_out, uint32_t *ids_out, uint4 *deposit_into,
+                   uint32_t tiles);
+void launch_unpermute(const LaunchCtx &L, const uint32_t *ids, float4 *out, uint32_t tile_base,
+                      uint32_t tiles);
+void launch_initialize(const LaunchCtx &L, float4 *part_out, uint32_t tile_base, uint32_t tiles);
+void launch_iota(cudaStream_t stream, uint32_t *ids, uint32_t count);
+
+// LSD radix sort of (key, value) pairs, 8-bit digits (kernels_sort.cu).
+struct SortScratch {
+  uint32_t *keys[2];
+  uint32_t *vals[2];
+  uint32_t *hist;     // 256 * sort tiles
+  uint32_t *totals;   // 256
+  uint32_t capacity;  // elements
+};
+uint32_t sort_tiles(uint32_t n);
+// Sorts keys[0]/vals[0] over `bits` low bits; returns which buffer holds the result.
+int radix_sort(cudaStream_t stream, SortScratch &s, uint32_t n, uint32_t bits);
+
+}  // namespace rfmm

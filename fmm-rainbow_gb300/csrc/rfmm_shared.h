@@ -1,0 +1,56 @@
+// Structures shared by host code and kernels.
+#pragma once
+
+#include <cstdint>
+
+namespace rfmm {
+
+// Bodies are processed in tiles of this many slots; every scene's slot range
+// starts on a tile boundary, so a tile (one integrate CTA) never mixes scenes.
+constexpr uint32_t kTile = 256u;
+
+// One independent scene (a plain solve is a batch of one scene).
+struct alignas(16) SceneDesc {
+  uint32_t n;          // bodies (particle_count, wgsl:19)
+  uint32_t depth;      // leaf level (wgsl:20)
+  uint32_t body_off;   // first slot of this scene in the particle arrays
+  uint32_t tile_off;   // first body tile of this scene
+  uint32_t cell_off;   // first cell of this scene's tree in moments/fields
+  uint32_t cells;      // total_cells(depth)
+  uint32_t sub_level;  // root level of the 8x8x8-leaf subtrees of the upward pass
+  uint32_t task_off;   // first upward task of this scene
+  float scale;         // fixed-point deposit scale (control_settings.z)
+  float gravity;       // wgsl:30
+  float softening;     // wgsl:31
+  float dt_eff;        // dt * speed (wgsl:693)
+  float n_f;           // f32(particle_count)
+  float control_strength;  // control_settings.x
+  float control_radius;    // control_settings.y
+  uint32_t key_base;   // scene rank shifted above the Morton bits (sort key)
+  float control_point[4];      // wgsl:45
+  float control_axis_mode[4];  // wgsl:47
+};
+static_assert(sizeof(SceneDesc) == 96, "SceneDesc layout");
+
+// Device-side counters and status words of one engine.
+struct Counters {
+  uint32_t parents[2];   // length of the parent work list, per step parity
+  uint32_t error;        // first error code raised by a kernel (0 = none)
+  uint32_t error_info;   // kernel-specific detail for `error`
+  uint32_t pad[4];
+};
+
+enum DeviceError : uint32_t {
+  kDevErrNone = 0,
+  kDevErrTmaTimeout = 1,     // an mbarrier wait for a bulk tensor copy gave up
+  kDevErrListOverflow = 2,   // a work list exceeded its capacity
+};
+
+// One M2L/L2L work item: a parent cell whose count exceeds the adaptive leaf
+// capacity; its non-empty children are the on-path targets (wgsl:472-476).
+struct WorkItem {
+  uint32_t scene;
+  uint32_t cell;  // local cell index in the scene's tree (level offset included)
+};
+
+}  // namespace rfmm

@@ -1,0 +1,273 @@
+"""Python host mirror of the GB300 FMM solver C ABI.
+
+The reference drives its solver from JavaScript/Rust host code that calls the
+planner exports (src/lib.rs:88-157) and encodes WGSL passes
+(app.js:525-648, native/main.rs:353-421).  This module binds the same planner
+exports and the `rfmm_*` dispatch-sequence ABI of ``lib/librfmm.so`` through
+ctypes, with numpy views of the reference buffer layouts.  It is what the
+tests, the bench and a Python host call; there is no fallback: if the shared
+library is missing, importing the solver raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.dirname(HERE)
+LIB_PATH = os.path.join(PKG, "lib", "librfmm.so")
+
+PARTICLE_DTYPE = np.dtype([("pos", "<f4", 3), ("hue", "<f4"), ("vel", "<f4", 3), ("exc", "<f4")])
+MOMENT_DTYPE = np.dtype([("count", "<u4"), ("sum", "<i4", 3)])
+FIELD_DTYPE = np.dtype([("a", "<f4", 4), ("j0", "<f4", 4), ("j1", "<f4", 4)])
+
+RFMM_OK = 0
+STATUS = {
+    0: "ok", -1: "invalid argument", -2: "CUDA runtime error", -3: "device memory exhausted",
+    -4: "call out of order", -5: "kernel wait timed out", -6: "no sm_103 CUDA device",
+    -7: "kernel reported an error", -8: "request exceeds the memory budget",
+}
+BUF_PARTICLES, BUF_MOMENTS, BUF_FIELDS = 0, 1, 2
+PHASES = ("clear", "deposit", "upward", "m2l", "downward", "near", "integrate")
+
+# Every symbol the headers in include/ declare, with its ctypes signature.
+_u32, _f32, _vp, _sz, _i = C.c_uint32, C.c_float, C.c_void_p, C.c_size_t, C.c_int
+
+
+class Params(C.Structure):
+    """`rfmm_params` (include/rfmm.h)."""
+
+    _fields_ = [
+        ("dt", C.c_float),
+        ("gravity", C.c_float),
+        ("softening", C.c_float),
+        ("speed", C.c_float),
+        ("control_point", C.c_float * 4),
+        ("control_axis_mode", C.c_float * 4),
+        ("control_strength", C.c_float),
+        ("control_radius", C.c_float),
+        ("fixed_point_scale", C.c_float),
+        ("depth", C.c_uint32),
+    ]
+
+
+class Plan(C.Structure):
+    _fields_ = [("particles", C.c_uint32), ("depth", C.c_uint32), ("cells", C.c_uint32),
+                ("fixed_point_scale", C.c_float)]
+
+
+_P = C.POINTER(Params)
+SIGNATURES = {
+    # include/rainbow_fmm.h
+    "rainbow_api_version": (_u32, []),
+    "rainbow_shader_ptr": (_vp, []),
+    "rainbow_shader_len": (_sz, []),
+    "rainbow_algorithm_ptr": (_vp, []),
+    "rainbow_algorithm_len": (_sz, []),
+    "rainbow_depth_for_particles": (_u32, [_u32]),
+    "rainbow_level_cells": (_u32, [_u32]),
+    "rainbow_level_offset": (_u32, [_u32]),
+    "rainbow_total_cells": (_u32, [_u32]),
+    "rainbow_clamp_particle_count": (_u32, [_u32]),
+    "rainbow_fixed_point_scale": (_f32, [_u32]),
+    "rainbow_linear_work_lo": (_u32, [_u32, _u32]),
+    "rainbow_plan_depth_unclamped": (_u32, [_u32]),
+    "rainbow_plan_scale_unclamped": (_f32, [_u32]),
+    "rainbow_plan_work_bound_unclamped": (C.c_uint64, [_u32, _u32]),
+    # include/rfmm.h
+    "rfmm_default_params": (None, [_P]),
+    "rfmm_status_string": (C.c_char_p, [_i]),
+    "rfmm_create": (_i, [_u32, _P, C.POINTER(_vp)]),
+    "rfmm_destroy": (_i, [_vp]),
+    "rfmm_set_stream": (_i, [_vp, _vp]),
+    "rfmm_get_plan": (_i, [_vp, C.POINTER(Plan)]),
+    "rfmm_set_params": (_i, [_vp, _P]),
+    "rfmm_upload_particles": (_i, [_vp, _vp, _sz]),
+    "rfmm_upload_particles_device": (_i, [_vp, _vp, _sz]),
+    "rfmm_seed_galaxy": (_i, [_vp]),
+    "rfmm_solve_fields": (_i, [_vp]),
+    "rfmm_step": (_i, [_vp, _u32]),
+    "rfmm_sync": (_i, [_vp]),
+    "rfmm_download": (_i, [_vp, _i, _vp, _sz]),
+    "rfmm_download_device": (_i, [_vp, _i, _vp, _sz]),
+    "rfmm_digest": (_i, [_vp, _i, C.POINTER(_u32)]),
+    "rfmm_phase_times": (_i, [_vp, C.POINTER(_f32)]),
+    "rfmm_check_finite": (_i, [_vp, _u32, C.POINTER(_u32), C.POINTER(_f32)]),
+    "rfmm_set_resort_interval": (_i, [_vp, _u32]),
+    "rfmm_device_error": (_i, [_vp, C.POINTER(_u32), C.POINTER(_u32)]),
+}
+
+_lib = None
+
+
+class RFMMError(RuntimeError):
+    def __init__(self, status: int, what: str = ""):
+        self.status = status
+        super().__init__("%s failed: %s (%d)" % (what, STATUS.get(status, "unknown"), status))
+
+
+def lib() -> C.CDLL:
+    """Load ``lib/librfmm.so``; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("librfmm.so is not built (%s); run the package build first" % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(status: int, what: str) -> None:
+    if status != RFMM_OK:
+        raise RFMMError(status, what)
+
+
+def default_params(**kw) -> Params:
+    p = Params()
+    lib().rfmm_default_params(C.byref(p))
+    for k, v in kw.items():
+        if k in ("control_point", "control_axis_mode"):
+            getattr(p, k)[:] = v
+        else:
+            setattr(p, k, v)
+    return p
+
+
+# ------------------------------------------------------------------ planner
+
+def api_version() -> int:
+    return lib().rainbow_api_version()
+
+
+def shader_text() -> str:
+    L = lib()
+    return C.string_at(L.rainbow_shader_ptr(), L.rainbow_shader_len()).decode()
+
+
+def algorithm() -> str:
+    L = lib()
+    return C.string_at(L.rainbow_algorithm_ptr(), L.rainbow_algorithm_len()).decode()
+
+
+def plan_unclamped(n: int):
+    """(depth, cells, scale) as the native harness plans it (native/main.rs:89-92)."""
+    L = lib()
+    d = L.rainbow_plan_depth_unclamped(n)
+    return d, L.rainbow_level_offset(d + 1), L.rainbow_plan_scale_unclamped(n)
+
+
+# ------------------------------------------------------------------- solver
+
+class Solver:
+    """One scene of N bodies resident on the GPU (the `rfmm_*` handle)."""
+
+    def __init__(self, n: int, params: Params | None = None, **kw):
+        if params is None:
+            params = default_params(**kw)
+        self._h = C.c_void_p()
+        _check(lib().rfmm_create(n, C.byref(params), C.byref(self._h)), "rfmm_create")
+        self.n = n
+        plan = Plan()
+        _check(lib().rfmm_get_plan(self._h, C.byref(plan)), "rfmm_get_plan")
+        self.depth, self.cells, self.scale = plan.depth, plan.cells, plan.fixed_point_scale
+
+    def close(self):
+        if self._h:
+            lib().rfmm_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_params(self, params: Params):
+        _check(lib().rfmm_set_params(self._h, C.byref(params)), "rfmm_set_params")
+
+    def set_stream(self, stream_ptr: int | None):
+        _check(lib().rfmm_set_stream(self._h, stream_ptr or None), "rfmm_set_stream")
+
+    def upload(self, particles: np.ndarray):
+        a = np.ascontiguousarray(particles)
+        assert a.dtype == PARTICLE_DTYPE and len(a) == self.n
+        _check(lib().rfmm_upload_particles(self._h, a.ctypes.data, a.nbytes), "rfmm_upload_particles")
+
+    def upload_device(self, ptr: int, nbytes: int):
+        _check(lib().rfmm_upload_particles_device(self._h, ptr, nbytes), "rfmm_upload_particles_device")
+
+    def upload_host_ptr(self, ptr: int, nbytes: int):
+        _check(lib().rfmm_upload_particles(self._h, ptr, nbytes), "rfmm_upload_particles")
+
+    def seed_galaxy(self):
+        _check(lib().rfmm_seed_galaxy(self._h), "rfmm_seed_galaxy")
+
+    def solve_fields(self):
+        _check(lib().rfmm_solve_fields(self._h), "rfmm_solve_fields")
+
+    def step(self, steps: int = 1):
+        _check(lib().rfmm_step(self._h, steps), "rfmm_step")
+
+    def sync(self):
+        _check(lib().rfmm_sync(self._h), "rfmm_sync")
+
+    def set_resort_interval(self, steps: int):
+        _check(lib().rfmm_set_resort_interval(self._h, steps), "rfmm_set_resort_interval")
+
+    def download(self, which: int = BUF_PARTICLES) -> np.ndarray:
+        dtype, count = {BUF_PARTICLES: (PARTICLE_DTYPE, self.n), BUF_MOMENTS: (MOMENT_DTYPE, self.cells),
+                        BUF_FIELDS: (FIELD_DTYPE, self.cells)}[which]
+        out = np.empty(count, dtype)
+        _check(lib().rfmm_download(self._h, which, out.ctypes.data, out.nbytes), "rfmm_download")
+        return out
+
+    def download_host_ptr(self, which: int, ptr: int, nbytes: int):
+        _check(lib().rfmm_download(self._h, which, ptr, nbytes), "rfmm_download")
+
+    def download_device(self, which: int, ptr: int, nbytes: int):
+        _check(lib().rfmm_download_device(self._h, which, ptr, nbytes), "rfmm_download_device")
+
+    def particles(self) -> np.ndarray:
+        return self.download(BUF_PARTICLES)
+
+    def moments(self) -> np.ndarray:
+        return self.download(BUF_MOMENTS)
+
+    def fields(self) -> np.ndarray:
+        return self.download(BUF_FIELDS)
+
+    def digest(self, which: int) -> int:
+        out = C.c_uint32()
+        _check(lib().rfmm_digest(self._h, which, C.byref(out)), "rfmm_digest")
+        return out.value
+
+    def phase_times(self) -> dict:
+        ms = (C.c_float * 7)()
+        _check(lib().rfmm_phase_times(self._h, ms), "rfmm_phase_times")
+        return dict(zip(PHASES, list(ms)))
+
+    def check_finite(self, probe: int = 8192):
+        bad, mx = C.c_uint32(), C.c_float()
+        _check(lib().rfmm_check_finite(self._h, probe, C.byref(bad), C.byref(mx)), "rfmm_check_finite")
+        return bad.value, mx.value
+
+    def device_error(self):
+        code, info = C.c_uint32(), C.c_uint32()
+        _check(lib().rfmm_device_error(self._h, C.byref(code), C.byref(info)), "rfmm_device_error")
+        return code.value, info.value

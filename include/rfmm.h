@@ -1,0 +1,156 @@
+/*
+ * rfmm.h -- C ABI of the GB300 FMM solver (the dispatch-sequence drop-in).
+ *
+ * The reference host encodes one solver frame as WGSL compute passes
+ * clear_cells -> deposit -> upward x depth -> m2l_all -> downward x depth ->
+ * near_all -> integrate, sized by the planner and fed by a 16-slot Params
+ * table (iskamag/fmm-rainbow app.js:141-213, 525-648; native/main.rs:36-128,
+ * 353-421).  This ABI replaces that whole sequence: the host creates a solver
+ * for N bodies, uploads or seeds particles, and calls rfmm_step /
+ * rfmm_solve_fields; the library owns device memory and runs sm_103a
+ * kernels on one GPU.  Buffers keep the reference layouts (Particle 32 B,
+ * Moment 16 B, Field 48 B; src/rainbow_fmm.wgsl:52-73) so content digests
+ * stay comparable with the reference harness (native/main.rs:152-163).
+ *
+ * Conventions: every function returns an int status (0 = RFMM_OK, negative
+ * = RFMM_ERR_*); no exception or abort crosses the ABI.  The library owns
+ * device memory, the caller owns host memory.  A handle is bound to one CUDA
+ * device and one stream and is not thread-safe; separate handles may be used
+ * from separate threads.  Calls are asynchronous on the handle's stream
+ * unless they return host data (download, digest, phase times, sync).
+ */
+#ifndef RFMM_H
+#define RFMM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RFMM_ABI_VERSION 1u
+
+enum rfmm_status {
+  RFMM_OK = 0,
+  RFMM_ERR_INVALID = -1,   /* bad argument (null pointer, size mismatch, range) */
+  RFMM_ERR_CUDA = -2,      /* a CUDA runtime call failed */
+  RFMM_ERR_OOM = -3,       /* device memory allocation failed */
+  RFMM_ERR_STATE = -4,     /* call out of order (e.g. step before particles exist) */
+  RFMM_ERR_TIMEOUT = -5,   /* a kernel's bounded wait gave up; see rfmm_device_error */
+  RFMM_ERR_NO_DEVICE = -6, /* no CUDA device, or the device is not sm_103 */
+  RFMM_ERR_DEVICE = -7,    /* a kernel reported an internal error word */
+  RFMM_ERR_BUDGET = -8     /* request does not fit the memory budget (server) */
+};
+
+/* Which buffer rfmm_download / rfmm_digest read. */
+enum rfmm_buffer {
+  RFMM_BUF_PARTICLES = 0, /* N x 32 B, in the caller's body order */
+  RFMM_BUF_MOMENTS = 1,   /* C x 16 B, the moment tree of the last solve */
+  RFMM_BUF_FIELDS = 2     /* C x 48 B, the fields of the last solve */
+};
+
+/* Physics parameters: the compute-relevant fields of `struct Params`
+ * (src/rainbow_fmm.wgsl:18-50).  depth/fixed_point_scale 0 = use the
+ * planner's unclamped plan (src/lib.rs:45-69), as the native harness does
+ * (native/main.rs:89-92). */
+typedef struct rfmm_params {
+  float dt;                   /* Params.dt */
+  float gravity;              /* Params.gravity */
+  float softening;            /* Params.softening */
+  float speed;                /* Params.speed; the step uses dt * speed */
+  float control_point[4];     /* xyz brush centre; w > 0.5 = control active */
+  float control_axis_mode[4]; /* xyz vortex axis; w 1 = pull, 2 = push, 3 = vortex */
+  float control_strength;     /* control_settings.x */
+  float control_radius;       /* control_settings.y */
+  float fixed_point_scale;    /* control_settings.z; 0 = planner scale */
+  uint32_t depth;             /* 0 = planner depth; else 4..6 */
+} rfmm_params;
+
+/* The plan a handle runs with. */
+typedef struct rfmm_plan {
+  uint32_t particles;
+  uint32_t depth;
+  uint32_t cells; /* total_cells(depth) */
+  float fixed_point_scale;
+} rfmm_plan;
+
+typedef struct rfmm_handle rfmm_handle;
+
+/* Fill `p` with the native harness's defaults (native/main.rs:57-81):
+ * dt 0.0009, gravity 0.34, softening 0.012, speed 1, control off,
+ * strength 0.7, radius 0.22. */
+void rfmm_default_params(rfmm_params *p);
+
+/* Human-readable name of a status code (static string). */
+const char *rfmm_status_string(int status);
+
+/* Create a solver for `n` bodies (1 <= n <= 2^23) on the current CUDA
+ * device.  Allocates the particle, moment and field buffers
+ * (app.js:543-559, native/main.rs:307-309).  `params` may be NULL for the
+ * harness defaults. */
+int rfmm_create(uint32_t n, const rfmm_params *params, rfmm_handle **out);
+int rfmm_destroy(rfmm_handle *h);
+
+/* Run the handle's work on `stream` (a cudaStream_t; NULL = the handle's
+ * own stream). */
+int rfmm_set_stream(rfmm_handle *h, void *stream);
+int rfmm_get_plan(const rfmm_handle *h, rfmm_plan *out);
+
+/* Replace the physics parameters (app.js updateComputeParams, 189-205).
+ * depth and fixed_point_scale must match the plan the handle was made with
+ * (0 = keep). */
+int rfmm_set_params(rfmm_handle *h, const rfmm_params *params);
+
+/* Upload N bodies (N x 32 B, reference Particle layout) from host memory
+ * (pinned or pageable) or from device memory. */
+int rfmm_upload_particles(rfmm_handle *h, const void *host_aos, size_t bytes);
+int rfmm_upload_particles_device(rfmm_handle *h, const void *device_aos, size_t bytes);
+
+/* Seed the reference galaxy (`initialize`, src/rainbow_fmm.wgsl:232-374). */
+int rfmm_seed_galaxy(rfmm_handle *h);
+
+/* One field solve without integrate: clear, deposit, upward, m2l, downward,
+ * near (native/main.rs:437-449).  Moments and fields then hold the tree and
+ * the field of the current positions. */
+int rfmm_solve_fields(rfmm_handle *h);
+
+/* `steps` full solver frames (native/main.rs:411-421). */
+int rfmm_step(rfmm_handle *h, uint32_t steps);
+
+/* Wait for the handle's queued work; reports kernel error words. */
+int rfmm_sync(rfmm_handle *h);
+
+/* Copy a buffer to host memory (bytes must equal the buffer size:
+ * N*32, C*16 or C*48) or to device memory.  Particles come back in the
+ * caller's body order. */
+int rfmm_download(rfmm_handle *h, int which, void *host_dst, size_t bytes);
+int rfmm_download_device(rfmm_handle *h, int which, void *device_dst, size_t bytes);
+
+/* FNV-1a digest of a buffer's little-endian bytes (native/main.rs:152-163). */
+int rfmm_digest(rfmm_handle *h, int which, uint32_t *out);
+
+/* Per-phase device time in ms of one instrumented frame, in the reference
+ * harness's phase order (native/main.rs:468): clear, deposit, upward, m2l,
+ * downward, near, integrate.  Fused phases report their time in the first
+ * phase of the fusion and 0 in the others: deposit carries the sort+gather
+ * refresh of the resident body order, downward carries L2L+near, clear is
+ * folded into upward.  The frame advances the simulation by one step. */
+int rfmm_phase_times(rfmm_handle *h, float ms[7]);
+
+/* Non-finite count and max |value| over the first min(N, probe) bodies'
+ * 8 floats (native/main.rs:536-549). */
+int rfmm_check_finite(rfmm_handle *h, uint32_t probe, uint32_t *non_finite, float *max_abs);
+
+/* Steps between refreshes of the resident leaf order (0 = never; default
+ * 16).  Results do not depend on it. */
+int rfmm_set_resort_interval(rfmm_handle *h, uint32_t steps);
+
+/* Last kernel error word (0 = none) and its detail. */
+int rfmm_device_error(rfmm_handle *h, uint32_t *code, uint32_t *info);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RFMM_H */

@@ -1,0 +1,31 @@
+"""Shared test setup: import paths, the `gpu` marker, common fixtures."""
+import os
+import sys
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+PKG = os.path.join(REPO, "fmm-rainbow_gb300")
+for p in (REPO, PKG):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA sm_103 device (GB300)")
+
+
+@pytest.fixture(scope="session")
+def oracle_mod():
+    from oracle import oracle as O
+    O.lib()
+    return O
+
+
+@pytest.fixture(scope="session")
+def rfmm_mod():
+    from rfmm import build as pkg_build
+    pkg_build.build()
+    import rfmm
+    rfmm.lib()
+    return rfmm
