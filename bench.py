@@ -1,0 +1,338 @@
+#!/usr/bin/env python3
+"""Throughput bench of the GB300 FMM gravity step (body-steps/s).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl fmm|reference]
+
+A bench step is one full solve of the workload: the scene is reset from a
+device-resident pristine copy (upload + leaf sort + deposit) and advanced
+`fmm_steps` leapfrog steps.  The default workload is the reference's default
+preset, a 1,048,576-body Plummer sphere (a = 0.1, centred in the unit box,
+truncated at r = 0.5, G = 1, eps = 1e-3, dt = 5e-4) run for 60 steps.
+
+Timing: W untimed warm-up steps, then exactly K timed steps, each bracketed by
+CUDA events on the solver's stream; L2 is flushed (512 MiB write) between
+timed steps, outside the events.  Barrier + synchronize on both sides, max
+over ranks.  N GPUs run N independent replicas (one process per GPU; the
+plain solve does not shard), so `value` is the sum of all replicas' work over
+the slowest replica's time.
+
+The JSON line adds: `e2e` (the same metric through the C ABI from pinned host
+buffers, host<->device copies inside the timed region), `roofline` for the
+dominant kernel (integrate), `cpu_baseline` (the CPU oracle on the host cores,
+rank 0 only), `clocks` sampled during the timed region, `gpu_launches`, and
+per-kernel times.
+
+`--impl reference` times the reference algorithm's CPU implementation (the
+oracle port: the reference's Rust/WGSL harness needs a Vulkan adapter and a
+Rust toolchain, neither of which exists here) on the host cores, one FMM step
+of the same workload per bench step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "fmm-rainbow_gb300")
+for _p in (REPO, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+WORKLOADS = {
+    # The reference's default preset (the metric's headline configuration).
+    "plummer_1m": dict(kind="plummer", n=1 << 20, seed=2, fmm_steps=60, dt=5e-4, eps=1e-3, G=1.0,
+                       desc="Plummer sphere a=0.1 at (0.5,0.5,0.5), r<0.5, N=1,048,576, "
+                            "G=1, eps=1e-3, 60 steps dt=5e-4, Plummer-DF velocities"),
+    # The reference's CPU-runnable case.
+    "uniform_64k": dict(kind="uniform", n=65536, seed=1, fmm_steps=1, dt=1e-3, eps=1e-3, G=1.0,
+                        desc="uniform [0,1)^3, N=65,536, G=1, eps=1e-3, v=0, 1 step dt=1e-3"),
+    # The budget maximum.
+    "clusters_5m": dict(kind="clusters", n=5242880, seed=3, fmm_steps=60, dt=5e-4, eps=5e-4, G=1.0,
+                        desc="8 Plummer clusters a~logU[0.02,0.1], centres U[0.2,0.8]^3, "
+                             "N=5,242,880, eps=5e-4, bulk sigma 0.05, 60 steps dt=5e-4"),
+}
+
+PEAKS_FILE = os.path.join(REPO, "MEASURED_PEAKS.json")
+TRAFFIC_FILE = os.path.join(REPO, "profiles", "ncu_traffic.json")
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse_args():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--workload", default="plummer_1m", choices=sorted(WORKLOADS))
+    ap.add_argument("--impl", default="fmm", choices=["fmm", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=8)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_scene(w):
+    from rfmm import scenes
+    return scenes.make(w["kind"], w["n"], w["seed"])
+
+
+def roofline_bytes_integrate(n, cells, depth):
+    """Algorithmic bytes of one fused integrate launch.
+
+    64 B per body (32 B particle in, 32 B out), 64 B per tree cell (48 B field
+    + 16 B moment gathered once) and 16 B per leaf cell (the next step's leaf
+    deposit written once).
+    """
+    leaves = 8 ** depth
+    return 64 * n + 64 * cells + 16 * leaves
+
+
+def clocks_sampler(gpu_index):
+    q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    try:
+        return subprocess.Popen(["nvidia-smi", "-i", str(gpu_index), "--query-gpu=" + q,
+                                 "--format=csv,noheader,nounits", "-lms", "100"],
+                                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+    except OSError:
+        return None
+
+
+def clocks_summary(proc):
+    if proc is None:
+        return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+    proc.terminate()
+    try:
+        out, _ = proc.communicate(timeout=5)
+    except subprocess.TimeoutExpired:
+        proc.kill()
+        out, _ = proc.communicate()
+    sm, smax, reasons = [], [], set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for line in out.strip().splitlines():
+        f = [x.strip() for x in line.split(",")]
+        if len(f) < 9:
+            continue
+        try:
+            sm.append(float(f[1]))
+            smax.append(float(f[2]))
+        except ValueError:
+            continue
+        for name, v in zip(names, f[5:9]):
+            if v.lower() == "active":
+                reasons.add(name)
+    return {"sm_mhz": statistics.median(sm) if sm else None,
+            "sm_max_mhz": max(smax) if smax else None,
+            "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def hbm_peak():
+    try:
+        with open(PEAKS_FILE) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def traffic_for(workload):
+    try:
+        with open(TRAFFIC_FILE) as f:
+            t = json.load(f)
+        entry = t.get("k_integrate", {}).get(workload)
+        return None if entry is None else float(entry["dram_bytes_per_launch"])
+    except (OSError, ValueError, KeyError):
+        return None
+
+
+def cpu_baseline(w, seconds, threads=None):
+    """The CPU oracle (the reference algorithm restated in C, OpenMP) on this host."""
+    import numpy as np  # noqa: F401
+    from oracle import oracle as O
+    cores = O.set_threads(threads or os.cpu_count() or 1)
+    scene = make_scene(w)
+    st = O.OracleState(scene, O.make_params(w["n"], gravity=w["G"], softening=w["eps"], dt=w["dt"]))
+    st.step(1)  # warm
+    done, t0 = 0, time.perf_counter()
+    while True:
+        st.step(1)
+        done += 1
+        el = time.perf_counter() - t0
+        if el >= seconds or done >= w["fmm_steps"]:
+            break
+    return {"value": w["n"] * done / el, "unit": "body-steps/s", "cores": cores, "kind": "port",
+            "sample": "%d FMM step(s) of the %s workload (%d bodies) on %d host threads, %.1f s"
+                      % (done, "same", w["n"], cores, el)}
+
+
+def run_reference(args, w):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from oracle import oracle as O
+    cores = O.set_threads(os.cpu_count() or 1)
+    scene = make_scene(w)
+    st = O.OracleState(scene, O.make_params(w["n"], gravity=w["G"], softening=w["eps"], dt=w["dt"]))
+    for _ in range(args.warmup):
+        st.step(1)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        st.step(1)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = w["n"] * args.steps / total
+    line = {
+        "impl": "reference", "metric": "body-steps/s", "value": value, "unit": "body-steps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded): " + w["desc"],
+        "config": {"workload": args.workload, "bodies": w["n"], "fmm_steps_per_bench_step": 1,
+                   "implementation": "CPU oracle port of the reference compute passes "
+                                     "(reference wgpu/Vulkan harness unavailable on this box)"},
+        "cpu_baseline": {"value": value, "unit": "body-steps/s", "cores": cores, "kind": "port",
+                         "sample": "one FMM step of %d bodies per bench step, %d host threads"
+                                   % (w["n"], cores)},
+        "e2e": {"value": value, "unit": "body-steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args, w):
+    import numpy as np
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from rfmm import build as pkg_build
+    pkg_build.build()
+    import rfmm
+
+    n, fmm_steps = w["n"], w["fmm_steps"]
+    scene = make_scene(w)
+    params = rfmm.default_params(gravity=w["G"], softening=w["eps"], dt=w["dt"])
+    # A real (non-default) stream shared by torch's events/flush and the solver.
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    solver = rfmm.Solver(n, params)
+    solver.set_stream(stream.cuda_stream)
+    pristine = torch.from_numpy(scene.view(np.uint8).copy()).cuda()
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+
+    def bench_step():
+        solver.upload_device(pristine.data_ptr(), pristine.numel())
+        solver.step(fmm_steps)
+
+    for _ in range(args.warmup):
+        bench_step()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    clk = clocks_sampler(local)
+    time.sleep(0.3)
+    barrier()
+    l0 = solver.launch_count()
+    for k in range(args.steps):
+        flush.zero_()
+        starts[k].record(stream)
+        bench_step()
+        ends[k].record(stream)
+    barrier()
+    launches = solver.launch_count() - l0
+    clocks = clocks_summary(clk)
+    total_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * n * fmm_steps * args.steps / (total_ms * 1e-3)
+    solver.sync()
+
+    # Per-kernel device times over the same workload (event pair around every launch).
+    solver.upload_device(pristine.data_ptr(), pristine.numel())
+    prof = solver.profile_steps(fmm_steps)
+    integ_ms, integ_n = prof["integrate"]
+    alg_bytes = roofline_bytes_integrate(n, solver.cells, solver.depth)
+    peak, peak_kind = hbm_peak()
+    achieved = alg_bytes / (integ_ms / integ_n * 1e-3) / 1e9
+    roofline = {"kernel": "k_integrate", "bound": "hbm", "achieved": achieved, "peak": peak,
+                "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                "algorithmic_bytes_per_launch": alg_bytes,
+                "avg_launch_ms": integ_ms / integ_n, "traffic": traffic_for(args.workload)}
+    kernel_ms = {k: (v[0] / v[1] if v[1] else 0.0) for k, v in prof.items()}
+
+    # End to end through the C ABI with host buffers: pinned input upload
+    # (H2D + leaf sort), the solve, pinned download of the result (D2H).
+    pin_in = torch.from_numpy(scene.view(np.uint8).copy()).pin_memory()
+    pin_out = torch.empty(n * 32, dtype=torch.uint8).pin_memory()
+    e2e_times = []
+    for k in range(args.e2e_steps + 1 if args.e2e_steps > 0 else 0):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        solver.upload_host_ptr(pin_in.data_ptr(), pin_in.numel())
+        solver.step(fmm_steps)
+        solver.download_host_ptr(rfmm.BUF_PARTICLES, pin_out.data_ptr(), pin_out.numel())
+        if k > 0:
+            e2e_times.append(time.perf_counter() - t0)
+    e2e = None
+    if e2e_times:
+        e2e_s = statistics.mean(e2e_times)
+        e2e = {"value": world * n * fmm_steps / e2e_s, "unit": "body-steps/s",
+               "h2d_bytes_per_step": n * 32, "d2h_bytes_per_step": n * 32,
+               "ms_per_step": 1e3 * e2e_s, "timer": "host wall clock"}
+
+    line = {
+        "metric": "body-steps/s", "value": value, "unit": "body-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded, numpy PCG64): " + w["desc"],
+        "config": {"workload": args.workload, "form": "plain single-scene solve",
+                   "bodies": n, "fmm_steps_per_bench_step": fmm_steps, "depth": solver.depth,
+                   "cells": solver.cells, "fixed_point_scale": solver.scale,
+                   "l2": "flushed between timed steps (512 MiB write outside the events)",
+                   "parallelism": "replicas x%d" % world},
+        "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
+        "kernel_avg_ms": kernel_ms,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    solver.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse_args()
+    w = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        return run_reference(args, w)
+    return run_gpu(args, w)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -181,4 +181,15 @@ int rfmm_device_error(rfmm_handle *h, uint32_t *code, uint32_t *info) {
   return h->engine->device_error(code, info);
 }
 
+int rfmm_profile_steps(rfmm_handle *h, uint32_t steps, float *kernel_ms, uint32_t *launches) {
+  if (guard(h) || kernel_ms == nullptr || launches == nullptr) return RFMM_ERR_INVALID;
+  return h->engine->profile_steps(steps, kernel_ms, launches);
+}
+
+int rfmm_launch_count(rfmm_handle *h, uint64_t *out) {
+  if (guard(h) || out == nullptr) return RFMM_ERR_INVALID;
+  *out = h->engine->launch_count();
+  return RFMM_OK;
+}
+
 }  // extern "C"

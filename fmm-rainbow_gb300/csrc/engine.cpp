@@ -120,7 +120,7 @@ int Engine::create(const std::vector<SceneSpec> &specs, Engine **out) {
     d.n_f = (float)sp.n;
     d.control_strength = sp.params.control_strength;
     d.control_radius = sp.params.control_radius;
-    d.key_base = i << 18;
+    d.key_base = 0u;  // set below, once the number of scenes fixes the key width
     for (int k = 0; k < 4; k++) {
       d.control_point[k] = sp.params.control_point[k];
       d.control_axis_mode[k] = sp.params.control_axis_mode[k];
@@ -139,7 +139,18 @@ int Engine::create(const std::vector<SceneSpec> &specs, Engine **out) {
   E->tiles_ = body_off / kTile;
   E->cells_ = cell_off;
   E->tasks_ = task_off;
-  E->key_bits_ = 18u + log2_ceil((uint32_t)specs.size());
+  // Sort key = scene rank above a Morton code of fine cells (level F >= depth):
+  // bodies of one leaf stay contiguous and a warp's bodies stay spatially
+  // compact, so a few steps of drift still leave few leaf runs per warp.
+  {
+    const uint32_t scene_bits = log2_ceil((uint32_t)specs.size());
+    const uint32_t fine = std::min(10u, (32u - scene_bits) / 3u);
+    for (uint32_t i = 0; i < E->scenes_.size(); i++) {
+      E->scenes_[i].key_level = fine;
+      E->scenes_[i].key_base = scene_bits ? (i << (3u * fine)) : 0u;
+    }
+    E->key_bits_ = scene_bits + 3u * fine;
+  }
   E->uploaded_.assign(specs.size(), false);
 
   int st = RFMM_OK;
@@ -159,6 +170,7 @@ int Engine::create(const std::vector<SceneSpec> &specs, Engine **out) {
     A((void **)&E->sort_.vals[b], 4 * S);
   }
   A((void **)&E->d_src_, 16 * C);
+  A((void **)&E->d_aux_, 8 * C);
   A((void **)&E->d_lfield_, 48 * C);
   A((void **)&E->d_fields_, 48 * C);
   A((void **)&E->d_ctr_, sizeof(Counters));
@@ -178,6 +190,7 @@ int Engine::create(const std::vector<SceneSpec> &specs, Engine **out) {
       if (e == cudaSuccess) e = cudaEventCreate(&ev);
   }
   if (e == cudaSuccess) e = configure_tree_kernels();
+  if (e == cudaSuccess) E->body_ctas_ = (uint32_t)E->sms_ * body_ctas_per_sm();
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(E->d_scenes_, E->scenes_.data(), sizeof(SceneDesc) * specs.size(),
                         cudaMemcpyHostToDevice, E->stream_);
@@ -193,6 +206,7 @@ int Engine::create(const std::vector<SceneSpec> &specs, Engine **out) {
     if (e == cudaSuccess) e = cudaMemsetAsync(E->d_ids_[b], 0, 4 * S, E->stream_);
   }
   if (e == cudaSuccess) e = cudaMemsetAsync(E->d_src_, 0, 16 * C, E->stream_);
+  if (e == cudaSuccess) e = cudaMemsetAsync(E->d_aux_, 0, 8 * C, E->stream_);
   if (e == cudaSuccess) e = cudaMemsetAsync(E->d_lfield_, 0, 48 * C, E->stream_);
   if (e == cudaSuccess) e = cudaMemsetAsync(E->d_fields_, 0, 48 * C, E->stream_);
   if (e == cudaSuccess) e = cudaMemsetAsync(E->d_ctr_, 0, sizeof(Counters), E->stream_);
@@ -237,7 +251,7 @@ int Engine::build_tensor_maps() {
 
 Engine::~Engine() {
   if (stream_ != nullptr) cudaStreamSynchronize(stream_);
-  for (auto &kv : graphs_) cudaGraphExecDestroy(kv.second);
+  for (auto &kv : graphs_) cudaGraphExecDestroy(kv.second.exec);
   for (auto &ev : ev_)
     if (ev != nullptr) cudaEventDestroy(ev);
   for (void *p : allocations_) cudaFree(p);
@@ -286,6 +300,7 @@ LaunchCtx Engine::ctx(uint32_t mpar, uint32_t lpar, uint32_t ppar) const {
   L.mom = d_mom_[mpar];
   L.mom_next = d_mom_[mpar ^ 1u];
   L.src = d_src_;
+  L.aux = d_aux_;
   L.lfield = d_lfield_;
   L.fields = d_fields_;
   L.plist = d_plist_[lpar];
@@ -294,6 +309,7 @@ LaunchCtx Engine::ctx(uint32_t mpar, uint32_t lpar, uint32_t ppar) const {
   L.ctr = d_ctr_;
   L.tickets = d_tickets_;
   L.tmaps = d_tmaps_;
+  L.body_ctas = body_ctas_;
   return L;
 }
 
@@ -304,6 +320,7 @@ int Engine::upload(uint32_t scene, const void *src, size_t bytes, cudaMemcpyKind
   RF_CK(cudaMemcpyAsync(d_part_[pcur_] + 2ull * d.body_off, src, bytes, kind, stream_));
   launch_iota(stream_, d_ids_[pcur_] + d.body_off, pad_tiles(d.n) * kTile);
   RF_CK(cudaGetLastError());
+  launches_ += 1;
   uploaded_[scene] = true;
   committed_ = false;
   return RFMM_OK;
@@ -316,10 +333,13 @@ int Engine::seed_galaxy(uint32_t scene) {
   launch_initialize(L, d_part_[pcur_], d.tile_off, pad_tiles(d.n));
   launch_iota(stream_, d_ids_[pcur_] + d.body_off, pad_tiles(d.n) * kTile);
   RF_CK(cudaGetLastError());
+  launches_ += 2;
   uploaded_[scene] = true;
   committed_ = false;
   return RFMM_OK;
 }
+
+uint32_t Engine::resort_kernels() const { return 2u + 3u * ((key_bits_ + 7u) / 8u); }
 
 void Engine::enqueue_resort(uint32_t ppar) {
   LaunchCtx L = ctx(mcur_, lpar_, ppar);
@@ -339,6 +359,7 @@ int Engine::commit() {
   launch_gather(L, sort_.vals[r], d_part_[pcur_], d_ids_[pcur_], d_part_[pcur_ ^ 1u],
                 d_ids_[pcur_ ^ 1u], d_mom_[mcur_], tiles_);
   RF_CK(cudaGetLastError());
+  launches_ += resort_kernels();
   pcur_ ^= 1u;
   committed_ = true;
   solved_ = false;
@@ -362,6 +383,7 @@ int Engine::solve_fields() {
   launch_m2l(L, lpar_, (uint32_t)sms_ * 3u);
   launch_l2l_near(L, lpar_, (uint32_t)sms_ * 8u);
   RF_CK(cudaGetLastError());
+  launches_ += 3;
   lpar_ ^= 1u;
   tree_buf_ = (int)mcur_;
   solved_ = true;
@@ -385,9 +407,11 @@ int Engine::launch_chunk(uint32_t len, bool sort_at_end) {
     e = cudaGraphInstantiate(&exec, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return cuda_status(e);
-    it = graphs_.emplace(key, exec).first;
+    const uint32_t kernels = len * kernels_per_step() + (sort_at_end ? resort_kernels() : 0u);
+    it = graphs_.emplace(key, Graph{exec, kernels}).first;
   }
-  RF_CK(cudaGraphLaunch(it->second, stream_));
+  RF_CK(cudaGraphLaunch(it->second.exec, stream_));
+  launches_ += it->second.kernels;
   const uint32_t flip = len & 1u;
   tree_buf_ = (int)(mcur_ ^ ((len - 1u) & 1u));
   mcur_ ^= flip;
@@ -402,6 +426,7 @@ int Engine::step(uint32_t steps) {
     if (resort_interval_ > 0 && since_sort_ >= resort_interval_) {
       enqueue_resort(pcur_);
       RF_CK(cudaGetLastError());
+      launches_ += resort_kernels();
       pcur_ ^= 1u;
       since_sort_ = 0;
     }
@@ -518,6 +543,7 @@ int Engine::phase_times(float ms[7]) {
   launch_integrate(L, tiles_);
   RF_CK(cudaEventRecord(ev_[4], stream_));
   RF_CK(cudaGetLastError());
+  launches_ += 5;
   tree_buf_ = (int)mcur_;
   mcur_ ^= 1u;
   lpar_ ^= 1u;
@@ -539,6 +565,63 @@ int Engine::phase_times(float ms[7]) {
   ms[5] = 0.0f;   // near: fused into downward
   ms[6] = t[4];   // integrate (+ next deposit)
   return RFMM_OK;
+}
+
+int Engine::profile_steps(uint32_t steps, float ms[kKernelKinds], uint32_t launches[kKernelKinds]) {
+  if (!committed_ || ms == nullptr || launches == nullptr) return RFMM_ERR_INVALID;
+  // Every launch is enqueued back to back between its own event pair, so the
+  // GPU never idles waiting for the host and each pair brackets device time.
+  struct Rec {
+    int kind;
+    cudaEvent_t a, b;
+  };
+  std::vector<Rec> recs;
+  int st = RFMM_OK;
+  auto timed = [&](int kind, auto &&enqueue) {
+    Rec r{kind, nullptr, nullptr};
+    if (st != RFMM_OK) return;
+    cudaError_t e = cudaEventCreate(&r.a);
+    if (e == cudaSuccess) e = cudaEventCreate(&r.b);
+    if (e == cudaSuccess) e = cudaEventRecord(r.a, stream_);
+    if (e == cudaSuccess) enqueue();
+    if (e == cudaSuccess) e = cudaEventRecord(r.b, stream_);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    recs.push_back(r);
+    if (e != cudaSuccess) st = cuda_status(e);
+  };
+  for (uint32_t s = 0; s < steps && st == RFMM_OK; s++) {
+    if (resort_interval_ > 0 && since_sort_ >= resort_interval_) {
+      timed(kKResort, [&] { enqueue_resort(pcur_); });
+      launches_ += resort_kernels();
+      pcur_ ^= 1u;
+      since_sort_ = 0;
+    }
+    LaunchCtx L = ctx(mcur_, lpar_, pcur_);
+    timed(kKUpward, [&] { launch_upward(L, lpar_, tasks_); });
+    timed(kKM2L, [&] { launch_m2l(L, lpar_, (uint32_t)sms_ * 3u); });
+    timed(kKL2LNear, [&] { launch_l2l_near(L, lpar_, (uint32_t)sms_ * 8u); });
+    timed(kKIntegrate, [&] { launch_integrate(L, tiles_); });
+    launches_ += kernels_per_step();
+    tree_buf_ = (int)mcur_;
+    mcur_ ^= 1u;
+    lpar_ ^= 1u;
+    since_sort_++;
+  }
+  solved_ = true;
+  cudaError_t e = cudaStreamSynchronize(stream_);
+  if (st == RFMM_OK && e != cudaSuccess) st = cuda_status(e);
+  for (Rec &r : recs) {
+    float t = 0.0f;
+    if (st == RFMM_OK && r.a != nullptr && r.b != nullptr &&
+        cudaEventElapsedTime(&t, r.a, r.b) == cudaSuccess) {
+      ms[r.kind] += t;
+      launches[r.kind] += 1u;
+    }
+    if (r.a != nullptr) cudaEventDestroy(r.a);
+    if (r.b != nullptr) cudaEventDestroy(r.b);
+  }
+  if (st != RFMM_OK) return st;
+  return check_device_error();
 }
 
 }  // namespace rfmm

@@ -21,6 +21,9 @@
 
 namespace rfmm {
 
+// Kernel kinds reported by profile_steps.
+enum KernelKind { kKUpward = 0, kKM2L, kKL2LNear, kKIntegrate, kKResort, kKernelKinds };
+
 struct SceneSpec {
   uint32_t n;
   rfmm_params params;
@@ -51,6 +54,10 @@ class Engine {
   int download(uint32_t scene, int which, void *dst, size_t bytes, cudaMemcpyKind kind);
   int digest(uint32_t scene, int which, uint32_t *out);
   int phase_times(float ms[7]);
+  // Runs `steps` frames with direct launches and CUDA events around every
+  // kernel; adds per-kind device time (ms) and launch counts.
+  int profile_steps(uint32_t steps, float ms[kKernelKinds], uint32_t launches[kKernelKinds]);
+  uint64_t launch_count() const { return launches_; }
   int device_error(uint32_t *code, uint32_t *info);
 
   uint32_t num_scenes() const { return (uint32_t)scenes_.size(); }
@@ -72,6 +79,7 @@ class Engine {
 
   int device_ = 0;
   int sms_ = 0;
+  uint32_t body_ctas_ = 0;
   cudaStream_t stream_ = nullptr;
   cudaStream_t own_stream_ = nullptr;
 
@@ -87,6 +95,7 @@ class Engine {
   uint4 *d_mom_[2] = {nullptr, nullptr};
   uint4 *d_mom_scratch_ = nullptr;
   float4 *d_src_ = nullptr;
+  float2 *d_aux_ = nullptr;
   float *d_lfield_ = nullptr, *d_fields_ = nullptr;
   WorkItem *d_plist_[2] = {nullptr, nullptr};
   Counters *d_ctr_ = nullptr;
@@ -106,7 +115,13 @@ class Engine {
   uint32_t resort_interval_ = 16, since_sort_ = 0;
   std::vector<bool> uploaded_;
 
-  std::map<std::tuple<uint32_t, uint32_t, uint32_t, uint32_t, bool>, cudaGraphExec_t> graphs_;
+  struct Graph {
+    cudaGraphExec_t exec;
+    uint32_t kernels;  // kernel launches per graph launch
+  };
+  std::map<std::tuple<uint32_t, uint32_t, uint32_t, uint32_t, bool>, Graph> graphs_;
+  uint64_t launches_ = 0;  // kernels this engine has launched (graph nodes included)
+  uint32_t resort_kernels() const;
   cudaEvent_t ev_[8] = {};
 };
 

@@ -23,8 +23,9 @@ namespace rfmm {
 // Leaf (level `depth`) cell of a position, local to the scene's tree.
 __device__ __forceinline__ uint32_t leaf_cell(float x, float y, float z, uint32_t depth) {
   const uint32_t dim = 1u << depth;
-  return level_offset_d(depth) + lin3(cell_of_unit(unit_coord(x), dim), cell_of_unit(unit_coord(y), dim),
-                                      cell_of_unit(unit_coord(z), dim), dim);
+  return level_offset_d(depth) + lin3_lv(cell_of_unit(unit_coord(x), dim),
+                                         cell_of_unit(unit_coord(y), dim),
+                                         cell_of_unit(unit_coord(z), dim), depth);
 }
 
 __device__ __forceinline__ float length3(float x, float y, float z) {
@@ -44,25 +45,21 @@ __device__ __forceinline__ void soft_wall(float &p, float &v, float world_edge, 
   }
 }
 
-__global__ void __launch_bounds__(256) k_integrate(const SceneDesc *__restrict__ scenes,
-                                                   const uint32_t *__restrict__ tile_scene,
-                                                   float4 *__restrict__ part,
-                                                   const uint4 *__restrict__ mom,
-                                                   const float4 *__restrict__ src,
-                                                   const float *__restrict__ fields,
-                                                   uint4 *__restrict__ mom_next) {
-  const uint32_t tile = blockIdx.x;
-  const SceneDesc &S = scenes[tile_scene[tile]];
-  const uint32_t slot = tile * kTile + threadIdx.x;
-  const bool active = slot - S.body_off < S.n;
-  uint32_t key = 0xFFFFFFFFu;
-  int32_t qx = 0, qy = 0, qz = 0;
-  if (active) {
-    const float4 p0 = part[2u * slot], p1 = part[2u * slot + 1u];
+// One body's integrate (wgsl:613-771).  Writes the new state into p0/p1 and
+// the new position's leaf cell and fixed-point coordinates (the next deposit).
+__device__ __forceinline__ void integrate_body(const SceneDesc &S, float4 &p0, float4 &p1,
+                                               const uint4 *__restrict__ mom,
+                                               const float4 *__restrict__ src,
+                                               const float2 *__restrict__ aux,
+                                               const float *__restrict__ fields, uint32_t &key,
+                                               int32_t &qx, int32_t &qy, int32_t &qz) {
     float px = p0.x, py = p0.y, pz = p0.z;
     float vx = p1.x, vy = p1.y, vz = p1.z;
     const uint32_t D = S.depth;
-    const float ux = unit_coord(px), uy = unit_coord(py), uz = unit_coord(pz);
+    // Leaf coordinates; floor(u * 2^l) == floor(u * 2^D) >> (D - l).
+    const uint32_t dimD = 1u << D;
+    const uint32_t lx = cell_of_unit(unit_coord(px), dimD), ly = cell_of_unit(unit_coord(py), dimD),
+                   lz = cell_of_unit(unit_coord(pz), dimD);
 
     // Adaptive descent (wgsl:625-639): first level whose cell holds at most
     // 16 bodies, else the leaf level.  The level loads are independent.
@@ -70,9 +67,8 @@ __global__ void __launch_bounds__(256) k_integrate(const SceneDesc *__restrict__
 #pragma unroll
     for (uint32_t l = 6u; l >= 1u; l--) {
       if (l <= D) {
-        const uint32_t dim = 1u << l;
-        const uint32_t idx = S.cell_off + level_offset_d(l) +
-                             lin3(cell_of_unit(ux, dim), cell_of_unit(uy, dim), cell_of_unit(uz, dim), dim);
+        const uint32_t sh = D - l;
+        const uint32_t idx = S.cell_off + level_offset_d(l) + lin3_lv(lx >> sh, ly >> sh, lz >> sh, l);
         const uint32_t c = __ldg(&mom[idx].x);
         if ((int32_t)c <= (int32_t)kAdaptive || l == D) {
           chosen = l;
@@ -81,10 +77,10 @@ __global__ void __launch_bounds__(256) k_integrate(const SceneDesc *__restrict__
         }
       }
     }
-    const uint32_t cdim = 1u << chosen;
-    const float cx = cell_center_axis(cell_of_unit(ux, cdim), cdim);
-    const float cy = cell_center_axis(cell_of_unit(uy, cdim), cdim);
-    const float cz = cell_center_axis(cell_of_unit(uz, cdim), cdim);
+    const uint32_t csh = D - chosen;
+    const float cx = cell_center_lv(lx >> csh, chosen);
+    const float cy = cell_center_lv(ly >> csh, chosen);
+    const float cz = cell_center_lv(lz >> csh, chosen);
 
     const float4 *fp = reinterpret_cast<const float4 *>(fields + (size_t)cell_index * 12u);
     const float4 fa = __ldg(fp), fj0 = __ldg(fp + 1), fj1 = __ldg(fp + 2);
@@ -94,13 +90,14 @@ __global__ void __launch_bounds__(256) k_integrate(const SceneDesc *__restrict__
     float az = fa.z + (fj0.z * rx + fj1.x * ry + fj1.y * rz);
 
     // Self leaf: softened monopole of the other count-1 bodies (wgsl:646-657).
+    // x / 2^l == x * 2^-l exactly, so the eps division is a scaling.
+    const float2 ax2 = __ldg(&aux[cell_index]);
     if (count > 1u) {
       const float4 s = __ldg(&src[cell_index]);
       const float dx = s.x - px, dy = s.y - py, dz = s.z - pz;
-      const float eps = fmaxf(S.softening, 0.62f * kHalf / (float)cdim);
+      const float eps = fmaxf(S.softening, (0.62f * kHalf) * pow2_neg(chosen));
       const float inv_r = 1.0f / sqrtf((dx * dx + dy * dy) + dz * dz + eps * eps);
-      const float self_mass = (float)(count - 1u) / S.n_f;
-      const float gsm = S.gravity * self_mass;
+      const float gsm = ax2.x;  // G * f32(count - 1) / f32(N)
       ax = ax + gsm * dx * inv_r * inv_r * inv_r;
       ay = ay + gsm * dy * inv_r * inv_r * inv_r;
       az = az + gsm * dz * inv_r * inv_r * inv_r;
@@ -148,7 +145,7 @@ __global__ void __launch_bounds__(256) k_integrate(const SceneDesc *__restrict__
     const float signed_radial = clampf_d(pv / (radius * vlen), -1.0f, 1.0f);
     const float rf = fabsf(signed_radial);
     const float radial_shock = rf * rf * rf;
-    const float density_pulse = clampf_d(((float)count - (float)kAdaptive) / 72.0f, 0.0f, 1.0f);
+    const float density_pulse = ax2.y;  // clamp((f32(count) - 16) / 72, 0, 1)
     const float field_strength = clampf_d(length3(ax, ay, az) * (radius + 0.12f) * 0.58f, 0.0f, 1.0f);
     const float target_exc = clampf_d(0.025f + radial_shock * 0.56f + density_pulse * 0.26f +
                                           field_strength * 0.13f + control_influence * 0.42f,
@@ -176,38 +173,99 @@ __global__ void __launch_bounds__(256) k_integrate(const SceneDesc *__restrict__
                                   (0.012f + signed_radial * 0.030f + exc * 0.036f +
                                    control_influence * 0.080f);
     const float hue = hsum - floorf(hsum);
-    part[2u * slot] = make_float4(px, py, pz, hue);
-    part[2u * slot + 1u] = make_float4(vx, vy, vz, exc);
+    p0 = make_float4(px, py, pz, hue);
+    p1 = make_float4(vx, vy, vz, exc);
 
     // The next step's deposit (wgsl:414-421 on the new position).
     key = S.cell_off + leaf_cell(px, py, pz, D);
     qx = f2i_rn_sat(px * S.scale);
     qy = f2i_rn_sat(py * S.scale);
     qz = f2i_rn_sat(pz * S.scale);
+}
+
+// Persistent integrate: each CTA walks a contiguous slice of body tiles
+// (leaf-sorted, so its bodies are spatially compact), integrates every body
+// and accumulates the next step's deposit in a shared-memory table flushed
+// once at the end.
+__global__ void __launch_bounds__(256) k_integrate(const SceneDesc *__restrict__ scenes,
+                                                   const uint32_t *__restrict__ tile_scene,
+                                                   float4 *__restrict__ part,
+                                                   const uint4 *__restrict__ mom,
+                                                   const float4 *__restrict__ src,
+                                                   const float2 *__restrict__ aux,
+                                                   const float *__restrict__ fields,
+                                                   uint4 *__restrict__ mom_next, uint32_t tiles) {
+  __shared__ DepositTable T;
+  __shared__ SceneDesc S;
+  uint32_t t0, t1;
+  cta_tile_range(tiles, t0, t1);
+  T.clear();
+  uint32_t cur = 0xFFFFFFFFu;
+  // The next tile's bodies are loaded one iteration ahead.
+  float4 n0 = make_float4(0.f, 0.f, 0.f, 0.f), n1 = n0;
+  if (t0 < t1) {
+    n0 = part[2u * (t0 * kTile + threadIdx.x)];
+    n1 = part[2u * (t0 * kTile + threadIdx.x) + 1u];
   }
-  deposit_segmented(key, active, qx, qy, qz, mom_next);
+  for (uint32_t tile = t0; tile < t1; tile++) {
+    const uint32_t slot = tile * kTile + threadIdx.x;
+    float4 p0 = n0, p1 = n1;
+    if (tile + 1u < t1) {
+      n0 = part[2u * (slot + kTile)];
+      n1 = part[2u * (slot + kTile) + 1u];
+    }
+    const uint32_t sc = tile_scene[tile];
+    if (sc != cur) {
+      load_scene(S, scenes, sc);
+      cur = sc;
+    }
+    const bool active = slot - S.body_off < S.n;
+    uint32_t key = DepositTable::kEmpty;
+    int32_t qx = 0, qy = 0, qz = 0;
+    if (active) {
+      integrate_body(S, p0, p1, mom, src, aux, fields, key, qx, qy, qz);
+      part[2u * slot] = p0;
+      part[2u * slot + 1u] = p1;
+    }
+    deposit_body(T, key, active, qx, qy, qz, mom_next);
+  }
+  __syncthreads();
+  T.flush(mom_next);
 }
 
 // Standalone P2M: deposit the current positions into `moments` (leaf level
-// must be zero).
+// must be zero).  Persistent like k_integrate.
 __global__ void __launch_bounds__(256) k_deposit(const SceneDesc *__restrict__ scenes,
                                                  const uint32_t *__restrict__ tile_scene,
                                                  const float4 *__restrict__ part,
-                                                 uint4 *__restrict__ moments) {
-  const uint32_t tile = blockIdx.x;
-  const SceneDesc &S = scenes[tile_scene[tile]];
-  const uint32_t slot = tile * kTile + threadIdx.x;
-  const bool active = slot - S.body_off < S.n;
-  uint32_t key = 0xFFFFFFFFu;
-  int32_t qx = 0, qy = 0, qz = 0;
-  if (active) {
+                                                 uint4 *__restrict__ moments, uint32_t tiles) {
+  __shared__ DepositTable T;
+  __shared__ SceneDesc S;
+  uint32_t t0, t1;
+  cta_tile_range(tiles, t0, t1);
+  T.clear();
+  uint32_t cur = 0xFFFFFFFFu;
+  for (uint32_t tile = t0; tile < t1; tile++) {
+    const uint32_t slot = tile * kTile + threadIdx.x;
     const float4 p = part[2u * slot];
-    key = S.cell_off + leaf_cell(p.x, p.y, p.z, S.depth);
-    qx = f2i_rn_sat(p.x * S.scale);
-    qy = f2i_rn_sat(p.y * S.scale);
-    qz = f2i_rn_sat(p.z * S.scale);
+    const uint32_t sc = tile_scene[tile];
+    if (sc != cur) {
+      load_scene(S, scenes, sc);
+      cur = sc;
+    }
+    const bool active = slot - S.body_off < S.n;
+    uint32_t key = DepositTable::kEmpty;
+    int32_t qx = 0, qy = 0, qz = 0;
+    if (active) {
+      key = S.cell_off + leaf_cell(p.x, p.y, p.z, S.depth);
+      qx = f2i_rn_sat(p.x * S.scale);
+      qy = f2i_rn_sat(p.y * S.scale);
+      qz = f2i_rn_sat(p.z * S.scale);
+    }
+    deposit_body(T, key, active, qx, qy, qz, moments);
   }
-  deposit_segmented(key, active, qx, qy, qz, moments);
+  __syncthreads();
+  T.flush(moments);
 }
 
 // 3-D Morton interleave of leaf coordinates (x in bit 0).
@@ -229,10 +287,12 @@ __global__ void __launch_bounds__(256) k_keys(const SceneDesc *__restrict__ scen
   const SceneDesc &S = scenes[tile_scene[tile]];
   const uint32_t slot = tile * kTile + threadIdx.x;
   const uint32_t local = slot - S.body_off;
-  uint32_t key = S.key_base | 0x3FFFFu;  // padding sorts after every body of its scene
+  const uint32_t F = S.key_level;
+  uint32_t key = S.key_base | ((1u << (3u * F)) - 1u);  // padding sorts after its scene's bodies
   if (local < S.n) {
     const float4 p = part[2u * slot];
-    const uint32_t dim = 1u << S.depth;
+    const uint32_t dim = 1u << F;
+    // floor(u * 2^F) >> (F - depth) == floor(u * 2^depth): the fine key refines the leaf key.
     key = S.key_base | (spread3(cell_of_unit(unit_coord(p.x), dim)) |
                         (spread3(cell_of_unit(unit_coord(p.y), dim)) << 1) |
                         (spread3(cell_of_unit(unit_coord(p.z), dim)) << 2));
@@ -242,6 +302,9 @@ __global__ void __launch_bounds__(256) k_keys(const SceneDesc *__restrict__ scen
   if (fresh_ids) ids[slot] = local;
 }
 
+// Apply a permutation to the resident bodies (and their caller ids).  With
+// `deposit_into`, the permuted bodies are also deposited (persistent grid,
+// per-CTA deposit table); otherwise one CTA per tile.
 __global__ void __launch_bounds__(256) k_gather(const SceneDesc *__restrict__ scenes,
                                                 const uint32_t *__restrict__ tile_scene,
                                                 const uint32_t *__restrict__ perm,
@@ -249,27 +312,45 @@ __global__ void __launch_bounds__(256) k_gather(const SceneDesc *__restrict__ sc
                                                 const uint32_t *__restrict__ ids_in,
                                                 float4 *__restrict__ part_out,
                                                 uint32_t *__restrict__ ids_out,
-                                                uint4 *__restrict__ deposit_into, uint32_t nslots) {
-  const uint32_t tile = blockIdx.x;
-  const uint32_t slot = tile * kTile + threadIdx.x;
-  uint32_t from = perm[slot];
-  if (from >= nslots) from = slot;  // defensive: a permutation never leaves the buffer
-  const float4 p0 = part_in[2u * from], p1 = part_in[2u * from + 1u];
-  part_out[2u * slot] = p0;
-  part_out[2u * slot + 1u] = p1;
-  ids_out[slot] = ids_in[from];
+                                                uint4 *__restrict__ deposit_into, uint32_t tiles) {
+  __shared__ DepositTable T;
+  __shared__ SceneDesc S;
+  const uint32_t nslots = tiles * kTile;
+  uint32_t t0 = blockIdx.x, t1 = blockIdx.x + 1u;
   if (deposit_into != nullptr) {
-    const SceneDesc &S = scenes[tile_scene[tile]];
-    const bool active = slot - S.body_off < S.n;
-    uint32_t key = 0xFFFFFFFFu;
-    int32_t qx = 0, qy = 0, qz = 0;
-    if (active) {
-      key = S.cell_off + leaf_cell(p0.x, p0.y, p0.z, S.depth);
-      qx = f2i_rn_sat(p0.x * S.scale);
-      qy = f2i_rn_sat(p0.y * S.scale);
-      qz = f2i_rn_sat(p0.z * S.scale);
+    cta_tile_range(tiles, t0, t1);
+    T.clear();
+  }
+  uint32_t cur = 0xFFFFFFFFu;
+  for (uint32_t tile = t0; tile < t1; tile++) {
+    const uint32_t slot = tile * kTile + threadIdx.x;
+    uint32_t from = perm[slot];
+    if (from >= nslots) from = slot;  // defensive: a permutation never leaves the buffer
+    const float4 p0 = part_in[2u * from], p1 = part_in[2u * from + 1u];
+    part_out[2u * slot] = p0;
+    part_out[2u * slot + 1u] = p1;
+    ids_out[slot] = ids_in[from];
+    if (deposit_into != nullptr) {
+      const uint32_t sc = tile_scene[tile];
+      if (sc != cur) {
+        load_scene(S, scenes, sc);
+        cur = sc;
+      }
+      const bool active = slot - S.body_off < S.n;
+      uint32_t key = DepositTable::kEmpty;
+      int32_t qx = 0, qy = 0, qz = 0;
+      if (active) {
+        key = S.cell_off + leaf_cell(p0.x, p0.y, p0.z, S.depth);
+        qx = f2i_rn_sat(p0.x * S.scale);
+        qy = f2i_rn_sat(p0.y * S.scale);
+        qz = f2i_rn_sat(p0.z * S.scale);
+      }
+      deposit_body(T, key, active, qx, qy, qz, deposit_into);
     }
-    deposit_segmented(key, active, qx, qy, qz, deposit_into);
+  }
+  if (deposit_into != nullptr) {
+    __syncthreads();
+    T.flush(deposit_into);
   }
 }
 
@@ -405,13 +486,26 @@ __global__ void __launch_bounds__(256) k_initialize(const SceneDesc *__restrict_
 
 // --------------------------------------------------------------- launches
 
+uint32_t body_ctas_per_sm() {
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_integrate, kTile, 0) != cudaSuccess || n < 1)
+    n = 1;
+  return (uint32_t)n;
+}
+
+// Persistent body-pass grid: whole waves of resident CTAs, at most one per tile.
+static uint32_t body_grid(const LaunchCtx &L, uint32_t tiles) {
+  return tiles < L.body_ctas ? tiles : L.body_ctas;
+}
+
 void launch_integrate(const LaunchCtx &L, uint32_t tiles) {
-  k_integrate<<<tiles, kTile, 0, L.stream>>>(L.scenes, L.tile_scene, L.part, L.mom, L.src, L.fields,
-                                             L.mom_next);
+  k_integrate<<<body_grid(L, tiles), kTile, 0, L.stream>>>(L.scenes, L.tile_scene, L.part, L.mom,
+                                                           L.src, L.aux, L.fields, L.mom_next, tiles);
 }
 
 void launch_deposit(const LaunchCtx &L, uint4 *moments, uint32_t tiles) {
-  k_deposit<<<tiles, kTile, 0, L.stream>>>(L.scenes, L.tile_scene, L.part, moments);
+  k_deposit<<<body_grid(L, tiles), kTile, 0, L.stream>>>(L.scenes, L.tile_scene, L.part, moments,
+                                                         tiles);
 }
 
 void launch_keys(const LaunchCtx &L, uint32_t *keys, uint32_t *vals, uint32_t *ids, int fresh_ids,
@@ -422,8 +516,9 @@ void launch_keys(const LaunchCtx &L, uint32_t *keys, uint32_t *vals, uint32_t *i
 void launch_gather(const LaunchCtx &L, const uint32_t *perm, const float4 *part_in,
                    const uint32_t *ids_in, float4 *part_out, uint32_t *ids_out, uint4 *deposit_into,
                    uint32_t tiles) {
-  k_gather<<<tiles, kTile, 0, L.stream>>>(L.scenes, L.tile_scene, perm, part_in, ids_in, part_out,
-                                          ids_out, deposit_into, tiles * kTile);
+  const uint32_t grid = deposit_into != nullptr ? body_grid(L, tiles) : tiles;
+  k_gather<<<grid, kTile, 0, L.stream>>>(L.scenes, L.tile_scene, perm, part_in, ids_in, part_out,
+                                         ids_out, deposit_into, tiles);
 }
 
 void launch_unpermute(const LaunchCtx &L, const uint32_t *ids, float4 *out, uint32_t tile_base,

@@ -40,16 +40,18 @@ __device__ __forceinline__ uint4 add_moment(uint4 a, uint4 b) {
 }
 
 __device__ __forceinline__ void store_cell(const SceneDesc &S, uint32_t local_cell, uint4 m,
-                                           uint4 *mom, float4 *src) {
+                                           uint4 *mom, float4 *src, float2 *aux) {
   const uint32_t g = S.cell_off + local_cell;
   mom[g] = m;
   src[g] = make_source(m, S.scale, S.gravity, S.n_f);
+  aux[g] = make_aux(m.x, S.gravity, S.n_f);
 }
 
 __global__ void __launch_bounds__(512) k_upward(const SceneDesc *__restrict__ scenes,
                                                 const uint32_t *__restrict__ task_scene,
                                                 uint4 *__restrict__ mom, uint4 *__restrict__ mom_next,
-                                                float4 *__restrict__ src, float *__restrict__ fields,
+                                                float4 *__restrict__ src, float2 *__restrict__ aux,
+                                                float *__restrict__ fields,
                                                 WorkItem *__restrict__ plist, uint32_t plist_cap,
                                                 const WorkItem *__restrict__ plist_prev,
                                                 Counters *__restrict__ ctr, uint32_t list_par,
@@ -98,6 +100,7 @@ __global__ void __launch_bounds__(512) k_upward(const SceneDesc *__restrict__ sc
     const uint4 m = mom[S.cell_off + leaf];
     s0[tid] = m;
     src[S.cell_off + leaf] = make_source(m, S.scale, S.gravity, S.n_f);
+    aux[S.cell_off + leaf] = make_aux(m.x, S.gravity, S.n_f);
     mom_next[S.cell_off + leaf] = make_uint4(0u, 0u, 0u, 0u);
   }
   __syncthreads();
@@ -115,7 +118,7 @@ __global__ void __launch_bounds__(512) k_upward(const SceneDesc *__restrict__ sc
     s1[tid] = acc;
     const uint32_t dim = 1u << (D - 1u);
     const uint32_t cell = level_offset_d(D - 1u) + lin3(sx * 4u + x, sy * 4u + y, sz * 4u + z, dim);
-    store_cell(S, cell, acc, mom, src);
+    store_cell(S, cell, acc, mom, src, aux);
     if ((int32_t)acc.x > (int32_t)kAdaptive) s_items[atomicAdd(&s_nitems, 1u)] = {scene, cell};
   }
   __syncthreads();
@@ -132,7 +135,7 @@ __global__ void __launch_bounds__(512) k_upward(const SceneDesc *__restrict__ sc
     s2[tid] = acc;
     const uint32_t dim = 1u << (D - 2u);
     const uint32_t cell = level_offset_d(D - 2u) + lin3(sx * 2u + x, sy * 2u + y, sz * 2u + z, dim);
-    store_cell(S, cell, acc, mom, src);
+    store_cell(S, cell, acc, mom, src, aux);
     if ((int32_t)acc.x > (int32_t)kAdaptive) s_items[atomicAdd(&s_nitems, 1u)] = {scene, cell};
   }
   __syncthreads();
@@ -140,7 +143,7 @@ __global__ void __launch_bounds__(512) k_upward(const SceneDesc *__restrict__ sc
     uint4 acc = make_uint4(0u, 0u, 0u, 0u);
     for (uint32_t k = 0; k < 8u; k++) acc = add_moment(acc, s2[k]);
     const uint32_t cell = level_offset_d(r) + lin3(sx, sy, sz, rdim);
-    store_cell(S, cell, acc, mom, src);
+    store_cell(S, cell, acc, mom, src, aux);
     if ((int32_t)acc.x > (int32_t)kAdaptive) s_items[atomicAdd(&s_nitems, 1u)] = {scene, cell};
   }
   __syncthreads();
@@ -183,7 +186,7 @@ __global__ void __launch_bounds__(512) k_upward(const SceneDesc *__restrict__ sc
           for (uint32_t dx = 0; dx < 2u; dx++)
             acc = add_moment(acc, s0[lin3(2u * x + dx, 2u * y + dy, 2u * z + dz, cdim)]);
       const uint32_t cell = level_offset_d((uint32_t)l) + tid;
-      store_cell(S, cell, acc, mom, src);
+      store_cell(S, cell, acc, mom, src, aux);
       if ((int32_t)acc.x > (int32_t)kAdaptive) s_items[atomicAdd(&s_nitems, 1u)] = {scene, cell};
     }
     __syncthreads();
@@ -318,9 +321,9 @@ __global__ void __launch_bounds__(256) k_m2l(const SceneDesc *__restrict__ scene
     const uint32_t target = lvl_base + lin3(tx, ty, tz, dim);
     const bool live = mom[target].x != 0u;  // empty children are not targets
     if (live) {
-      const float ctx = cell_center_axis(tx, dim), cty = cell_center_axis(ty, dim),
-                  ctz = cell_center_axis(tz, dim);
-      const float eps = 0.06f * kHalf / (float)dim;  // wgsl:507
+      const float ctx = cell_center_lv(tx, l), cty = cell_center_lv(ty, l),
+                  ctz = cell_center_lv(tz, l);
+      const float eps = (0.06f * kHalf) * pow2_neg(l);  // wgsl:507, / 2^l as an exact scaling
       for (uint32_t k = lane; k < kTileCells; k += 32u) {
         // Reference loop order: source parent (pz, py, px) then child (cz, cy, cx).
         const uint32_t pidx = k >> 3, ch = k & 7u;
@@ -345,7 +348,9 @@ __global__ void __launch_bounds__(256) k_m2l(const SceneDesc *__restrict__ scene
       if (lane < 12u) {
         float acc = 0.0f;
         if (lane < 10u) {
+          // Strictly sequential sum in slot order; loads run 8 ahead of the adds.
           const float *row = sh.vals[warp][lane];
+#pragma unroll 8
           for (uint32_t k = 0; k < kTileCells; k++) acc = acc + row[k];
         }
         lfield[(size_t)target * 12u + lane] = acc;
@@ -387,47 +392,60 @@ __global__ void __launch_bounds__(256) k_l2l_near(const SceneDesc *__restrict__ 
     if (tcount == 0u) continue;  // warp-uniform
 
     // Top-down chain: f_level = m2l(level) + translate(f_parent), root field 0
-    // (the reference never writes cell 0's field, wgsl:459).
+    // (the reference never writes cell 0's field, wgsl:459).  The ancestors'
+    // M2L results are loaded up front; the chain itself is sequential.
+    float4 g[6][3];
+#pragma unroll
+    for (uint32_t a = 1u; a <= 6u; a++) {
+      if (a <= l) {
+        const uint32_t sh_ = l - a;
+        const uint32_t anc = S.cell_off + level_offset_d(a) + lin3_lv(tx >> sh_, ty >> sh_, tz >> sh_, a);
+        const float4 *lf = reinterpret_cast<const float4 *>(lfield + (size_t)anc * 12u);
+        g[a - 1][0] = __ldg(lf);
+        g[a - 1][1] = __ldg(lf + 1);
+        g[a - 1][2] = __ldg(lf + 2);
+      }
+    }
     float f[12];
 #pragma unroll
     for (int c = 0; c < 12; c++) f[c] = 0.0f;
-    for (uint32_t a = 1u; a <= l; a++) {
-      const uint32_t sh_ = l - a, adim = 1u << a, padim = adim >> 1;
-      const uint32_t ax = tx >> sh_, ay = ty >> sh_, az = tz >> sh_;
-      const uint32_t pax = ax >> 1, pay = ay >> 1, paz = az >> 1;
-      const float dx = cell_center_axis(ax, adim) - cell_center_axis(pax, padim);
-      const float dy = cell_center_axis(ay, adim) - cell_center_axis(pay, padim);
-      const float dz = cell_center_axis(az, adim) - cell_center_axis(paz, padim);
-      // inherited (wgsl:603-609): a += J . delta, phi -= a . delta, J unchanged.
-      float inh[12];
-      inh[0] = f[0] + (f[4] * dx + f[5] * dy + f[6] * dz);
-      inh[1] = f[1] + (f[5] * dx + f[7] * dy + f[8] * dz);
-      inh[2] = f[2] + (f[6] * dx + f[8] * dy + f[9] * dz);
-      inh[3] = f[3] - ((f[0] * dx + f[1] * dy) + f[2] * dz);
 #pragma unroll
-      for (int c = 4; c < 12; c++) inh[c] = f[c];
-      const uint32_t anc = S.cell_off + level_offset_d(a) + lin3(ax, ay, az, adim);
-      const float4 *lf = reinterpret_cast<const float4 *>(lfield + (size_t)anc * 12u);
-      const float4 g0 = __ldg(lf), g1 = __ldg(lf + 1), g2 = __ldg(lf + 2);
-      f[0] = g0.x + inh[0];
-      f[1] = g0.y + inh[1];
-      f[2] = g0.z + inh[2];
-      f[3] = g0.w + inh[3];
-      f[4] = g1.x + inh[4];
-      f[5] = g1.y + inh[5];
-      f[6] = g1.z + inh[6];
-      f[7] = g1.w + inh[7];
-      f[8] = g2.x + inh[8];
-      f[9] = g2.y + inh[9];
-      f[10] = g2.z + inh[10];
-      f[11] = g2.w + inh[11];
+    for (uint32_t a = 1u; a <= 6u; a++) {
+      if (a <= l) {
+        const uint32_t sh_ = l - a;
+        const uint32_t ax = tx >> sh_, ay = ty >> sh_, az = tz >> sh_;
+        const float dx = cell_center_lv(ax, a) - cell_center_lv(ax >> 1, a - 1u);
+        const float dy = cell_center_lv(ay, a) - cell_center_lv(ay >> 1, a - 1u);
+        const float dz = cell_center_lv(az, a) - cell_center_lv(az >> 1, a - 1u);
+        // inherited (wgsl:603-609): a += J . delta, phi -= a . delta, J unchanged.
+        float inh[12];
+        inh[0] = f[0] + (f[4] * dx + f[5] * dy + f[6] * dz);
+        inh[1] = f[1] + (f[5] * dx + f[7] * dy + f[8] * dz);
+        inh[2] = f[2] + (f[6] * dx + f[8] * dy + f[9] * dz);
+        inh[3] = f[3] - ((f[0] * dx + f[1] * dy) + f[2] * dz);
+#pragma unroll
+        for (int c = 4; c < 12; c++) inh[c] = f[c];
+        const float4 g0 = g[a - 1][0], g1 = g[a - 1][1], g2 = g[a - 1][2];
+        f[0] = g0.x + inh[0];
+        f[1] = g0.y + inh[1];
+        f[2] = g0.z + inh[2];
+        f[3] = g0.w + inh[3];
+        f[4] = g1.x + inh[4];
+        f[5] = g1.y + inh[5];
+        f[6] = g1.z + inh[6];
+        f[7] = g1.w + inh[7];
+        f[8] = g2.x + inh[8];
+        f[9] = g2.y + inh[9];
+        f[10] = g2.z + inh[10];
+        f[11] = g2.w + inh[11];
+      }
     }
 
     const bool leaf = tcount <= kAdaptive || l == S.depth;  // wgsl:537-541
     if (leaf) {
-      const float ctx = cell_center_axis(tx, dim), cty = cell_center_axis(ty, dim),
-                  ctz = cell_center_axis(tz, dim);
-      const float near_eps = fmaxf(S.softening, 0.72f * kHalf / (float)dim);
+      const float ctx = cell_center_lv(tx, l), cty = cell_center_lv(ty, l),
+                  ctz = cell_center_lv(tz, l);
+      const float near_eps = fmaxf(S.softening, (0.72f * kHalf) * pow2_neg(l));
       if (lane < 26u) {
         const uint32_t j = lane < 13u ? lane : lane + 1u;  // skip the centre (13)
         const int dx = (int)(j % 3u) - 1, dy = (int)((j / 3u) % 3u) - 1, dz = (int)(j / 9u) - 1;
@@ -468,7 +486,8 @@ __global__ void __launch_bounds__(256) k_l2l_near(const SceneDesc *__restrict__ 
 // --------------------------------------------------------------- launches
 
 void launch_upward(const LaunchCtx &L, uint32_t list_par, uint32_t tasks) {
-  k_upward<<<tasks, 512, 0, L.stream>>>(L.scenes, L.task_scene, L.mom, L.mom_next, L.src, L.fields,
+  k_upward<<<tasks, 512, 0, L.stream>>>(L.scenes, L.task_scene, L.mom, L.mom_next, L.src, L.aux,
+                                        L.fields,
                                         L.plist, L.plist_cap, L.plist_prev, L.ctr, list_par,
                                         L.tickets);
 }

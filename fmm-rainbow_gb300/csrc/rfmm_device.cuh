@@ -48,10 +48,19 @@ __device__ __forceinline__ uint32_t cell_of_unit(float u, uint32_t dim) {
   return (uint32_t)floorf(u * (float)dim);
 }
 
-// cell_center (wgsl:136-142) for one axis.
-__device__ __forceinline__ float cell_center_axis(uint32_t c, uint32_t dim) {
-  float w = 2.0f / (float)dim;
+// 2^-l, exact (0 <= l <= 126).
+__device__ __forceinline__ float pow2_neg(uint32_t l) { return __int_as_float((int)(127u - l) << 23); }
+
+// cell_center (wgsl:136-142) for one axis at level l: 2.0 / f32(2^l) is
+// exactly 2^(1-l), so it is formed from its exponent instead of a division.
+__device__ __forceinline__ float cell_center_lv(uint32_t c, uint32_t l) {
+  const float w = __int_as_float((int)(128u - l) << 23);
   return (((float)c + 0.5f) * w - 1.0f) * kHalf;
+}
+
+// Linear index x + dim * (y + dim * z) for dim = 2^l (wgsl:120-122).
+__device__ __forceinline__ uint32_t lin3_lv(uint32_t x, uint32_t y, uint32_t z, uint32_t l) {
+  return x | (y << l) | (z << (2u * l));
 }
 
 __device__ __forceinline__ uint32_t lin3(uint32_t x, uint32_t y, uint32_t z, uint32_t dim) {
@@ -97,6 +106,15 @@ __device__ __forceinline__ void pair_field_d(float4 src, float tx, float ty, flo
   out[9] = diagonal + tidal * rz * rz;
 }
 
+// Per-cell terms of integrate's self-leaf and excitation update that depend
+// only on the cell's count: (G * f32(count - 1) / f32(N), clamp((f32(count) -
+// 16) / 72, 0, 1)) (wgsl:655-656, 703-707), evaluated once per cell.
+__device__ __forceinline__ float2 make_aux(uint32_t count, float gravity, float n_f) {
+  const float self_mass = count > 1u ? (float)(count - 1u) / n_f : 0.0f;
+  return make_float2(gravity * self_mass,
+                     clampf_d(((float)count - (float)kAdaptive) / 72.0f, 0.0f, 1.0f));
+}
+
 // Source record of a cell: centre of mass and G * mass (0 for empty cells).
 // com = f32(sum) * (1 / (scale * f32(count))), mass = f32(count) / f32(N)
 // (wgsl:163-168, 182-183).
@@ -108,44 +126,89 @@ __device__ __forceinline__ float4 make_source(uint4 m, float scale, float gravit
                      (float)(int32_t)m.w * inv, gravity * mass);
 }
 
-// Warp-level segmented reduction of (count, qx, qy, qz) over runs of equal
-// key, followed by one set of 32-bit reductions into `moments` per run.  The
-// sums are exact modulo 2^32, so the result equals the reference's per-body
-// atomics (wgsl:418-421) bit for bit, whatever the body order.
-__device__ __forceinline__ void deposit_segmented(uint32_t key, bool active, int32_t qx, int32_t qy,
-                                                  int32_t qz, uint4 *moments) {
-  const unsigned lane = threadIdx.x & 31u;
-  if (!active) key = 0xFFFFFFFFu;
-  uint32_t c = active ? 1u : 0u;
-  uint32_t sx = active ? (uint32_t)qx : 0u, sy = active ? (uint32_t)qy : 0u,
-           sz = active ? (uint32_t)qz : 0u;
-  const uint32_t prev_key = __shfl_up_sync(0xFFFFFFFFu, key, 1);
-  const uint32_t next_key = __shfl_down_sync(0xFFFFFFFFu, key, 1);
-  const bool head = lane == 0u || prev_key != key;
-  const bool tail = lane == 31u || next_key != key;
-  const uint32_t heads = __ballot_sync(0xFFFFFFFFu, head);
-  const uint32_t le_mask = 0xFFFFFFFFu >> (31u - lane);
-  const uint32_t seg_start = 31u - __clz(heads & le_mask);
-#pragma unroll
-  for (uint32_t off = 1u; off < 32u; off <<= 1) {
-    const uint32_t uc = __shfl_up_sync(0xFFFFFFFFu, c, off);
-    const uint32_t ux = __shfl_up_sync(0xFFFFFFFFu, sx, off);
-    const uint32_t uy = __shfl_up_sync(0xFFFFFFFFu, sy, off);
-    const uint32_t uz = __shfl_up_sync(0xFFFFFFFFu, sz, off);
-    if (lane >= seg_start + off) {
-      c += uc;
-      sx += ux;
-      sy += uy;
-      sz += uz;
+// Per-CTA deposit accumulator: an open-addressing hash table in shared
+// memory keyed by global leaf cell.  A CTA reduces a contiguous slice of the
+// leaf-sorted bodies into it and flushes each touched leaf with one set of
+// 32-bit reductions, so a leaf holding tens of thousands of bodies receives a
+// few global reductions instead of one per warp.  All sums are integers
+// modulo 2^32, so the result is independent of order and equals the
+// reference's per-body atomics (wgsl:418-421) bit for bit.
+struct DepositTable {
+  static constexpr uint32_t kSlots = 1024u;
+  static constexpr uint32_t kEmpty = 0xFFFFFFFFu;
+  static constexpr uint32_t kProbes = 32u;
+  uint32_t key[kSlots];
+  uint32_t val[4][kSlots];
+
+  __device__ __forceinline__ void clear() {
+    for (uint32_t i = threadIdx.x; i < kSlots; i += blockDim.x) {
+      key[i] = kEmpty;
+      val[0][i] = val[1][i] = val[2][i] = val[3][i] = 0u;
     }
   }
-  if (tail && key != 0xFFFFFFFFu) {
-    uint32_t *m = reinterpret_cast<uint32_t *>(moments + key);
+
+  __device__ __forceinline__ void insert(uint32_t k, uint32_t c, uint32_t sx, uint32_t sy,
+                                         uint32_t sz, uint4 *moments) {
+    uint32_t h = (k * 2654435761u) >> 22;  // 10-bit multiplicative hash
+    for (uint32_t probe = 0; probe < kProbes; probe++) {
+      const uint32_t prev = atomicCAS(&key[h], kEmpty, k);
+      if (prev == kEmpty || prev == k) {
+        atomicAdd(&val[0][h], c);
+        atomicAdd(&val[1][h], sx);
+        atomicAdd(&val[2][h], sy);
+        atomicAdd(&val[3][h], sz);
+        return;
+      }
+      h = (h + 1u) & (kSlots - 1u);
+    }
+    uint32_t *m = reinterpret_cast<uint32_t *>(moments + k);  // table crowded: go direct
     atomicAdd(m + 0, c);
     atomicAdd(m + 1, sx);
     atomicAdd(m + 2, sy);
     atomicAdd(m + 3, sz);
   }
+
+  __device__ __forceinline__ void flush(uint4 *moments) {
+    for (uint32_t i = threadIdx.x; i < kSlots; i += blockDim.x) {
+      const uint32_t k = key[i];
+      if (k == kEmpty) continue;
+      uint32_t *m = reinterpret_cast<uint32_t *>(moments + k);
+      atomicAdd(m + 0, val[0][i]);
+      atomicAdd(m + 1, val[1][i]);
+      atomicAdd(m + 2, val[2][i]);
+      atomicAdd(m + 3, val[3][i]);
+    }
+  }
+};
+
+// One body's deposit into the CTA table: lanes with the same leaf are
+// grouped (__match_any_sync), their values summed with __reduce_add_sync, and
+// the group's lowest lane inserts the totals.
+__device__ __forceinline__ void deposit_body(DepositTable &T, uint32_t key, bool active, int32_t qx,
+                                             int32_t qy, int32_t qz, uint4 *moments) {
+  if (!active) key = DepositTable::kEmpty;
+  const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
+  const uint32_t c = __reduce_add_sync(peers, active ? 1u : 0u);
+  const uint32_t sx = __reduce_add_sync(peers, active ? (uint32_t)qx : 0u);
+  const uint32_t sy = __reduce_add_sync(peers, active ? (uint32_t)qy : 0u);
+  const uint32_t sz = __reduce_add_sync(peers, active ? (uint32_t)qz : 0u);
+  if (active && (threadIdx.x & 31u) == (uint32_t)(__ffs(peers) - 1)) T.insert(key, c, sx, sy, sz, moments);
+}
+
+// Contiguous range of body tiles handled by this CTA of a persistent grid.
+__device__ __forceinline__ void cta_tile_range(uint32_t tiles, uint32_t &t0, uint32_t &t1) {
+  const uint32_t per = (tiles + gridDim.x - 1u) / gridDim.x;
+  t0 = min(blockIdx.x * per, tiles);
+  t1 = min(t0 + per, tiles);
+}
+
+// Stage a scene descriptor in shared memory (all threads of the CTA call it).
+__device__ __forceinline__ void load_scene(SceneDesc &dst, const SceneDesc *scenes, uint32_t s) {
+  __syncthreads();
+  if (threadIdx.x < sizeof(SceneDesc) / 4u)
+    reinterpret_cast<uint32_t *>(&dst)[threadIdx.x] =
+        reinterpret_cast<const uint32_t *>(scenes + s)[threadIdx.x];
+  __syncthreads();
 }
 
 }  // namespace rfmm

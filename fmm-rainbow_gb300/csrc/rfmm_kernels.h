@@ -21,6 +21,7 @@ struct LaunchCtx {
   uint4 *mom;                  // moments of the current positions (leaf level valid)
   uint4 *mom_next;             // leaf level receives the integrate deposit
   float4 *src;                 // per-cell (com, G*m)
+  float2 *aux;                 // per-cell (G*(count-1)/N, density pulse) for integrate
   float *lfield;               // per-cell M2L result (12 floats)
   float *fields;               // per-cell final field (12 floats, reference layout)
   WorkItem *plist;             // parent list written this step
@@ -29,6 +30,7 @@ struct LaunchCtx {
   Counters *ctr;
   uint32_t *tickets;
   const CUtensorMap *tmaps;    // 8 per scene (levels 0..7; 3..6 used)
+  uint32_t body_ctas;          // persistent grid of the body passes (resident CTAs)
 };
 
 // Tree passes (kernels_tree.cu).
@@ -49,6 +51,7 @@ void launch_unpermute(const LaunchCtx &L, const uint32_t *ids, float4 *out, uint
                       uint32_t tiles);
 void launch_initialize(const LaunchCtx &L, float4 *part_out, uint32_t tile_base, uint32_t tiles);
 void launch_iota(cudaStream_t stream, uint32_t *ids, uint32_t count);
+uint32_t body_ctas_per_sm();  // resident 256-thread CTAs per SM of the persistent body passes
 
 // LSD radix sort of (key, value) pairs, 8-bit digits (kernels_sort.cu).
 struct SortScratch {

@@ -26,11 +26,13 @@ struct alignas(16) SceneDesc {
   float n_f;           // f32(particle_count)
   float control_strength;  // control_settings.x
   float control_radius;    // control_settings.y
-  uint32_t key_base;   // scene rank shifted above the Morton bits (sort key)
+  uint32_t key_base;   // scene rank shifted above the 3*key_level Morton bits (sort key)
   float control_point[4];      // wgsl:45
   float control_axis_mode[4];  // wgsl:47
+  uint32_t key_level;  // level of the fine Morton cells the resident order sorts by (>= depth)
+  uint32_t pad_[3];
 };
-static_assert(sizeof(SceneDesc) == 96, "SceneDesc layout");
+static_assert(sizeof(SceneDesc) == 112, "SceneDesc layout");
 
 // Device-side counters and status words of one engine.
 struct Counters {

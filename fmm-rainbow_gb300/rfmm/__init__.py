@@ -17,7 +17,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.dirname(HERE)
-LIB_PATH = os.path.join(PKG, "lib", "librfmm.so")
+LIB_PATH = os.environ.get("RFMM_LIB") or os.path.join(PKG, "lib", "librfmm.so")
 
 PARTICLE_DTYPE = np.dtype([("pos", "<f4", 3), ("hue", "<f4"), ("vel", "<f4", 3), ("exc", "<f4")])
 MOMENT_DTYPE = np.dtype([("count", "<u4"), ("sum", "<i4", 3)])
@@ -97,7 +97,10 @@ SIGNATURES = {
     "rfmm_check_finite": (_i, [_vp, _u32, C.POINTER(_u32), C.POINTER(_f32)]),
     "rfmm_set_resort_interval": (_i, [_vp, _u32]),
     "rfmm_device_error": (_i, [_vp, C.POINTER(_u32), C.POINTER(_u32)]),
+    "rfmm_profile_steps": (_i, [_vp, _u32, C.POINTER(_f32), C.POINTER(_u32)]),
+    "rfmm_launch_count": (_i, [_vp, C.POINTER(C.c_uint64)]),
 }
+KERNEL_KINDS = ("upward", "m2l", "l2l_near", "integrate", "resort")
 
 _lib = None
 
@@ -266,6 +269,18 @@ class Solver:
         bad, mx = C.c_uint32(), C.c_float()
         _check(lib().rfmm_check_finite(self._h, probe, C.byref(bad), C.byref(mx)), "rfmm_check_finite")
         return bad.value, mx.value
+
+    def profile_steps(self, steps: int):
+        """Per-kernel-kind device ms and launch counts over `steps` frames."""
+        ms = (C.c_float * len(KERNEL_KINDS))()
+        cnt = (C.c_uint32 * len(KERNEL_KINDS))()
+        _check(lib().rfmm_profile_steps(self._h, steps, ms, cnt), "rfmm_profile_steps")
+        return {k: (ms[i], cnt[i]) for i, k in enumerate(KERNEL_KINDS)}
+
+    def launch_count(self) -> int:
+        out = C.c_uint64()
+        _check(lib().rfmm_launch_count(self._h, C.byref(out)), "rfmm_launch_count")
+        return out.value
 
     def device_error(self):
         code, info = C.c_uint32(), C.c_uint32()

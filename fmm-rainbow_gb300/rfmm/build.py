@@ -68,8 +68,8 @@ def _gen_source_text() -> str:
     return out
 
 
-def _compile(src: str, obj: str) -> None:
-    flags = list(COMMON) + list(ARCH)
+def _compile(src: str, obj: str, extra=()) -> None:
+    flags = list(COMMON) + list(ARCH) + list(extra)
     if src.endswith(".cu"):
         flags += KERNEL_FLAGS
     cmd = [nvcc(), *flags, "-c", src, "-o", obj]
@@ -91,23 +91,36 @@ def up_to_date() -> bool:
     return all(os.path.getmtime(f) <= t for f in _deps())
 
 
-def build(force: bool = False) -> str:
-    """Compile and link ``lib/librfmm.so`` if any input changed."""
-    if not force and up_to_date():
-        return LIB
-    os.makedirs(BUILD, exist_ok=True)
-    os.makedirs(LIB_DIR, exist_ok=True)
-    srcs = [os.path.join(CSRC, s) for s in SOURCES] + [_gen_source_text()]
-    objs = [os.path.join(BUILD, os.path.basename(s) + ".o") for s in srcs]
+def build(force: bool = False, csrc: str | None = None, lib: str | None = None,
+          extra_flags=()) -> str:
+    """Compile and link ``lib/librfmm.so`` if any input changed.
+
+    ``csrc``/``lib``/``extra_flags`` build an alternative source tree into an
+    alternative library path (used to compare kernel variants side by side).
+    """
+    if csrc is None and lib is None and not extra_flags:
+        if not force and up_to_date():
+            return LIB
+        csrc_dir, out_lib, build_dir = CSRC, LIB, BUILD
+    else:
+        csrc_dir = csrc or CSRC
+        out_lib = lib or LIB
+        build_dir = os.path.join(os.path.dirname(os.path.abspath(out_lib)), "_build")
+    os.makedirs(build_dir, exist_ok=True)
+    os.makedirs(os.path.dirname(os.path.abspath(out_lib)), exist_ok=True)
+    srcs = [os.path.join(csrc_dir, s) for s in SOURCES] + [_gen_source_text()]
+    objs = [os.path.join(build_dir, os.path.basename(s) + ".o") for s in srcs]
+    extra = list(extra_flags) + ["-I", csrc_dir]
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
-        list(ex.map(_compile, srcs, objs))
-    tmp = LIB + ".tmp%d" % os.getpid()
+        list(ex.map(lambda a: _compile(a[0], a[1], extra), zip(srcs, objs)))
+    LIB_OUT = out_lib
+    tmp = LIB_OUT + ".tmp%d" % os.getpid()
     cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-Xcompiler", "-fPIC"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), res.stderr))
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, LIB_OUT)
+    return LIB_OUT
 
 
 if __name__ == "__main__":

@@ -133,9 +133,11 @@ int rfmm_digest(rfmm_handle *h, int which, uint32_t *out);
 /* Per-phase device time in ms of one instrumented frame, in the reference
  * harness's phase order (native/main.rs:468): clear, deposit, upward, m2l,
  * downward, near, integrate.  Fused phases report their time in the first
- * phase of the fusion and 0 in the others: deposit carries the sort+gather
- * refresh of the resident body order, downward carries L2L+near, clear is
- * folded into upward.  The frame advances the simulation by one step. */
+ * phase of the fusion and 0 in the others: clear is folded into upward,
+ * downward carries L2L+near, integrate carries the next step's deposit.
+ * deposit is a standalone P2M of the current positions into a scratch tree
+ * (in a step the deposit rides on integrate).  The frame advances the
+ * simulation by one step. */
 int rfmm_phase_times(rfmm_handle *h, float ms[7]);
 
 /* Non-finite count and max |value| over the first min(N, probe) bodies'
@@ -148,6 +150,27 @@ int rfmm_set_resort_interval(rfmm_handle *h, uint32_t steps);
 
 /* Last kernel error word (0 = none) and its detail. */
 int rfmm_device_error(rfmm_handle *h, uint32_t *code, uint32_t *info);
+
+/* Kernel kinds of rfmm_profile_steps. */
+enum rfmm_kernel_kind {
+  RFMM_KERNEL_UPWARD = 0,    /* M2M + source records + work list */
+  RFMM_KERNEL_M2L = 1,       /* 189-cell M2L */
+  RFMM_KERNEL_L2L_NEAR = 2,  /* L2L chain + adaptive-leaf near field */
+  RFMM_KERNEL_INTEGRATE = 3, /* L2P + self leaf + kick/drift + next deposit */
+  RFMM_KERNEL_RESORT = 4,    /* refresh of the resident leaf order */
+  RFMM_KERNEL_KINDS = 5
+};
+
+/* Profiling counterpart of rfmm_step: runs `steps` frames with direct
+ * launches and a CUDA event pair around every kernel on the handle's
+ * stream, and ADDS each kind's device time (ms) and launch count into the
+ * caller's arrays (RFMM_KERNEL_KINDS entries each). Same results as
+ * rfmm_step; only the launch mechanism differs (no graph). */
+int rfmm_profile_steps(rfmm_handle *h, uint32_t steps, float *kernel_ms, uint32_t *launches);
+
+/* Number of solver kernels this handle has launched so far (kernels inside
+ * CUDA graphs included). */
+int rfmm_launch_count(rfmm_handle *h, uint64_t *out);
 
 #ifdef __cplusplus
 }
