@@ -99,6 +99,7 @@ SIGNATURES = {
     "rfmm_device_error": (_i, [_vp, C.POINTER(_u32), C.POINTER(_u32)]),
     "rfmm_profile_steps": (_i, [_vp, _u32, C.POINTER(_f32), C.POINTER(_u32)]),
     "rfmm_launch_count": (_i, [_vp, C.POINTER(C.c_uint64)]),
+    "rfmm_solve_fields_noalloc": (_i, [_vp, _u32, _P, _vp, _vp, _vp]),
 }
 KERNEL_KINDS = ("upward", "m2l", "l2l_near", "integrate", "resort")
 
@@ -166,6 +167,14 @@ def plan_unclamped(n: int):
 
 
 # ------------------------------------------------------------------- solver
+
+def solve_fields_noalloc(particles_ptr: int, n: int, params: Params | None, moments_ptr: int,
+                         fields_ptr: int, stream_ptr: int | None = None) -> None:
+    """Allocation-free field solve on caller-owned device buffers (n <= 131072)."""
+    _check(lib().rfmm_solve_fields_noalloc(particles_ptr, n, C.byref(params) if params else None,
+                                           moments_ptr, fields_ptr, stream_ptr or None),
+           "rfmm_solve_fields_noalloc")
+
 
 class Solver:
     """One scene of N bodies resident on the GPU (the `rfmm_*` handle)."""

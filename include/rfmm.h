@@ -172,6 +172,28 @@ int rfmm_profile_steps(rfmm_handle *h, uint32_t steps, float *kernel_ms, uint32_
  * CUDA graphs included). */
 int rfmm_launch_count(rfmm_handle *h, uint64_t *out);
 
+/* Allocation-free field solve (this entry point has no counterpart in the
+ * reference).  For callers that cannot allocate device memory -- a plugin
+ * whose device memory is owned by the host framework, or code running where
+ * a cudaMalloc would synchronise the device -- it computes exactly what
+ * rfmm_solve_fields followed by rfmm_download_device(MOMENTS / FIELDS)
+ * computes, on caller-owned device buffers: `device_particles` (n x 32 B,
+ * reference Particle layout), `device_moments` (C x 16 B) and
+ * `device_fields` (C x 48 B), C = total_cells(depth) of the unclamped plan
+ * (rainbow_plan_depth_unclamped).  All pointers 16-byte aligned; `params`
+ * may be NULL for the harness defaults; `stream` is a cudaStream_t (NULL =
+ * default stream).  Work is enqueued asynchronously on `stream`.
+ *
+ * It calls no cudaMalloc/cudaFree: its intermediate data lives in one fixed
+ * __device__ array of about 7.4 MB that every GPU loading this library holds
+ * until exit, so n is limited to 1..131072 (tree depth 4 or 5); larger n
+ * returns RFMM_ERR_INVALID.  Every call reuses that one array: calls that
+ * overlap on the GPU race on it.  The first call on a device does a one-time
+ * set-up (resolving the array's device address, encoding TMA descriptors);
+ * make that first call before any stream capture. */
+int rfmm_solve_fields_noalloc(const void *device_particles, uint32_t n, const rfmm_params *params,
+                              void *device_moments, void *device_fields, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
