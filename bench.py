@@ -262,12 +262,10 @@ def run_gpu(args, w):
     barrier()
     launches = solver.launch_count() - l0
     clocks = clocks_summary(clk)
-    total_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * n * fmm_steps * args.steps / (total_ms * 1e-3)
+    local_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    from rfmm import replicas
+    value, _, slowest_s = replicas.reduce_throughput(n * fmm_steps * args.steps, local_ms * 1e-3)
+    total_ms = slowest_s * 1e3
     solver.sync()
 
     # Per-kernel device times over the same workload (event pair around every launch).

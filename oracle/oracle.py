@@ -75,6 +75,7 @@ def lib():
             "oracle_sample_cells": (None, [vp, vp, P, vp]),
             "oracle_leaf_of": (u32, [vp, u32]),
             "oracle_direct_sum_f64": (None, [vp, u32, vp, u32, C.c_double, C.c_double, vp]),
+            "oracle_accelerations": (None, [vp, vp, vp, P, vp]),
             "oracle_set_threads": (C.c_int, [C.c_int]),
         }
         for name, (res, args) in sig.items():
@@ -135,6 +136,13 @@ class OracleState:
     def integrate(self):
         lib().oracle_integrate(_ptr(self.particles), _ptr(self.moments), _ptr(self.fields),
                                C.byref(self.params))
+
+    def accelerations(self) -> np.ndarray:
+        """FMM acceleration of every body from the current moments/fields."""
+        out = np.zeros((self.params.n, 3), np.float32)
+        lib().oracle_accelerations(_ptr(self.particles), _ptr(self.moments), _ptr(self.fields),
+                                   C.byref(self.params), _ptr(out))
+        return out
 
     def m2l_targets(self) -> np.ndarray:
         cap = len(self.moments)

@@ -460,51 +460,70 @@ static float fractf(float x) { return x - floorf(x); }
 
 static float length3(const float v[3]) { return sqrtf((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]); }
 
+/* The FMM acceleration integrate applies before the control field
+ * (wgsl:619-657): adaptive descent, local expansion, self-leaf monopole.
+ * Returns the chosen cell's count. */
+static uint32_t fmm_acceleration(const OParticle *particle, const OMoment *moments,
+                                 const OField *fields, const OParams *P, float acc[3]) {
+  const uint32_t depth = P->depth;
+  float pos[3] = {particle->px, particle->py, particle->pz};
+  uint32_t chosen_dim = 1u << depth, chosen_cell[3], cell_index;
+  position_cell(pos, chosen_dim, chosen_cell);
+  cell_index = o_level_offset(depth) + linear_index(chosen_cell, chosen_dim);
+  for (uint32_t level = 1u; level <= depth; level++) {
+    uint32_t dim = 1u << level, c[3];
+    position_cell(pos, dim, c);
+    uint32_t index = o_level_offset(level) + linear_index(c, dim);
+    int32_t count_at_level = (int32_t)moments[index].count;
+    if (count_at_level <= (int32_t)O_ADAPTIVE || level == depth) {
+      chosen_dim = dim;
+      chosen_cell[0] = c[0];
+      chosen_cell[1] = c[1];
+      chosen_cell[2] = c[2];
+      cell_index = index;
+      break;
+    }
+  }
+  float center[3], rel[3], jm[3];
+  cell_center(chosen_cell, chosen_dim, center);
+  const OField *field = &fields[cell_index];
+  for (int k = 0; k < 3; k++) rel[k] = pos[k] - center[k];
+  field_j_mul(field, rel, jm);
+  for (int k = 0; k < 3; k++) acc[k] = field->a[k] + jm[k];
+
+  const uint32_t count = moments[cell_index].count;
+  if (count > 1u) {
+    float com[3], delta[3];
+    moment_com(&moments[cell_index], count, P->scale, com);
+    for (int k = 0; k < 3; k++) delta[k] = com[k] - pos[k];
+    const float ce = 0.62f * O_HALF / (float)chosen_dim;
+    const float eps = fmaxf(P->softening, ce);
+    const float inv_r =
+        1.0f / sqrtf((delta[0] * delta[0] + delta[1] * delta[1]) + delta[2] * delta[2] + eps * eps);
+    const float self_mass = (float)(count - 1u) / (float)P->n;
+    for (int k = 0; k < 3; k++)
+      acc[k] = acc[k] + P->gravity * self_mass * delta[k] * inv_r * inv_r * inv_r;
+  }
+  return count;
+}
+
+/* FMM accelerations of every body (no update). */
+void oracle_accelerations(const OParticle *particles, const OMoment *moments, const OField *fields,
+                          const OParams *P, float *acc_out) {
+#pragma omp parallel for schedule(static) if (P->n >= 8192u)
+  for (int64_t i = 0; i < (int64_t)P->n; i++) fmm_acceleration(&particles[i], moments, fields, P, &acc_out[3 * i]);
+}
+
 void oracle_integrate(OParticle *particles, const OMoment *moments, const OField *fields,
                       const OParams *P) { /* wgsl:613-771 */
-  const uint32_t n = P->n, depth = P->depth;
+  const uint32_t n = P->n;
 #pragma omp parallel for schedule(static) if (n >= 8192u)
   for (int64_t ii = 0; ii < (int64_t)n; ii++) {
     OParticle particle = particles[ii];
     float pos[3] = {particle.px, particle.py, particle.pz};
     float velocity[3] = {particle.vx, particle.vy, particle.vz};
-    uint32_t chosen_dim = 1u << depth, chosen_cell[3], cell_index;
-    position_cell(pos, chosen_dim, chosen_cell);
-    cell_index = o_level_offset(depth) + linear_index(chosen_cell, chosen_dim);
-    for (uint32_t level = 1u; level <= depth; level++) {
-      uint32_t dim = 1u << level, c[3];
-      position_cell(pos, dim, c);
-      uint32_t index = o_level_offset(level) + linear_index(c, dim);
-      int32_t count_at_level = (int32_t)moments[index].count;
-      if (count_at_level <= (int32_t)O_ADAPTIVE || level == depth) {
-        chosen_dim = dim;
-        chosen_cell[0] = c[0];
-        chosen_cell[1] = c[1];
-        chosen_cell[2] = c[2];
-        cell_index = index;
-        break;
-      }
-    }
-    float center[3], rel[3], jm[3], acc[3];
-    cell_center(chosen_cell, chosen_dim, center);
-    const OField *field = &fields[cell_index];
-    for (int k = 0; k < 3; k++) rel[k] = pos[k] - center[k];
-    field_j_mul(field, rel, jm);
-    for (int k = 0; k < 3; k++) acc[k] = field->a[k] + jm[k];
-
-    const uint32_t count = moments[cell_index].count;
-    if (count > 1u) {
-      float com[3], delta[3];
-      moment_com(&moments[cell_index], count, P->scale, com);
-      for (int k = 0; k < 3; k++) delta[k] = com[k] - pos[k];
-      const float ce = 0.62f * O_HALF / (float)chosen_dim;
-      const float eps = fmaxf(P->softening, ce);
-      const float inv_r =
-          1.0f / sqrtf((delta[0] * delta[0] + delta[1] * delta[1]) + delta[2] * delta[2] + eps * eps);
-      const float self_mass = (float)(count - 1u) / (float)n;
-      for (int k = 0; k < 3; k++)
-        acc[k] = acc[k] + P->gravity * self_mass * delta[k] * inv_r * inv_r * inv_r;
-    }
+    float acc[3];
+    const uint32_t count = fmm_acceleration(&particle, moments, fields, P, acc);
 
     float control_influence = 0.0f;
     if (P->control_point[3] > 0.5f) { /* wgsl:659-689 */
