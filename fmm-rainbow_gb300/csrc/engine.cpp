@@ -170,7 +170,8 @@ int Engine::create(const std::vector<SceneSpec> &specs, Engine **out) {
     A((void **)&E->sort_.vals[b], 4 * S);
   }
   A((void **)&E->d_src_, 16 * C);
-  A((void **)&E->d_aux_, 8 * C);
+  A((void **)&E->d_aux_, 16 * C);
+  A((void **)&E->d_choice_, 4 * C);
   A((void **)&E->d_lfield_, 48 * C);
   A((void **)&E->d_fields_, 48 * C);
   A((void **)&E->d_ctr_, sizeof(Counters));
@@ -206,7 +207,8 @@ int Engine::create(const std::vector<SceneSpec> &specs, Engine **out) {
     if (e == cudaSuccess) e = cudaMemsetAsync(E->d_ids_[b], 0, 4 * S, E->stream_);
   }
   if (e == cudaSuccess) e = cudaMemsetAsync(E->d_src_, 0, 16 * C, E->stream_);
-  if (e == cudaSuccess) e = cudaMemsetAsync(E->d_aux_, 0, 8 * C, E->stream_);
+  if (e == cudaSuccess) e = cudaMemsetAsync(E->d_aux_, 0, 16 * C, E->stream_);
+  if (e == cudaSuccess) e = cudaMemsetAsync(E->d_choice_, 0xFF, 4 * C, E->stream_);
   if (e == cudaSuccess) e = cudaMemsetAsync(E->d_lfield_, 0, 48 * C, E->stream_);
   if (e == cudaSuccess) e = cudaMemsetAsync(E->d_fields_, 0, 48 * C, E->stream_);
   if (e == cudaSuccess) e = cudaMemsetAsync(E->d_ctr_, 0, sizeof(Counters), E->stream_);
@@ -301,6 +303,7 @@ LaunchCtx Engine::ctx(uint32_t mpar, uint32_t lpar, uint32_t ppar) const {
   L.mom_next = d_mom_[mpar ^ 1u];
   L.src = d_src_;
   L.aux = d_aux_;
+  L.choice = d_choice_;
   L.lfield = d_lfield_;
   L.fields = d_fields_;
   L.plist = d_plist_[lpar];
@@ -310,6 +313,7 @@ LaunchCtx Engine::ctx(uint32_t mpar, uint32_t lpar, uint32_t ppar) const {
   L.tickets = d_tickets_;
   L.tmaps = d_tmaps_;
   L.body_ctas = body_ctas_;
+  L.pdl = pdl_;
   return L;
 }
 

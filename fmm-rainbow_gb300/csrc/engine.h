@@ -95,7 +95,8 @@ class Engine {
   uint4 *d_mom_[2] = {nullptr, nullptr};
   uint4 *d_mom_scratch_ = nullptr;
   float4 *d_src_ = nullptr;
-  float2 *d_aux_ = nullptr;
+  float4 *d_aux_ = nullptr;
+  uint32_t *d_choice_ = nullptr;
   float *d_lfield_ = nullptr, *d_fields_ = nullptr;
   WorkItem *d_plist_[2] = {nullptr, nullptr};
   Counters *d_ctr_ = nullptr;
@@ -112,7 +113,8 @@ class Engine {
   int tree_buf_ = -1;    // moment buffer holding the last complete tree
   bool committed_ = false;
   bool solved_ = false;  // fields hold a solution
-  uint32_t resort_interval_ = 16, since_sort_ = 0;
+  uint32_t resort_interval_ = 64, since_sort_ = 0;
+  bool pdl_ = true;  // programmatic dependent launch between step kernels
   std::vector<bool> uploaded_;
 
   struct Graph {

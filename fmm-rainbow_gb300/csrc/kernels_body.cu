@@ -50,7 +50,8 @@ __device__ __forceinline__ void soft_wall(float &p, float &v, float world_edge, 
 __device__ __forceinline__ void integrate_body(const SceneDesc &S, float4 &p0, float4 &p1,
                                                const uint4 *__restrict__ mom,
                                                const float4 *__restrict__ src,
-                                               const float2 *__restrict__ aux,
+                                               const float4 *__restrict__ aux,
+                                               const uint32_t *__restrict__ choice,
                                                const float *__restrict__ fields, uint32_t &key,
                                                int32_t &qx, int32_t &qy, int32_t &qz) {
     float px = p0.x, py = p0.y, pz = p0.z;
@@ -62,21 +63,29 @@ __device__ __forceinline__ void integrate_body(const SceneDesc &S, float4 &p0, f
                    lz = cell_of_unit(unit_coord(pz), dimD);
 
     // Adaptive descent (wgsl:625-639): first level whose cell holds at most
-    // 16 bodies, else the leaf level.  The level loads are independent.
-    uint32_t chosen = D, cell_index = 0u, count = 0u;
+    // 16 bodies, else the leaf level.  Resolved once per leaf by the upward
+    // pass; bodies of unresolved leaves (sparse subtrees) descend here.
+    uint32_t chosen = D, cell_index = 0u;
+    const uint32_t pick = __ldg(&choice[S.cell_off + level_offset_d(D) + lin3_lv(lx, ly, lz, D)]);
+    if (pick != kChoiceUnresolved) {
+      chosen = pick >> 28;
+      cell_index = S.cell_off + (pick & 0x0FFFFFFFu);
+    } else {
 #pragma unroll
-    for (uint32_t l = 6u; l >= 1u; l--) {
-      if (l <= D) {
-        const uint32_t sh = D - l;
-        const uint32_t idx = S.cell_off + level_offset_d(l) + lin3_lv(lx >> sh, ly >> sh, lz >> sh, l);
-        const uint32_t c = __ldg(&mom[idx].x);
-        if ((int32_t)c <= (int32_t)kAdaptive || l == D) {
-          chosen = l;
-          cell_index = idx;
-          count = c;
+      for (uint32_t l = 6u; l >= 1u; l--) {
+        if (l <= D) {
+          const uint32_t sh = D - l;
+          const uint32_t idx = S.cell_off + level_offset_d(l) + lin3_lv(lx >> sh, ly >> sh, lz >> sh, l);
+          const uint32_t c = __ldg(&mom[idx].x);
+          if ((int32_t)c <= (int32_t)kAdaptive || l == D) {
+            chosen = l;
+            cell_index = idx;
+          }
         }
       }
     }
+    const float4 ax4 = __ldg(&aux[cell_index]);
+    const uint32_t count = __float_as_uint(ax4.z);
     const uint32_t csh = D - chosen;
     const float cx = cell_center_lv(lx >> csh, chosen);
     const float cy = cell_center_lv(ly >> csh, chosen);
@@ -91,13 +100,12 @@ __device__ __forceinline__ void integrate_body(const SceneDesc &S, float4 &p0, f
 
     // Self leaf: softened monopole of the other count-1 bodies (wgsl:646-657).
     // x / 2^l == x * 2^-l exactly, so the eps division is a scaling.
-    const float2 ax2 = __ldg(&aux[cell_index]);
     if (count > 1u) {
       const float4 s = __ldg(&src[cell_index]);
       const float dx = s.x - px, dy = s.y - py, dz = s.z - pz;
       const float eps = fmaxf(S.softening, (0.62f * kHalf) * pow2_neg(chosen));
       const float inv_r = 1.0f / sqrtf((dx * dx + dy * dy) + dz * dz + eps * eps);
-      const float gsm = ax2.x;  // G * f32(count - 1) / f32(N)
+      const float gsm = ax4.x;  // G * f32(count - 1) / f32(N)
       ax = ax + gsm * dx * inv_r * inv_r * inv_r;
       ay = ay + gsm * dy * inv_r * inv_r * inv_r;
       az = az + gsm * dz * inv_r * inv_r * inv_r;
@@ -145,7 +153,7 @@ __device__ __forceinline__ void integrate_body(const SceneDesc &S, float4 &p0, f
     const float signed_radial = clampf_d(pv / (radius * vlen), -1.0f, 1.0f);
     const float rf = fabsf(signed_radial);
     const float radial_shock = rf * rf * rf;
-    const float density_pulse = ax2.y;  // clamp((f32(count) - 16) / 72, 0, 1)
+    const float density_pulse = ax4.y;  // clamp((f32(count) - 16) / 72, 0, 1)
     const float field_strength = clampf_d(length3(ax, ay, az) * (radius + 0.12f) * 0.58f, 0.0f, 1.0f);
     const float target_exc = clampf_d(0.025f + radial_shock * 0.56f + density_pulse * 0.26f +
                                           field_strength * 0.13f + control_influence * 0.42f,
@@ -192,7 +200,8 @@ __global__ void __launch_bounds__(256) k_integrate(const SceneDesc *__restrict__
                                                    float4 *__restrict__ part,
                                                    const uint4 *__restrict__ mom,
                                                    const float4 *__restrict__ src,
-                                                   const float2 *__restrict__ aux,
+                                                   const float4 *__restrict__ aux,
+                                                   const uint32_t *__restrict__ choice,
                                                    const float *__restrict__ fields,
                                                    uint4 *__restrict__ mom_next, uint32_t tiles) {
   __shared__ DepositTable T;
@@ -200,6 +209,7 @@ __global__ void __launch_bounds__(256) k_integrate(const SceneDesc *__restrict__
   uint32_t t0, t1;
   cta_tile_range(tiles, t0, t1);
   T.clear();
+  grid_dependency_wait();  // fields of this step are complete
   uint32_t cur = 0xFFFFFFFFu;
   // The next tile's bodies are loaded one iteration ahead.
   float4 n0 = make_float4(0.f, 0.f, 0.f, 0.f), n1 = n0;
@@ -223,7 +233,7 @@ __global__ void __launch_bounds__(256) k_integrate(const SceneDesc *__restrict__
     uint32_t key = DepositTable::kEmpty;
     int32_t qx = 0, qy = 0, qz = 0;
     if (active) {
-      integrate_body(S, p0, p1, mom, src, aux, fields, key, qx, qy, qz);
+      integrate_body(S, p0, p1, mom, src, aux, choice, fields, key, qx, qy, qz);
       part[2u * slot] = p0;
       part[2u * slot + 1u] = p1;
     }
@@ -231,6 +241,7 @@ __global__ void __launch_bounds__(256) k_integrate(const SceneDesc *__restrict__
   }
   __syncthreads();
   T.flush(mom_next);
+  grid_dependents_may_launch();
 }
 
 // Standalone P2M: deposit the current positions into `moments` (leaf level
@@ -499,8 +510,10 @@ static uint32_t body_grid(const LaunchCtx &L, uint32_t tiles) {
 }
 
 void launch_integrate(const LaunchCtx &L, uint32_t tiles) {
-  k_integrate<<<body_grid(L, tiles), kTile, 0, L.stream>>>(L.scenes, L.tile_scene, L.part, L.mom,
-                                                           L.src, L.aux, L.fields, L.mom_next, tiles);
+  launch_step_kernel(L, k_integrate, dim3(body_grid(L, tiles)), dim3(kTile), 0, L.scenes,
+                     L.tile_scene, L.part, (const uint4 *)L.mom, (const float4 *)L.src,
+                     (const float4 *)L.aux, (const uint32_t *)L.choice, (const float *)L.fields,
+                     L.mom_next, tiles);
 }
 
 void launch_deposit(const LaunchCtx &L, uint4 *moments, uint32_t tiles) {

@@ -40,17 +40,18 @@ __device__ __forceinline__ uint4 add_moment(uint4 a, uint4 b) {
 }
 
 __device__ __forceinline__ void store_cell(const SceneDesc &S, uint32_t local_cell, uint4 m,
-                                           uint4 *mom, float4 *src, float2 *aux) {
+                                           uint4 *mom, float4 *src, float4 *aux) {
   const uint32_t g = S.cell_off + local_cell;
   mom[g] = m;
   src[g] = make_source(m, S.scale, S.gravity, S.n_f);
   aux[g] = make_aux(m.x, S.gravity, S.n_f);
 }
 
-__global__ void __launch_bounds__(512) k_upward(const SceneDesc *__restrict__ scenes,
+__global__ void __launch_bounds__(256) k_upward(const SceneDesc *__restrict__ scenes,
                                                 const uint32_t *__restrict__ task_scene,
                                                 uint4 *__restrict__ mom, uint4 *__restrict__ mom_next,
-                                                float4 *__restrict__ src, float2 *__restrict__ aux,
+                                                float4 *__restrict__ src, float4 *__restrict__ aux,
+                                                uint32_t *__restrict__ choice,
                                                 float *__restrict__ fields,
                                                 WorkItem *__restrict__ plist, uint32_t plist_cap,
                                                 const WorkItem *__restrict__ plist_prev,
@@ -60,7 +61,7 @@ __global__ void __launch_bounds__(512) k_upward(const SceneDesc *__restrict__ sc
   __shared__ uint4 s1[64];
   __shared__ uint4 s2[8];
   __shared__ WorkItem s_items[80];
-  __shared__ uint32_t s_nitems, s_base, s_last;
+  __shared__ uint32_t s_nitems, s_base, s_last, s_root;
 
   const uint32_t tid = threadIdx.x;
   const uint32_t scene = task_scene[blockIdx.x];
@@ -69,12 +70,15 @@ __global__ void __launch_bounds__(512) k_upward(const SceneDesc *__restrict__ sc
   const uint32_t sub = blockIdx.x - S.task_off;
   const uint32_t rdim = 1u << r;
   const uint32_t sx = sub % rdim, sy = (sub / rdim) % rdim, sz = sub / (rdim * rdim);
+  if (tid == 0) s_nitems = 0;
+  grid_dependency_wait();  // the previous integrate deposited and read the fields
 
   // Clear the fields of the previous step's targets (children of listed parents).
   {
     const uint32_t prev_n = min(ctr->parents[list_par ^ 1u], plist_cap);
-    const uint32_t warp = blockIdx.x * 16u + (tid >> 5), lane = tid & 31u;
-    for (uint32_t i = warp; i < prev_n; i += gridDim.x * 16u) {
+    const uint32_t wpb = blockDim.x >> 5;
+    const uint32_t warp = blockIdx.x * wpb + (tid >> 5), lane = tid & 31u;
+    for (uint32_t i = warp; i < prev_n; i += gridDim.x * wpb) {
       const WorkItem w = plist_prev[i];
       const SceneDesc &P = scenes[w.scene];
       const uint32_t lp = w.cell == 0u ? 0u : level_of_d(w.cell);
@@ -91,14 +95,15 @@ __global__ void __launch_bounds__(512) k_upward(const SceneDesc *__restrict__ sc
     }
   }
 
-  if (tid == 0) s_nitems = 0;
-  // Leaves of this subtree: 8x8x8 block, x fastest (rows of 128 B).
-  {
-    const uint32_t lx = tid & 7u, ly = (tid >> 3) & 7u, lz = tid >> 6;
+  // Leaves of this subtree: 8x8x8 block, x fastest (rows of 128 B); two per thread.
+#pragma unroll
+  for (uint32_t h = 0; h < 2u; h++) {
+    const uint32_t t = tid + h * 256u;
+    const uint32_t lx = t & 7u, ly = (t >> 3) & 7u, lz = t >> 6;
     const uint32_t dim = 1u << D;
     const uint32_t leaf = level_offset_d(D) + lin3(sx * 8u + lx, sy * 8u + ly, sz * 8u + lz, dim);
     const uint4 m = mom[S.cell_off + leaf];
-    s0[tid] = m;
+    s0[t] = m;
     src[S.cell_off + leaf] = make_source(m, S.scale, S.gravity, S.n_f);
     aux[S.cell_off + leaf] = make_aux(m.x, S.gravity, S.n_f);
     mom_next[S.cell_off + leaf] = make_uint4(0u, 0u, 0u, 0u);
@@ -145,8 +150,33 @@ __global__ void __launch_bounds__(512) k_upward(const SceneDesc *__restrict__ sc
     const uint32_t cell = level_offset_d(r) + lin3(sx, sy, sz, rdim);
     store_cell(S, cell, acc, mom, src, aux);
     if ((int32_t)acc.x > (int32_t)kAdaptive) s_items[atomicAdd(&s_nitems, 1u)] = {scene, cell};
+    s_root = acc.x;
   }
   __syncthreads();
+  // Sample cell of each leaf.  Counts never shrink towards the root, so when
+  // this subtree's root holds more than 16 bodies every level <= r is skipped
+  // by the descent and the choice lies within the subtree: the first of
+  // levels D-2, D-1 with count <= 16, else the leaf.
+#pragma unroll
+  for (uint32_t h = 0; h < 2u; h++) {
+    const uint32_t t = tid + h * 256u;
+    const uint32_t lx = t & 7u, ly = (t >> 3) & 7u, lz = t >> 6;
+    uint32_t v = kChoiceUnresolved;
+    if ((int32_t)s_root > (int32_t)kAdaptive) {
+      const uint32_t c2 = s2[(lx >> 2) + 2u * ((ly >> 2) + 2u * (lz >> 2))].x;
+      const uint32_t c1 = s1[(lx >> 1) + 4u * ((ly >> 1) + 4u * (lz >> 1))].x;
+      if ((int32_t)c2 <= (int32_t)kAdaptive) {
+        v = ((D - 2u) << 28) | (level_offset_d(D - 2u) +
+                                lin3_lv(sx * 2u + (lx >> 2), sy * 2u + (ly >> 2), sz * 2u + (lz >> 2), D - 2u));
+      } else if ((int32_t)c1 <= (int32_t)kAdaptive) {
+        v = ((D - 1u) << 28) | (level_offset_d(D - 1u) +
+                                lin3_lv(sx * 4u + (lx >> 1), sy * 4u + (ly >> 1), sz * 4u + (lz >> 1), D - 1u));
+      } else {
+        v = (D << 28) | (level_offset_d(D) + lin3_lv(sx * 8u + lx, sy * 8u + ly, sz * 8u + lz, D));
+      }
+    }
+    choice[S.cell_off + level_offset_d(D) + lin3_lv(sx * 8u + lx, sy * 8u + ly, sz * 8u + lz, D)] = v;
+  }
   // Publish this subtree's parents.
   if (tid == 0) {
     uint32_t base = atomicAdd(&ctr->parents[list_par], s_nitems);
@@ -159,10 +189,11 @@ __global__ void __launch_bounds__(512) k_upward(const SceneDesc *__restrict__ sc
   __syncthreads();
   for (uint32_t i = tid; i < s_nitems; i += blockDim.x) plist[s_base + i] = s_items[i];
 
-  // The last subtree CTA of the scene reduces levels r-1 .. 0.
-  __threadfence();
+  // The last subtree CTA of the scene reduces levels r-1 .. 0.  Only thread 0
+  // wrote the level-r cell the last CTA reads, so only it fences.
   __syncthreads();
   if (tid == 0) {
+    __threadfence();
     const uint32_t ntasks = 1u << (3u * r);
     const uint32_t done = atomicAdd(&tickets[scene], 1u);
     s_last = (done == ntasks - 1u) ? 1u : 0u;
@@ -215,6 +246,7 @@ struct M2LShared {
   float4 tile[kTileCells];  // first member: 128-byte aligned by the launch
   unsigned long long mbar;
   uint32_t stop;
+  uint32_t live[8];         // target cell of each child, or ~0 if the child is empty
   float vals[8][10][kSlotStride];
 };
 
@@ -271,13 +303,14 @@ __global__ void __launch_bounds__(256) k_m2l(const SceneDesc *__restrict__ scene
   const uint32_t pad = (128u - (smem_u32(smem_raw) & 127u)) & 127u;
   M2LShared &sh = *reinterpret_cast<M2LShared *>(smem_raw + pad);
   const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
-  const uint32_t count = min(ctr->parents[list_par], plist_cap);
-  if (blockIdx.x == 0 && tid == 0) ctr->parents[list_par ^ 1u] = 0u;  // reset for the next step
   if (tid == 0) {
     mbar_init(&sh.mbar, 1u);
     sh.stop = 0u;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
+  grid_dependency_wait();  // the upward pass built the tree and the parent list
+  const uint32_t count = min(ctr->parents[list_par], plist_cap);
+  if (blockIdx.x == 0 && tid == 0) ctr->parents[list_par ^ 1u] = 0u;  // reset for the next step
   __syncthreads();
   uint32_t phase = 0u;
 
@@ -315,11 +348,12 @@ __global__ void __launch_bounds__(256) k_m2l(const SceneDesc *__restrict__ scene
     __syncthreads();
     if (sh.stop) return;
 
-    // Warp w handles child w of the parent.
+    // Warp w evaluates the stencil of child w of the parent.
     const int cx = (int)(warp & 1u), cy = (int)((warp >> 1) & 1u), cz = (int)(warp >> 2);
     const uint32_t tx = (uint32_t)(2 * pcx + cx), ty = (uint32_t)(2 * pcy + cy), tz = (uint32_t)(2 * pcz + cz);
     const uint32_t target = lvl_base + lin3(tx, ty, tz, dim);
     const bool live = mom[target].x != 0u;  // empty children are not targets
+    if (lane == 0) sh.live[warp] = live ? target : 0xFFFFFFFFu;
     if (live) {
       const float ctx = cell_center_lv(tx, l), cty = cell_center_lv(ty, l),
                   ctz = cell_center_lv(tz, l);
@@ -344,20 +378,29 @@ __global__ void __launch_bounds__(256) k_m2l(const SceneDesc *__restrict__ scene
 #pragma unroll
         for (int c = 0; c < 10; c++) sh.vals[warp][c][k] = out[c];
       }
-      __syncwarp();
-      if (lane < 12u) {
-        float acc = 0.0f;
-        if (lane < 10u) {
-          // Strictly sequential sum in slot order; loads run 8 ahead of the adds.
-          const float *row = sh.vals[warp][lane];
+    }
+    __syncthreads();
+    // 80 threads sum the 8 children x 10 components, each strictly in slot
+    // order (loads run ahead of the dependent adds); 16 more write the pads.
+    if (tid < 96u) {
+      const uint32_t t = tid < 80u ? tid / 10u : (tid - 80u) >> 1;
+      const uint32_t tgt = sh.live[t];
+      if (tgt != 0xFFFFFFFFu) {
+        if (tid < 80u) {
+          const uint32_t c = tid % 10u;
+          const float *row = sh.vals[t][c];
+          float acc = 0.0f;
 #pragma unroll 8
           for (uint32_t k = 0; k < kTileCells; k++) acc = acc + row[k];
+          lfield[(size_t)tgt * 12u + c] = acc;
+        } else {
+          lfield[(size_t)tgt * 12u + 10u + (tid & 1u)] = 0.0f;
         }
-        lfield[(size_t)target * 12u + lane] = acc;
       }
     }
     __syncthreads();
   }
+  grid_dependents_may_launch();
 }
 
 // ------------------------------------------------------------ L2L + near
@@ -376,7 +419,10 @@ __global__ void __launch_bounds__(256) k_l2l_near(const SceneDesc *__restrict__ 
                                                   float *__restrict__ fields) {
   __shared__ L2LShared sh;
   const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
+  grid_dependency_wait();  // M2L results of every target are complete
   const uint32_t count = min(ctr->parents[list_par], plist_cap);
+  // Lane c < 12 owns field component c (ax ay az phi Jxx Jxy Jxz Jyy Jyz Jzz 0 0).
+  const uint32_t c = lane < 12u ? lane : 11u;
   for (uint32_t item = blockIdx.x; item < count; item += gridDim.x) {
     const WorkItem w = plist[item];
     const SceneDesc &S = scenes[w.scene];
@@ -391,24 +437,20 @@ __global__ void __launch_bounds__(256) k_l2l_near(const SceneDesc *__restrict__ 
     const uint32_t tcount = mom[target].x;
     if (tcount == 0u) continue;  // warp-uniform
 
-    // Top-down chain: f_level = m2l(level) + translate(f_parent), root field 0
+    // Top-down chain f_a = m2l(a) + translate(f_{a-1}) from the root field 0
     // (the reference never writes cell 0's field, wgsl:459).  The ancestors'
-    // M2L results are loaded up front; the chain itself is sequential.
-    float4 g[6][3];
+    // M2L components are loaded up front (lane c reads component c).
+    float g[6];
 #pragma unroll
     for (uint32_t a = 1u; a <= 6u; a++) {
+      g[a - 1] = 0.0f;
       if (a <= l) {
         const uint32_t sh_ = l - a;
         const uint32_t anc = S.cell_off + level_offset_d(a) + lin3_lv(tx >> sh_, ty >> sh_, tz >> sh_, a);
-        const float4 *lf = reinterpret_cast<const float4 *>(lfield + (size_t)anc * 12u);
-        g[a - 1][0] = __ldg(lf);
-        g[a - 1][1] = __ldg(lf + 1);
-        g[a - 1][2] = __ldg(lf + 2);
+        g[a - 1] = __ldg(lfield + (size_t)anc * 12u + c);
       }
     }
-    float f[12];
-#pragma unroll
-    for (int c = 0; c < 12; c++) f[c] = 0.0f;
+    float f = 0.0f;
 #pragma unroll
     for (uint32_t a = 1u; a <= 6u; a++) {
       if (a <= l) {
@@ -417,27 +459,16 @@ __global__ void __launch_bounds__(256) k_l2l_near(const SceneDesc *__restrict__ 
         const float dx = cell_center_lv(ax, a) - cell_center_lv(ax >> 1, a - 1u);
         const float dy = cell_center_lv(ay, a) - cell_center_lv(ay >> 1, a - 1u);
         const float dz = cell_center_lv(az, a) - cell_center_lv(az >> 1, a - 1u);
-        // inherited (wgsl:603-609): a += J . delta, phi -= a . delta, J unchanged.
-        float inh[12];
-        inh[0] = f[0] + (f[4] * dx + f[5] * dy + f[6] * dz);
-        inh[1] = f[1] + (f[5] * dx + f[7] * dy + f[8] * dz);
-        inh[2] = f[2] + (f[6] * dx + f[8] * dy + f[9] * dz);
-        inh[3] = f[3] - ((f[0] * dx + f[1] * dy) + f[2] * dz);
+        float v[10];
 #pragma unroll
-        for (int c = 4; c < 12; c++) inh[c] = f[c];
-        const float4 g0 = g[a - 1][0], g1 = g[a - 1][1], g2 = g[a - 1][2];
-        f[0] = g0.x + inh[0];
-        f[1] = g0.y + inh[1];
-        f[2] = g0.z + inh[2];
-        f[3] = g0.w + inh[3];
-        f[4] = g1.x + inh[4];
-        f[5] = g1.y + inh[5];
-        f[6] = g1.z + inh[6];
-        f[7] = g1.w + inh[7];
-        f[8] = g2.x + inh[8];
-        f[9] = g2.y + inh[9];
-        f[10] = g2.z + inh[10];
-        f[11] = g2.w + inh[11];
+        for (int k = 0; k < 10; k++) v[k] = __shfl_sync(0xFFFFFFFFu, f, k);
+        // inherited (wgsl:603-609): a += J . delta, phi -= a . delta, J unchanged.
+        float inh = f;
+        if (c == 0u) inh = v[0] + (v[4] * dx + v[5] * dy + v[6] * dz);
+        if (c == 1u) inh = v[1] + (v[5] * dx + v[7] * dy + v[8] * dz);
+        if (c == 2u) inh = v[2] + (v[6] * dx + v[8] * dy + v[9] * dz);
+        if (c == 3u) inh = v[3] - ((v[0] * dx + v[1] * dy) + v[2] * dz);
+        f = g[a - 1] + inh;
       }
     }
 
@@ -452,56 +483,46 @@ __global__ void __launch_bounds__(256) k_l2l_near(const SceneDesc *__restrict__ 
         const int sx = (int)tx + dx, sy = (int)ty + dy, sz = (int)tz + dz;
         float out[10];
 #pragma unroll
-        for (int c = 0; c < 10; c++) out[c] = 0.0f;
+        for (int k = 0; k < 10; k++) out[k] = 0.0f;
         if (sx >= 0 && sy >= 0 && sz >= 0 && sx < (int)dim && sy < (int)dim && sz < (int)dim) {
           const float4 s = __ldg(&src[lvl_base + lin3((uint32_t)sx, (uint32_t)sy, (uint32_t)sz, dim)]);
           if (s.w != 0.0f) pair_field_d(s, ctx, cty, ctz, near_eps, out);
         }
 #pragma unroll
-        for (int c = 0; c < 10; c++) sh.vals[warp][c][lane] = out[c];
+        for (int k = 0; k < 10; k++) sh.vals[warp][k][lane] = out[k];
       }
       __syncwarp();
       if (lane < 10u) {
-        float acc = f[0];
-#pragma unroll
-        for (int c = 1; c < 10; c++)
-          if ((int)lane == c) acc = f[c];
         const float *row = sh.vals[warp][lane];
-        for (uint32_t k = 0; k < 26u; k++) acc = acc + row[k];
-        fields[(size_t)target * 12u + lane] = acc;
-      } else if (lane < 12u) {
-        fields[(size_t)target * 12u + lane] = f[lane == 10u ? 10 : 11];
+        for (uint32_t k = 0; k < 26u; k++) f = f + row[k];
       }
       __syncwarp();
-    } else if (lane < 12u) {
-      float v = f[0];
-#pragma unroll
-      for (int c = 1; c < 12; c++)
-        if ((int)lane == c) v = f[c];
-      fields[(size_t)target * 12u + lane] = v;
     }
+    if (lane < 12u) fields[(size_t)target * 12u + lane] = f;
   }
+  grid_dependents_may_launch();
 }
 
 // --------------------------------------------------------------- launches
 
 void launch_upward(const LaunchCtx &L, uint32_t list_par, uint32_t tasks) {
-  k_upward<<<tasks, 512, 0, L.stream>>>(L.scenes, L.task_scene, L.mom, L.mom_next, L.src, L.aux,
-                                        L.fields,
-                                        L.plist, L.plist_cap, L.plist_prev, L.ctr, list_par,
-                                        L.tickets);
+  launch_step_kernel(L, k_upward, dim3(tasks), dim3(256), 0, L.scenes, L.task_scene, L.mom,
+                     L.mom_next, L.src, L.aux, L.choice, L.fields, L.plist, L.plist_cap, L.plist_prev,
+                     L.ctr, list_par, L.tickets);
 }
 
 size_t m2l_smem_bytes() { return sizeof(M2LShared) + 128; }
 
 void launch_m2l(const LaunchCtx &L, uint32_t list_par, uint32_t grid) {
-  k_m2l<<<grid, 256, m2l_smem_bytes(), L.stream>>>(L.scenes, L.plist, L.plist_cap, L.ctr, list_par,
-                                                    L.mom, L.src, L.lfield, L.tmaps);
+  launch_step_kernel(L, k_m2l, dim3(grid), dim3(256), m2l_smem_bytes(), L.scenes,
+                     (const WorkItem *)L.plist, L.plist_cap, L.ctr, list_par, (const uint4 *)L.mom,
+                     (const float4 *)L.src, L.lfield, L.tmaps);
 }
 
 void launch_l2l_near(const LaunchCtx &L, uint32_t list_par, uint32_t grid) {
-  k_l2l_near<<<grid, 256, 0, L.stream>>>(L.scenes, L.plist, L.plist_cap, L.ctr, list_par, L.mom,
-                                         L.src, L.lfield, L.fields);
+  launch_step_kernel(L, k_l2l_near, dim3(grid), dim3(256), 0, L.scenes, (const WorkItem *)L.plist,
+                     L.plist_cap, (const Counters *)L.ctr, list_par, (const uint4 *)L.mom,
+                     (const float4 *)L.src, (const float *)L.lfield, L.fields);
 }
 
 cudaError_t configure_tree_kernels() {

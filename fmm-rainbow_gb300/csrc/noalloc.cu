@@ -11,7 +11,7 @@
 //
 // Limits and sharing:
 //   * at most kMaxBodies = 131,072 bodies (planner depth 4 or 5, at most
-//     37,449 cells); the array is about 7.4 MB and every GPU that loads the
+//     37,449 cells); the array is about 7.9 MB and every GPU that loads the
 //     library holds it until the process exits;
 //   * every call shares the one array, which keeps the last call's contents;
 //     calls that overlap on the GPU (different streams, or different host
@@ -56,7 +56,8 @@ struct Scratch {
   alignas(16) uint4 mom_next[kMaxCells];       // leaf level the upward pass zeroes
   alignas(16) float4 src[kMaxCells];
   alignas(16) float lfield[12 * kMaxCells];
-  alignas(16) float2 aux[kMaxCells];
+  alignas(16) float4 aux[kMaxCells];
+  alignas(16) uint32_t choice[kMaxCells];
   alignas(16) WorkItem plist[2][kMaxParents];
 };
 static_assert(offsetof(Scratch, lfield) % 16 == 0 && offsetof(Scratch, src) % 16 == 0 &&
@@ -207,6 +208,7 @@ extern "C" int rfmm_solve_fields_noalloc(const void *device_particles, uint32_t 
   L.mom_next = S->mom_next;
   L.src = S->src;
   L.aux = S->aux;
+  L.choice = S->choice;
   L.lfield = S->lfield;
   L.fields = static_cast<float *>(device_fields);
   L.plist = S->plist[0];
@@ -216,6 +218,7 @@ extern "C" int rfmm_solve_fields_noalloc(const void *device_particles, uint32_t 
   L.tickets = S->tickets;
   L.tmaps = S->tmaps;
   L.body_ctas = st.body_ctas;
+  L.pdl = false;
 
   launch_deposit(L, L.mom, tiles);
   launch_upward(L, 0u, tasks);

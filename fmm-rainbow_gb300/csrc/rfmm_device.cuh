@@ -77,9 +77,17 @@ __device__ __forceinline__ uint32_t level_of_d(uint32_t g) {
   return level;
 }
 
-struct Pair10 {
-  float v[10];  // ax ay az phi Jxx Jxy Jxz Jyy Jyz Jzz
-};
+// Programmatic dependent launch: a kernel launched with the programmatic
+// stream-serialization attribute may start while its predecessor drains;
+// grid_dependency_wait() blocks until the predecessor grid has completed and
+// its writes are visible, so every kernel calls it before touching data the
+// predecessor produced or consumed.  Without the attribute both are no-ops.
+__device__ __forceinline__ void grid_dependency_wait() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+__device__ __forceinline__ void grid_dependents_may_launch() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
 
 // pair_field (wgsl:170-203) for a source cell whose centre of mass `src`
 // and gravity-times-mass `gm` were precomputed exactly as the reference
@@ -108,12 +116,21 @@ __device__ __forceinline__ void pair_field_d(float4 src, float tx, float ty, flo
 
 // Per-cell terms of integrate's self-leaf and excitation update that depend
 // only on the cell's count: (G * f32(count - 1) / f32(N), clamp((f32(count) -
-// 16) / 72, 0, 1)) (wgsl:655-656, 703-707), evaluated once per cell.
-__device__ __forceinline__ float2 make_aux(uint32_t count, float gravity, float n_f) {
+// 16) / 72, 0, 1), count bits, 0) (wgsl:646-656, 703-707), evaluated once per
+// cell with the reference's expressions.
+__device__ __forceinline__ float4 make_aux(uint32_t count, float gravity, float n_f) {
   const float self_mass = count > 1u ? (float)(count - 1u) / n_f : 0.0f;
-  return make_float2(gravity * self_mass,
-                     clampf_d(((float)count - (float)kAdaptive) / 72.0f, 0.0f, 1.0f));
+  return make_float4(gravity * self_mass,
+                     clampf_d(((float)count - (float)kAdaptive) / 72.0f, 0.0f, 1.0f),
+                     __uint_as_float(count), 0.0f);
 }
+
+// The cell integrate samples for bodies of one leaf (wgsl:625-639) depends
+// only on the counts of the leaf's ancestors, so it is resolved once per leaf:
+// (level << 28) | local cell index, or kChoiceUnresolved when the leaf's
+// subtree root holds at most 16 bodies (then an ancestor above the subtree
+// may be the sampled cell and integrate descends itself).
+constexpr uint32_t kChoiceUnresolved = 0xFFFFFFFFu;
 
 // Source record of a cell: centre of mass and G * mass (0 for empty cells).
 // com = f32(sum) * (1 / (scale * f32(count))), mass = f32(count) / f32(N)

@@ -21,7 +21,8 @@ struct LaunchCtx {
   uint4 *mom;                  // moments of the current positions (leaf level valid)
   uint4 *mom_next;             // leaf level receives the integrate deposit
   float4 *src;                 // per-cell (com, G*m)
-  float2 *aux;                 // per-cell (G*(count-1)/N, density pulse) for integrate
+  float4 *aux;                 // per-cell (G*(count-1)/N, density pulse, count) for integrate
+  uint32_t *choice;            // per-leaf sample cell of integrate's descent
   float *lfield;               // per-cell M2L result (12 floats)
   float *fields;               // per-cell final field (12 floats, reference layout)
   WorkItem *plist;             // parent list written this step
@@ -31,7 +32,36 @@ struct LaunchCtx {
   uint32_t *tickets;
   const CUtensorMap *tmaps;    // 8 per scene (levels 0..7; 3..6 used)
   uint32_t body_ctas;          // persistent grid of the body passes (resident CTAs)
+  bool pdl;                    // launch step kernels with programmatic stream serialization
 };
+
+// Launch `kernel` on L.stream, with programmatic dependent launch when L.pdl:
+// the kernel may start while its predecessor drains and waits for it with
+// griddepcontrol.wait before touching shared data.
+template <typename... K, typename... A>
+inline void launch_step_kernel(const LaunchCtx &L, void (*kernel)(K...), dim3 grid, dim3 block,
+                               size_t smem, A &&...args) {
+  if (!L.pdl) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = L.stream;
+    cudaLaunchKernelEx(&cfg, kernel, static_cast<A &&>(args)...);
+    return;
+  }
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = L.stream;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kernel, static_cast<A &&>(args)...);
+}
 
 // Tree passes (kernels_tree.cu).
 void launch_upward(const LaunchCtx &L, uint32_t list_par, uint32_t tasks);

@@ -145,7 +145,7 @@ int rfmm_phase_times(rfmm_handle *h, float ms[7]);
 int rfmm_check_finite(rfmm_handle *h, uint32_t probe, uint32_t *non_finite, float *max_abs);
 
 /* Steps between refreshes of the resident leaf order (0 = never; default
- * 16).  Results do not depend on it. */
+ * 64).  Results do not depend on it. */
 int rfmm_set_resort_interval(rfmm_handle *h, uint32_t steps);
 
 /* Last kernel error word (0 = none) and its detail. */
@@ -185,7 +185,7 @@ int rfmm_launch_count(rfmm_handle *h, uint64_t *out);
  * default stream).  Work is enqueued asynchronously on `stream`.
  *
  * It calls no cudaMalloc/cudaFree: its intermediate data lives in one fixed
- * __device__ array of about 7.4 MB that every GPU loading this library holds
+ * __device__ array of about 7.9 MB that every GPU loading this library holds
  * until exit, so n is limited to 1..131072 (tree depth 4 or 5); larger n
  * returns RFMM_ERR_INVALID.  Every call reuses that one array: calls that
  * overlap on the GPU race on it.  The first call on a device does a one-time
