@@ -55,6 +55,11 @@ WORKLOADS = {
     "clusters_5m": dict(kind="clusters", n=5242880, seed=3, fmm_steps=60, dt=5e-4, eps=5e-4, G=1.0,
                         desc="8 Plummer clusters a~logU[0.02,0.1], centres U[0.2,0.8]^3, "
                              "N=5,242,880, eps=5e-4, bulk sigma 0.05, 60 steps dt=5e-4"),
+    # Batched form: many scenes per launch, against the same scenes back to back.
+    "batched_256": dict(kind="batched", scenes=256, n_min=4096, n_max=262144, seed=4,
+                        fmm_steps=60, dt=5e-4, eps=1e-3, G=1.0,
+                        desc="256 scenes, N log-uniform [4096, 262144], half uniform cube, "
+                             "half Plummer a=0.1, G=1, eps=1e-3, 60 steps dt=5e-4"),
 }
 
 PEAKS_FILE = os.path.join(REPO, "MEASURED_PEAKS.json")
@@ -85,6 +90,16 @@ def dist_env():
 def make_scene(w):
     from rfmm import scenes
     return scenes.make(w["kind"], w["n"], w["seed"])
+
+
+def batch_scenes(w):
+    """The batched workload's scenes: seeded sizes, alternating uniform / Plummer."""
+    import numpy as np
+    from rfmm import scenes
+    rng = np.random.default_rng(w["seed"])
+    sizes = np.exp(rng.uniform(np.log(w["n_min"]), np.log(w["n_max"]), w["scenes"])).astype(int)
+    return [scenes.make("uniform" if i % 2 == 0 else "plummer", int(n), 1000 + i)
+            for i, n in enumerate(sizes)]
 
 
 def roofline_bytes_integrate(n, cells, depth):
@@ -182,28 +197,37 @@ def run_reference(args, w):
         return 0
     from oracle import oracle as O
     cores = O.set_threads(os.cpu_count() or 1)
-    scene = make_scene(w)
-    st = O.OracleState(scene, O.make_params(w["n"], gravity=w["G"], softening=w["eps"], dt=w["dt"]))
+    if w["kind"] == "batched":
+        ps = batch_scenes(w)
+        states = [O.OracleState(p, O.make_params(len(p), gravity=w["G"], softening=w["eps"],
+                                                 dt=w["dt"])) for p in ps]
+        bodies = sum(len(p) for p in ps)
+    else:
+        states = [O.OracleState(make_scene(w), O.make_params(w["n"], gravity=w["G"],
+                                                             softening=w["eps"], dt=w["dt"]))]
+        bodies = w["n"]
     for _ in range(args.warmup):
-        st.step(1)
+        for st in states:
+            st.step(1)
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        st.step(1)
+        for st in states:
+            st.step(1)
         times.append(time.perf_counter() - t0)
     total = sum(times)
-    value = w["n"] * args.steps / total
+    value = bodies * args.steps / total
     line = {
         "impl": "reference", "metric": "body-steps/s", "value": value, "unit": "body-steps/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded): " + w["desc"],
-        "config": {"workload": args.workload, "bodies": w["n"], "fmm_steps_per_bench_step": 1,
+        "config": {"workload": args.workload, "bodies": bodies, "fmm_steps_per_bench_step": 1,
                    "implementation": "CPU oracle port of the reference compute passes "
                                      "(reference wgpu/Vulkan harness unavailable on this box)"},
         "cpu_baseline": {"value": value, "unit": "body-steps/s", "cores": cores, "kind": "port",
                          "sample": "one FMM step of %d bodies per bench step, %d host threads"
-                                   % (w["n"], cores)},
+                                   % (bodies, cores)},
         "e2e": {"value": value, "unit": "body-steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -324,11 +348,150 @@ def run_gpu(args, w):
     return 0
 
 
+def run_gpu_batched(args, w):
+    """Batched form vs the same scenes solved back to back through plain handles."""
+    import numpy as np
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from rfmm import build as pkg_build
+    pkg_build.build()
+    import rfmm
+    from rfmm import replicas
+
+    all_scenes = batch_scenes(w)
+    mine = replicas.shard_scenes([len(p) for p in all_scenes], world)[rank]
+    ps = [all_scenes[i] for i in mine]
+    sizes = [len(p) for p in ps]
+    bodies = sum(sizes)
+    fmm_steps = w["fmm_steps"]
+    params = rfmm.default_params(gravity=w["G"], softening=w["eps"], dt=w["dt"])
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    dev = [torch.from_numpy(p.view(np.uint8).copy()).cuda() for p in ps]
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    batch = rfmm.Batch(sizes, [params] * len(ps))
+    batch.set_stream(stream.cuda_stream)
+
+    def batched_step():
+        for i, d in enumerate(dev):
+            batch.upload_device(i, d.data_ptr(), d.numel())
+        batch.commit()
+        batch.step(fmm_steps)
+
+    def timed(fn, k):
+        st = [torch.cuda.Event(enable_timing=True) for _ in range(k)]
+        en = [torch.cuda.Event(enable_timing=True) for _ in range(k)]
+        for j in range(k):
+            flush.zero_()
+            st[j].record(stream)
+            fn()
+            en[j].record(stream)
+        torch.cuda.synchronize()
+        return sum(a.elapsed_time(b) for a, b in zip(st, en))
+
+    for _ in range(args.warmup):
+        batched_step()
+    torch.cuda.synchronize()
+    clk = clocks_sampler(local)
+    time.sleep(0.3)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    l0 = batch.launch_count()
+    local_ms = timed(batched_step, args.steps)
+    if world > 1:
+        torch.distributed.barrier()
+    launches = batch.launch_count() - l0
+    clocks = clocks_summary(clk)
+    value, _, slowest_s = replicas.reduce_throughput(bodies * fmm_steps * args.steps, local_ms * 1e-3)
+
+    # The same scenes back to back through plain handles (one handle per scene).
+    solvers = []
+    for p in ps:
+        s = rfmm.Solver(len(p), params)
+        s.set_stream(stream.cuda_stream)
+        solvers.append(s)
+
+    def plain_step():
+        for s, d in zip(solvers, dev):
+            s.upload_device(d.data_ptr(), d.numel())
+            s.step(fmm_steps)
+
+    plain_step()
+    torch.cuda.synchronize()
+    plain_k = max(1, min(args.steps, 3))
+    plain_ms = timed(plain_step, plain_k)
+    plain_value = bodies * fmm_steps * plain_k / (plain_ms * 1e-3)
+    for s in solvers:
+        s.close()
+
+    prof = batch.profile_steps(fmm_steps)
+    kernel_ms = {k: (v[0] / v[1] if v[1] else 0.0) for k, v in prof.items()}
+    integ_ms, integ_n = prof["integrate"]
+    alg = sum(64 * n for n in sizes) + sum(64 * pl[1] + 16 * 8 ** pl[0] for pl in batch.plans)
+    peak, peak_kind = hbm_peak()
+    achieved = alg / (integ_ms / integ_n * 1e-3) / 1e9
+    roofline = {"kernel": "k_integrate", "bound": "hbm", "achieved": achieved, "peak": peak,
+                "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                "algorithmic_bytes_per_launch": alg, "avg_launch_ms": integ_ms / integ_n,
+                "traffic": traffic_for(args.workload)}
+
+    # End to end: pinned host scenes in, every scene's particles out.
+    pin = [torch.from_numpy(p.view(np.uint8).copy()).pin_memory() for p in ps]
+    outs = [torch.empty(len(p) * 32, dtype=torch.uint8).pin_memory() for p in ps]
+    e2e_times = []
+    for k in range(args.e2e_steps + 1 if args.e2e_steps > 0 else 0):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for i, t in enumerate(pin):
+            rfmm._check(rfmm.lib().rfmm_batch_upload(batch._h, i, t.data_ptr(), t.numel()), "upload")
+        batch.commit()
+        batch.step(fmm_steps)
+        for i, t in enumerate(outs):
+            rfmm._check(rfmm.lib().rfmm_batch_download(batch._h, i, rfmm.BUF_PARTICLES, t.data_ptr(),
+                                                       t.numel()), "download")
+        if k > 0:
+            e2e_times.append(time.perf_counter() - t0)
+    e2e = None
+    if e2e_times:
+        e2e_s = statistics.mean(e2e_times)
+        e2e = {"value": world * bodies * fmm_steps / e2e_s, "unit": "body-steps/s",
+               "h2d_bytes_per_step": bodies * 32, "d2h_bytes_per_step": bodies * 32,
+               "ms_per_step": 1e3 * e2e_s, "timer": "host wall clock"}
+    line = {
+        "metric": "body-steps/s", "value": value, "unit": "body-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": slowest_s * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded, numpy PCG64): " + w["desc"],
+        "config": {"workload": args.workload, "form": "batched (all scenes per launch)",
+                   "scenes": len(ps), "bodies": bodies, "fmm_steps_per_bench_step": fmm_steps,
+                   "plain_back_to_back_body_steps_per_s": plain_value,
+                   "batched_over_plain": value / world / plain_value,
+                   "l2": "flushed between timed steps (512 MiB write outside the events)",
+                   "parallelism": "scenes sharded over %d rank(s)" % world},
+        "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
+        "kernel_avg_ms": kernel_ms,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    batch.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
 def main():
     args = parse_args()
     w = WORKLOADS[args.workload]
     if args.impl == "reference":
         return run_reference(args, w)
+    if w["kind"] == "batched":
+        return run_gpu_batched(args, w)
     return run_gpu(args, w)
 
 

@@ -100,6 +100,24 @@ SIGNATURES = {
     "rfmm_profile_steps": (_i, [_vp, _u32, C.POINTER(_f32), C.POINTER(_u32)]),
     "rfmm_launch_count": (_i, [_vp, C.POINTER(C.c_uint64)]),
     "rfmm_solve_fields_noalloc": (_i, [_vp, _u32, _P, _vp, _vp, _vp]),
+    "rfmm_batch_create": (_i, [_u32, C.POINTER(_u32), _P, C.POINTER(_vp)]),
+    "rfmm_batch_destroy": (_i, [_vp]),
+    "rfmm_batch_set_stream": (_i, [_vp, _vp]),
+    "rfmm_batch_get_plan": (_i, [_vp, _u32, C.POINTER(Plan)]),
+    "rfmm_batch_set_params": (_i, [_vp, _u32, _P]),
+    "rfmm_batch_upload": (_i, [_vp, _u32, _vp, _sz]),
+    "rfmm_batch_upload_device": (_i, [_vp, _u32, _vp, _sz]),
+    "rfmm_batch_seed_galaxy": (_i, [_vp, _u32]),
+    "rfmm_batch_commit": (_i, [_vp]),
+    "rfmm_batch_solve_fields": (_i, [_vp]),
+    "rfmm_batch_step": (_i, [_vp, _u32]),
+    "rfmm_batch_sync": (_i, [_vp]),
+    "rfmm_batch_download": (_i, [_vp, _u32, _i, _vp, _sz]),
+    "rfmm_batch_download_device": (_i, [_vp, _u32, _i, _vp, _sz]),
+    "rfmm_batch_digest": (_i, [_vp, _u32, _i, C.POINTER(_u32)]),
+    "rfmm_batch_launch_count": (_i, [_vp, C.POINTER(C.c_uint64)]),
+    "rfmm_batch_profile_steps": (_i, [_vp, _u32, C.POINTER(_f32), C.POINTER(_u32)]),
+    "rfmm_batch_set_resort_interval": (_i, [_vp, _u32]),
 }
 KERNEL_KINDS = ("upward", "m2l", "l2l_near", "integrate", "resort")
 
@@ -295,3 +313,90 @@ class Solver:
         code, info = C.c_uint32(), C.c_uint32()
         _check(lib().rfmm_device_error(self._h, C.byref(code), C.byref(info)), "rfmm_device_error")
         return code.value, info.value
+
+
+class Batch:
+    """Many independent scenes stepped together (the `rfmm_batch_*` handle)."""
+
+    def __init__(self, sizes, params=None):
+        sizes = [int(x) for x in sizes]
+        arr = (C.c_uint32 * len(sizes))(*sizes)
+        prm = None
+        if params is not None:
+            prm = (Params * len(sizes))(*params)
+        self._h = C.c_void_p()
+        _check(lib().rfmm_batch_create(len(sizes), arr, prm, C.byref(self._h)), "rfmm_batch_create")
+        self.sizes = sizes
+        self.plans = []
+        for i in range(len(sizes)):
+            plan = Plan()
+            _check(lib().rfmm_batch_get_plan(self._h, i, C.byref(plan)), "rfmm_batch_get_plan")
+            self.plans.append((plan.depth, plan.cells, plan.fixed_point_scale))
+
+    def close(self):
+        if self._h:
+            lib().rfmm_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_stream(self, stream_ptr):
+        _check(lib().rfmm_batch_set_stream(self._h, stream_ptr or None), "rfmm_batch_set_stream")
+
+    def set_resort_interval(self, steps):
+        _check(lib().rfmm_batch_set_resort_interval(self._h, steps), "rfmm_batch_set_resort_interval")
+
+    def upload(self, scene, particles):
+        a = np.ascontiguousarray(particles)
+        assert a.dtype == PARTICLE_DTYPE and len(a) == self.sizes[scene]
+        _check(lib().rfmm_batch_upload(self._h, scene, a.ctypes.data, a.nbytes), "rfmm_batch_upload")
+
+    def upload_device(self, scene, ptr, nbytes):
+        _check(lib().rfmm_batch_upload_device(self._h, scene, ptr, nbytes), "rfmm_batch_upload_device")
+
+    def commit(self):
+        _check(lib().rfmm_batch_commit(self._h), "rfmm_batch_commit")
+
+    def solve_fields(self):
+        _check(lib().rfmm_batch_solve_fields(self._h), "rfmm_batch_solve_fields")
+
+    def step(self, steps=1):
+        _check(lib().rfmm_batch_step(self._h, steps), "rfmm_batch_step")
+
+    def sync(self):
+        _check(lib().rfmm_batch_sync(self._h), "rfmm_batch_sync")
+
+    def download(self, scene, which=BUF_PARTICLES):
+        depth, cells, _ = self.plans[scene]
+        dtype, count = {BUF_PARTICLES: (PARTICLE_DTYPE, self.sizes[scene]),
+                        BUF_MOMENTS: (MOMENT_DTYPE, cells), BUF_FIELDS: (FIELD_DTYPE, cells)}[which]
+        out = np.empty(count, dtype)
+        _check(lib().rfmm_batch_download(self._h, scene, which, out.ctypes.data, out.nbytes),
+               "rfmm_batch_download")
+        return out
+
+    def digest(self, scene, which):
+        out = C.c_uint32()
+        _check(lib().rfmm_batch_digest(self._h, scene, which, C.byref(out)), "rfmm_batch_digest")
+        return out.value
+
+    def launch_count(self):
+        out = C.c_uint64()
+        _check(lib().rfmm_batch_launch_count(self._h, C.byref(out)), "rfmm_batch_launch_count")
+        return out.value
+
+    def profile_steps(self, steps):
+        ms = (C.c_float * len(KERNEL_KINDS))()
+        cnt = (C.c_uint32 * len(KERNEL_KINDS))()
+        _check(lib().rfmm_batch_profile_steps(self._h, steps, ms, cnt), "rfmm_batch_profile_steps")
+        return {k: (ms[i], cnt[i]) for i, k in enumerate(KERNEL_KINDS)}

@@ -36,6 +36,7 @@ SOURCES = [
     "noalloc.cu",
     "engine.cpp",
     "capi.cpp",
+    "capi_batch.cpp",
     "planner.cpp",
 ]
 # Text embedded as the "shader" payload of rainbow_shader_ptr().

@@ -172,6 +172,41 @@ int rfmm_profile_steps(rfmm_handle *h, uint32_t steps, float *kernel_ms, uint32_
  * CUDA graphs included). */
 int rfmm_launch_count(rfmm_handle *h, uint64_t *out);
 
+/* ------------------------------------------------------------------ batches
+ *
+ * Many independent scenes of uneven size in one set of launches: every
+ * kernel of a step covers all scenes (concatenated body tiles, concatenated
+ * per-scene trees, one parent work list), and each scene keeps its own plan,
+ * parameters and buffers in the reference layouts.  Results per scene are
+ * identical to a plain handle's.  A batch replaces running the reference's
+ * dispatch sequence once per scene. */
+typedef struct rfmm_batch rfmm_batch;
+
+/* `params` points to `scenes` parameter blocks, or is NULL for the harness
+ * defaults for every scene. */
+int rfmm_batch_create(uint32_t scenes, const uint32_t *bodies_per_scene, const rfmm_params *params,
+                      rfmm_batch **out);
+int rfmm_batch_destroy(rfmm_batch *b);
+int rfmm_batch_set_stream(rfmm_batch *b, void *stream);
+int rfmm_batch_get_plan(const rfmm_batch *b, uint32_t scene, rfmm_plan *out);
+int rfmm_batch_set_params(rfmm_batch *b, uint32_t scene, const rfmm_params *params);
+/* Stage a scene's bodies (host or device memory); rfmm_batch_commit makes
+ * every staged scene resident (sort + deposit) in one pass. */
+int rfmm_batch_upload(rfmm_batch *b, uint32_t scene, const void *host_aos, size_t bytes);
+int rfmm_batch_upload_device(rfmm_batch *b, uint32_t scene, const void *device_aos, size_t bytes);
+int rfmm_batch_seed_galaxy(rfmm_batch *b, uint32_t scene);
+int rfmm_batch_commit(rfmm_batch *b);
+int rfmm_batch_solve_fields(rfmm_batch *b);
+int rfmm_batch_step(rfmm_batch *b, uint32_t steps);
+int rfmm_batch_sync(rfmm_batch *b);
+int rfmm_batch_download(rfmm_batch *b, uint32_t scene, int which, void *host_dst, size_t bytes);
+int rfmm_batch_download_device(rfmm_batch *b, uint32_t scene, int which, void *device_dst,
+                               size_t bytes);
+int rfmm_batch_digest(rfmm_batch *b, uint32_t scene, int which, uint32_t *out);
+int rfmm_batch_launch_count(rfmm_batch *b, uint64_t *out);
+int rfmm_batch_profile_steps(rfmm_batch *b, uint32_t steps, float *kernel_ms, uint32_t *launches);
+int rfmm_batch_set_resort_interval(rfmm_batch *b, uint32_t steps);
+
 /* Allocation-free field solve (this entry point has no counterpart in the
  * reference).  For callers that cannot allocate device memory -- a plugin
  * whose device memory is owned by the host framework, or code running where
