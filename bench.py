@@ -55,6 +55,12 @@ WORKLOADS = {
     "clusters_5m": dict(kind="clusters", n=5242880, seed=3, fmm_steps=60, dt=5e-4, eps=5e-4, G=1.0,
                         desc="8 Plummer clusters a~logU[0.02,0.1], centres U[0.2,0.8]^3, "
                              "N=5,242,880, eps=5e-4, bulk sigma 0.05, 60 steps dt=5e-4"),
+    # Served form: Poisson request arrivals, continuous batching.
+    "served": dict(kind="served", n_min=16384, n_max=2097152, steps_max=60, seed=5, dt=5e-4,
+                   eps=1e-3, G=1.0, rates=[50, 200, 1000, 2000], requests=300, slots=128,
+                   budget=150 << 30, fmm_steps=None,
+                   desc="requests with N log-uniform [16384, 2097152] (uniform / Plummer / "
+                        "4-cluster), steps U[1,60], dt=5e-4, eps=1e-3, Poisson arrivals"),
     # Batched form: many scenes per launch, against the same scenes back to back.
     "batched_256": dict(kind="batched", scenes=256, n_min=4096, n_max=262144, seed=4,
                         fmm_steps=60, dt=5e-4, eps=1e-3, G=1.0,
@@ -77,6 +83,8 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=8)
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--requests", type=int, default=0, help="served: requests per rate point")
+    ap.add_argument("--rates", type=float, nargs="*", default=None, help="served: arrival rates /s")
     return ap.parse_args()
 
 
@@ -485,6 +493,102 @@ def run_gpu_batched(args, w):
     return 0
 
 
+def served_requests(w, count):
+    """Seeded request pool: (particles, steps)."""
+    import numpy as np
+    from rfmm import scenes
+    rng = np.random.default_rng(w["seed"])
+    out = []
+    for i in range(count):
+        n = int(np.exp(rng.uniform(np.log(w["n_min"]), np.log(w["n_max"]))))
+        steps = int(rng.integers(1, w["steps_max"] + 1))
+        kind = ("uniform", "plummer", "clusters4")[i % 3]
+        out.append((scenes.make(kind, n, 2000 + i), steps))
+    return out
+
+
+def run_gpu_served(args, w):
+    """Throughput and p50/p99 latency of the continuous-batching server."""
+    import threading
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    from rfmm import build as pkg_build
+    pkg_build.build()
+    import rfmm
+
+    import numpy as np
+    count = max(4, args.requests or w["requests"])
+    pool = served_requests(w, count)
+    params = rfmm.default_params(gravity=w["G"], softening=w["eps"], dt=w["dt"])
+    rates = args.rates or w["rates"]
+    sweep = []
+    clk = None
+    launches = 0
+    # Warm-up: module load and first graph captures on a small server.
+    warm = rfmm.Server(max_bodies=w["n_max"], memory_budget_bytes=w["budget"], max_slots=4,
+                       max_chunk_steps=4)
+    for p, steps in pool[: min(3, len(pool))]:
+        rid = warm.submit(p, steps, params)
+        warm.wait(rid, 600000)
+        warm.result(rid)
+    warm.close()
+    for ri, rate in enumerate(rates):
+        srv = rfmm.Server(max_bodies=w["n_max"], memory_budget_bytes=w["budget"],
+                          max_slots=w["slots"], max_chunk_steps=4)
+        arrivals = np.cumsum(np.random.default_rng(w["seed"] + ri).exponential(1.0 / rate, count))
+        ids = [None] * count
+        if ri == len(rates) - 1:
+            clk = clocks_sampler(local)
+        t0 = time.perf_counter()
+
+        def producer():
+            for i, (p, steps) in enumerate(pool):
+                delay = t0 + arrivals[i] - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+                ids[i] = srv.submit(p, steps, params)
+
+        th = threading.Thread(target=producer)
+        th.start()
+        th.join()
+        for rid in ids:
+            srv.wait(rid, 3600000)
+            srv.result(rid)
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        srv.close()
+        sweep.append({"rate_per_s": rate, "requests": count, "p50_ms": st["p50_ms"],
+                      "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"], "max_ms": st["max_ms"],
+                      "body_steps_per_s": st["body_steps_per_s"], "wall_s": wall,
+                      "slots": st["slots"]})
+    clocks = clocks_summary(clk)
+    top = sweep[-1]
+    body_steps = sum(len(p) * s for p, s in pool)
+    line = {
+        "metric": "body-steps/s", "value": top["body_steps_per_s"], "unit": "body-steps/s",
+        "n_gpus": world, "steps": count, "warmup": 3, "ms_per_step": top["wall_s"] * 1e3 / count,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded, numpy PCG64): " + w["desc"],
+        "config": {"workload": args.workload, "form": "served (continuous batching)",
+                   "requests_per_rate": count, "body_steps_per_rate": body_steps,
+                   "memory_budget_bytes": w["budget"], "slot_capacity": w["n_max"],
+                   "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"], "sweep": sweep,
+                   "timer": "host wall clock, submit to result on host",
+                   "parallelism": "1 GPU"},
+        "clocks": clocks,
+        "e2e": {"value": top["body_steps_per_s"], "unit": "body-steps/s",
+                "h2d_bytes_per_step": body_steps and int(sum(len(p) for p, _ in pool) * 32 / count),
+                "d2h_bytes_per_step": int(sum(len(p) for p, _ in pool) * 32 / count),
+                "note": "a step is one request; the served path is end to end by construction"},
+        "gpu_launches": None,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse_args()
     w = WORKLOADS[args.workload]
@@ -492,6 +596,8 @@ def main():
         return run_reference(args, w)
     if w["kind"] == "batched":
         return run_gpu_batched(args, w)
+    if w["kind"] == "served":
+        return run_gpu_served(args, w)
     return run_gpu(args, w)
 
 

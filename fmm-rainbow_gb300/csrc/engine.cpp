@@ -121,6 +121,9 @@ int Engine::create(const std::vector<SceneSpec> &specs, Engine **out) {
     d.control_strength = sp.params.control_strength;
     d.control_radius = sp.params.control_radius;
     d.key_base = 0u;  // set below, once the number of scenes fixes the key width
+    d.max_depth = d.depth;
+    d.tile_cap = pad_tiles(sp.n);
+    if (sp.slot) E->use_lists_ = true;
     for (int k = 0; k < 4; k++) {
       d.control_point[k] = sp.params.control_point[k];
       d.control_axis_mode[k] = sp.params.control_axis_mode[k];
@@ -129,6 +132,7 @@ int Engine::create(const std::vector<SceneSpec> &specs, Engine **out) {
     for (uint32_t t = 0; t < tiles; t++) E->tile_scene_h_.push_back(i);
     const uint32_t ntasks = 1u << (3u * d.sub_level);
     for (uint32_t t = 0; t < ntasks; t++) E->task_scene_h_.push_back(i);
+    if (sp.slot) d.n = 0u;  // an empty slot: no bodies until activate()
     E->plist_cap_ += total_cells(d.depth - 1u);
     body_off += tiles * kTile;
     cell_off += d.cells;
@@ -161,6 +165,8 @@ int Engine::create(const std::vector<SceneSpec> &specs, Engine **out) {
   A((void **)&E->d_scenes_, sizeof(SceneDesc) * specs.size());
   A((void **)&E->d_tile_scene_, 4 * E->tiles_);
   A((void **)&E->d_task_scene_, 4 * E->tasks_);
+  A((void **)&E->d_tile_list_, 4 * E->tiles_);
+  A((void **)&E->d_task_list_, 4 * E->tasks_);
   for (int b = 0; b < 2; b++) {
     A((void **)&E->d_part_[b], 32 * S);
     A((void **)&E->d_ids_[b], 4 * S);
@@ -192,6 +198,8 @@ int Engine::create(const std::vector<SceneSpec> &specs, Engine **out) {
   }
   if (e == cudaSuccess) e = configure_tree_kernels();
   if (e == cudaSuccess) E->body_ctas_ = (uint32_t)E->sms_ * body_ctas_per_sm();
+  E->tree_ctas_ = (uint32_t)E->sms_ * 6u;
+  if (E->use_lists_) E->resort_interval_ = 0;  // slots are sorted when they are filled
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(E->d_scenes_, E->scenes_.data(), sizeof(SceneDesc) * specs.size(),
                         cudaMemcpyHostToDevice, E->stream_);
@@ -218,6 +226,7 @@ int Engine::create(const std::vector<SceneSpec> &specs, Engine **out) {
     return cuda_status(e);
   }
   st = E->build_tensor_maps();
+  if (st == RFMM_OK) st = E->rebuild_lists();
   if (st == RFMM_OK) st = cuda_status(cudaStreamSynchronize(E->stream_));
   if (st != RFMM_OK) {
     delete E;
@@ -313,6 +322,9 @@ LaunchCtx Engine::ctx(uint32_t mpar, uint32_t lpar, uint32_t ppar) const {
   L.tickets = d_tickets_;
   L.tmaps = d_tmaps_;
   L.body_ctas = body_ctas_;
+  L.tree_ctas = tree_ctas_;
+  L.tile_list = use_lists_ ? d_tile_list_ : nullptr;
+  L.task_list = use_lists_ ? d_task_list_ : nullptr;
   L.pdl = pdl_;
   return L;
 }
@@ -347,21 +359,114 @@ uint32_t Engine::resort_kernels() const { return 2u + 3u * ((key_bits_ + 7u) / 8
 
 void Engine::enqueue_resort(uint32_t ppar) {
   LaunchCtx L = ctx(mcur_, lpar_, ppar);
-  launch_keys(L, sort_.keys[0], sort_.vals[0], nullptr, 0, tiles_);
+  launch_keys(L, sort_.keys[0], sort_.vals[0], nullptr, 0, tiles_, 0u);
   const int r = radix_sort(stream_, sort_, slots_, key_bits_);
   launch_gather(L, sort_.vals[r], d_part_[ppar], d_ids_[ppar], d_part_[ppar ^ 1u], d_ids_[ppar ^ 1u],
-                nullptr, tiles_);
+                nullptr, tiles_, 0u);
+}
+
+int Engine::rebuild_lists() {
+  tile_list_h_.clear();
+  task_list_h_.clear();
+  for (const SceneDesc &d : scenes_) {
+    if (d.n == 0u) continue;
+    for (uint32_t t = 0; t < pad_tiles(d.n); t++) tile_list_h_.push_back(d.tile_off + t);
+    for (uint32_t t = 0; t < (1u << (3u * d.sub_level)); t++) task_list_h_.push_back(d.task_off + t);
+  }
+  const uint32_t counts[2] = {(uint32_t)tile_list_h_.size(), (uint32_t)task_list_h_.size()};
+  if (!tile_list_h_.empty())
+    RF_CK(cudaMemcpyAsync(d_tile_list_, tile_list_h_.data(), 4 * tile_list_h_.size(),
+                          cudaMemcpyHostToDevice, stream_));
+  if (!task_list_h_.empty())
+    RF_CK(cudaMemcpyAsync(d_task_list_, task_list_h_.data(), 4 * task_list_h_.size(),
+                          cudaMemcpyHostToDevice, stream_));
+  RF_CK(cudaMemcpyAsync(&d_ctr_->tiles_active, counts, sizeof(counts), cudaMemcpyHostToDevice,
+                        stream_));
+  return RFMM_OK;
+}
+
+int Engine::commit_scene(uint32_t scene) {
+  const SceneDesc &d = scenes_[scene];
+  const uint32_t tiles = pad_tiles(d.n);
+  LaunchCtx L = ctx(mcur_, lpar_, pcur_);
+  launch_keys(L, sort_.keys[0], sort_.vals[0], nullptr, 0, tiles, d.tile_off);
+  const int r = radix_sort(stream_, sort_, tiles * kTile, 3u * d.key_level);
+  RF_CK(cudaMemsetAsync(d_mom_[mcur_] + d.cell_off, 0, 16ull * d.cells, stream_));
+  launch_gather(L, sort_.vals[r], d_part_[pcur_], d_ids_[pcur_], d_part_[pcur_ ^ 1u],
+                d_ids_[pcur_ ^ 1u], d_mom_[mcur_], tiles, d.tile_off);
+  RF_CK(cudaGetLastError());
+  // The sorted scene lands in the other buffer; copy it back into the current one.
+  RF_CK(cudaMemcpyAsync(d_part_[pcur_] + 2ull * d.body_off, d_part_[pcur_ ^ 1u] + 2ull * d.body_off,
+                        32ull * tiles * kTile, cudaMemcpyDeviceToDevice, stream_));
+  RF_CK(cudaMemcpyAsync(d_ids_[pcur_] + d.body_off, d_ids_[pcur_ ^ 1u] + d.body_off,
+                        4ull * tiles * kTile, cudaMemcpyDeviceToDevice, stream_));
+  launches_ += 2u + 3u * ((3u * d.key_level + 7u) / 8u);
+  return RFMM_OK;
+}
+
+int Engine::activate(uint32_t scene, uint32_t n, const rfmm_params &p, const void *src,
+                     cudaMemcpyKind kind) {
+  if (scene >= scenes_.size() || n == 0u) return RFMM_ERR_INVALID;
+  SceneDesc &d = scenes_[scene];
+  if (d.n != 0u) return RFMM_ERR_STATE;
+  if (n > d.tile_cap * kTile) return RFMM_ERR_BUDGET;
+  const uint32_t depth = p.depth ? p.depth : depth_for_particles(n);
+  if (depth < 4u || depth > d.max_depth) return RFMM_ERR_BUDGET;
+  d.n = n;
+  d.depth = depth;
+  d.cells = total_cells(depth);
+  d.sub_level = depth - 3u;
+  d.scale = p.fixed_point_scale > 0.0f ? p.fixed_point_scale : fixed_point_scale(n);
+  d.gravity = p.gravity;
+  d.softening = p.softening;
+  d.dt_eff = p.dt * p.speed;
+  d.n_f = (float)n;
+  d.control_strength = p.control_strength;
+  d.control_radius = p.control_radius;
+  for (int k = 0; k < 4; k++) {
+    d.control_point[k] = p.control_point[k];
+    d.control_axis_mode[k] = p.control_axis_mode[k];
+  }
+  RF_CK(cudaMemcpyAsync(d_scenes_ + scene, &d, sizeof(SceneDesc), cudaMemcpyHostToDevice, stream_));
+  if (src != nullptr)  // null: the caller already staged the bodies at slot_bodies(scene)
+    RF_CK(cudaMemcpyAsync(d_part_[pcur_] + 2ull * d.body_off, src, 32ull * n, kind, stream_));
+  launch_iota(stream_, d_ids_[pcur_] + d.body_off, pad_tiles(n) * kTile);
+  RF_CK(cudaGetLastError());
+  launches_ += 1;
+  const int st = commit_scene(scene);
+  if (st != RFMM_OK) return st;
+  uploaded_[scene] = true;
+  committed_ = true;
+  return rebuild_lists();
+}
+
+int Engine::retire(uint32_t scene) {
+  if (scene >= scenes_.size() || scenes_[scene].n == 0u) return RFMM_ERR_INVALID;
+  const SceneDesc &d = scenes_[scene];
+  LaunchCtx L = ctx(mcur_, lpar_, pcur_);
+  launch_unpermute(L, d_ids_[pcur_], d_part_[pcur_ ^ 1u], d.tile_off, pad_tiles(d.n));
+  RF_CK(cudaGetLastError());
+  launches_ += 1;
+  return deactivate(scene);
+}
+
+int Engine::deactivate(uint32_t scene) {
+  if (scene >= scenes_.size()) return RFMM_ERR_INVALID;
+  SceneDesc &d = scenes_[scene];
+  d.n = 0u;
+  RF_CK(cudaMemcpyAsync(d_scenes_ + scene, &d, sizeof(SceneDesc), cudaMemcpyHostToDevice, stream_));
+  return rebuild_lists();
 }
 
 int Engine::commit() {
   for (bool u : uploaded_)
     if (!u) return RFMM_ERR_STATE;
   LaunchCtx L = ctx(mcur_, lpar_, pcur_);
-  launch_keys(L, sort_.keys[0], sort_.vals[0], nullptr, 0, tiles_);
+  launch_keys(L, sort_.keys[0], sort_.vals[0], nullptr, 0, tiles_, 0u);
   const int r = radix_sort(stream_, sort_, slots_, key_bits_);
   RF_CK(cudaMemsetAsync(d_mom_[mcur_], 0, 16ull * cells_, stream_));
   launch_gather(L, sort_.vals[r], d_part_[pcur_], d_ids_[pcur_], d_part_[pcur_ ^ 1u],
-                d_ids_[pcur_ ^ 1u], d_mom_[mcur_], tiles_);
+                d_ids_[pcur_ ^ 1u], d_mom_[mcur_], tiles_, 0u);
   RF_CK(cudaGetLastError());
   launches_ += resort_kernels();
   pcur_ ^= 1u;

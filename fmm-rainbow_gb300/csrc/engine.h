@@ -25,8 +25,9 @@ namespace rfmm {
 enum KernelKind { kKUpward = 0, kKM2L, kKL2LNear, kKIntegrate, kKResort, kKernelKinds };
 
 struct SceneSpec {
-  uint32_t n;
-  rfmm_params params;
+  uint32_t n;          // bodies (or, for a slot, the capacity)
+  rfmm_params params;  // for a slot: params.depth = deepest tree it must hold (0 = planner)
+  bool slot = false;   // reserve buffers but start empty (serving slots)
 };
 
 class Engine {
@@ -49,6 +50,21 @@ class Engine {
 
   int solve_fields();
   int step(uint32_t steps);
+
+  // Serving slots: put `n` bodies with `params` into an empty slot (sorted
+  // and deposited on the spot, other scenes untouched) or empty it again.
+  int activate(uint32_t scene, uint32_t n, const rfmm_params &params, const void *src,
+               cudaMemcpyKind kind);
+  int deactivate(uint32_t scene);
+  // Bodies of a finished slot back to the caller's order in the scratch
+  // range (slot_scratch), then the slot is emptied.
+  int retire(uint32_t scene);
+  float4 *slot_bodies(uint32_t scene) const { return d_part_[pcur_] + 2ull * scenes_[scene].body_off; }
+  float4 *slot_scratch(uint32_t scene) const {
+    return d_part_[pcur_ ^ 1u] + 2ull * scenes_[scene].body_off;
+  }
+  uint32_t capacity(uint32_t scene) const { return scenes_[scene].tile_cap * kTile; }
+  bool active(uint32_t scene) const { return scenes_[scene].n != 0u; }
   int sync();
 
   int download(uint32_t scene, int which, void *dst, size_t bytes, cudaMemcpyKind kind);
@@ -75,11 +91,15 @@ class Engine {
   void enqueue_step(uint32_t mpar, uint32_t lpar, uint32_t ppar);
   void enqueue_resort(uint32_t ppar);
   int launch_chunk(uint32_t len, bool sort_at_end);
+  int commit_scene(uint32_t scene);
+  int rebuild_lists();
   int check_device_error();
 
   int device_ = 0;
   int sms_ = 0;
   uint32_t body_ctas_ = 0;
+  uint32_t tree_ctas_ = 0;
+  bool use_lists_ = false;  // serving: kernels walk the active tile/task lists
   cudaStream_t stream_ = nullptr;
   cudaStream_t own_stream_ = nullptr;
 
@@ -96,6 +116,8 @@ class Engine {
   uint4 *d_mom_scratch_ = nullptr;
   float4 *d_src_ = nullptr;
   float4 *d_aux_ = nullptr;
+  uint32_t *d_tile_list_ = nullptr, *d_task_list_ = nullptr;
+  std::vector<uint32_t> tile_list_h_, task_list_h_;
   uint32_t *d_choice_ = nullptr;
   float *d_lfield_ = nullptr, *d_fields_ = nullptr;
   WorkItem *d_plist_[2] = {nullptr, nullptr};

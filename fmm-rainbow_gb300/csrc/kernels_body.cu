@@ -203,26 +203,32 @@ __global__ void __launch_bounds__(256) k_integrate(const SceneDesc *__restrict__
                                                    const float4 *__restrict__ aux,
                                                    const uint32_t *__restrict__ choice,
                                                    const float *__restrict__ fields,
-                                                   uint4 *__restrict__ mom_next, uint32_t tiles) {
+                                                   uint4 *__restrict__ mom_next, uint32_t tiles,
+                                                   const uint32_t *__restrict__ tile_list,
+                                                   const Counters *__restrict__ ctr) {
   __shared__ DepositTable T;
   __shared__ SceneDesc S;
-  uint32_t t0, t1;
-  cta_tile_range(tiles, t0, t1);
   T.clear();
   grid_dependency_wait();  // fields of this step are complete
+  const uint32_t ntiles = tile_list != nullptr ? min(ctr->tiles_active, tiles) : tiles;
+  uint32_t t0, t1;
+  cta_tile_range(ntiles, t0, t1);
   uint32_t cur = 0xFFFFFFFFu;
   // The next tile's bodies are loaded one iteration ahead.
   float4 n0 = make_float4(0.f, 0.f, 0.f, 0.f), n1 = n0;
+  uint32_t next_tile = t0 < t1 ? (tile_list != nullptr ? tile_list[t0] : t0) : 0u;
   if (t0 < t1) {
-    n0 = part[2u * (t0 * kTile + threadIdx.x)];
-    n1 = part[2u * (t0 * kTile + threadIdx.x) + 1u];
+    n0 = part[2u * (next_tile * kTile + threadIdx.x)];
+    n1 = part[2u * (next_tile * kTile + threadIdx.x) + 1u];
   }
-  for (uint32_t tile = t0; tile < t1; tile++) {
+  for (uint32_t i = t0; i < t1; i++) {
+    const uint32_t tile = next_tile;
     const uint32_t slot = tile * kTile + threadIdx.x;
     float4 p0 = n0, p1 = n1;
-    if (tile + 1u < t1) {
-      n0 = part[2u * (slot + kTile)];
-      n1 = part[2u * (slot + kTile) + 1u];
+    if (i + 1u < t1) {
+      next_tile = tile_list != nullptr ? tile_list[i + 1u] : i + 1u;
+      n0 = part[2u * (next_tile * kTile + threadIdx.x)];
+      n1 = part[2u * (next_tile * kTile + threadIdx.x) + 1u];
     }
     const uint32_t sc = tile_scene[tile];
     if (sc != cur) {
@@ -249,14 +255,18 @@ __global__ void __launch_bounds__(256) k_integrate(const SceneDesc *__restrict__
 __global__ void __launch_bounds__(256) k_deposit(const SceneDesc *__restrict__ scenes,
                                                  const uint32_t *__restrict__ tile_scene,
                                                  const float4 *__restrict__ part,
-                                                 uint4 *__restrict__ moments, uint32_t tiles) {
+                                                 uint4 *__restrict__ moments, uint32_t tiles,
+                                                 const uint32_t *__restrict__ tile_list,
+                                                 const Counters *__restrict__ ctr) {
   __shared__ DepositTable T;
   __shared__ SceneDesc S;
+  const uint32_t ntiles = tile_list != nullptr ? min(ctr->tiles_active, tiles) : tiles;
   uint32_t t0, t1;
-  cta_tile_range(tiles, t0, t1);
+  cta_tile_range(ntiles, t0, t1);
   T.clear();
   uint32_t cur = 0xFFFFFFFFu;
-  for (uint32_t tile = t0; tile < t1; tile++) {
+  for (uint32_t i = t0; i < t1; i++) {
+    const uint32_t tile = tile_list != nullptr ? tile_list[i] : i;
     const uint32_t slot = tile * kTile + threadIdx.x;
     const float4 p = part[2u * slot];
     const uint32_t sc = tile_scene[tile];
@@ -293,10 +303,12 @@ __global__ void __launch_bounds__(256) k_keys(const SceneDesc *__restrict__ scen
                                               const uint32_t *__restrict__ tile_scene,
                                               const float4 *__restrict__ part,
                                               uint32_t *__restrict__ keys, uint32_t *__restrict__ vals,
-                                              uint32_t *__restrict__ ids, int fresh_ids) {
-  const uint32_t tile = blockIdx.x;
+                                              uint32_t *__restrict__ ids, int fresh_ids,
+                                              uint32_t tile_base) {
+  const uint32_t tile = tile_base + blockIdx.x;
   const SceneDesc &S = scenes[tile_scene[tile]];
   const uint32_t slot = tile * kTile + threadIdx.x;
+  const uint32_t out = blockIdx.x * kTile + threadIdx.x;  // keys/vals are relative to tile_base
   const uint32_t local = slot - S.body_off;
   const uint32_t F = S.key_level;
   uint32_t key = S.key_base | ((1u << (3u * F)) - 1u);  // padding sorts after its scene's bodies
@@ -308,8 +320,8 @@ __global__ void __launch_bounds__(256) k_keys(const SceneDesc *__restrict__ scen
                         (spread3(cell_of_unit(unit_coord(p.y), dim)) << 1) |
                         (spread3(cell_of_unit(unit_coord(p.z), dim)) << 2));
   }
-  keys[slot] = key;
-  vals[slot] = slot;
+  keys[out] = key;
+  vals[out] = slot;
   if (fresh_ids) ids[slot] = local;
 }
 
@@ -323,20 +335,24 @@ __global__ void __launch_bounds__(256) k_gather(const SceneDesc *__restrict__ sc
                                                 const uint32_t *__restrict__ ids_in,
                                                 float4 *__restrict__ part_out,
                                                 uint32_t *__restrict__ ids_out,
-                                                uint4 *__restrict__ deposit_into, uint32_t tiles) {
+                                                uint4 *__restrict__ deposit_into, uint32_t tiles,
+                                                uint32_t tile_base) {
   __shared__ DepositTable T;
   __shared__ SceneDesc S;
-  const uint32_t nslots = tiles * kTile;
+  // Slots [tile_base * 256, (tile_base + tiles) * 256) are permuted among
+  // themselves; perm is relative to tile_base and holds absolute slots.
+  const uint32_t lo = tile_base * kTile, hi = (tile_base + tiles) * kTile;
   uint32_t t0 = blockIdx.x, t1 = blockIdx.x + 1u;
   if (deposit_into != nullptr) {
     cta_tile_range(tiles, t0, t1);
     T.clear();
   }
   uint32_t cur = 0xFFFFFFFFu;
-  for (uint32_t tile = t0; tile < t1; tile++) {
+  for (uint32_t i = t0; i < t1; i++) {
+    const uint32_t tile = tile_base + i;
     const uint32_t slot = tile * kTile + threadIdx.x;
-    uint32_t from = perm[slot];
-    if (from >= nslots) from = slot;  // defensive: a permutation never leaves the buffer
+    uint32_t from = perm[i * kTile + threadIdx.x];
+    if (from < lo || from >= hi) from = slot;  // defensive: a permutation never leaves the range
     const float4 p0 = part_in[2u * from], p1 = part_in[2u * from + 1u];
     part_out[2u * slot] = p0;
     part_out[2u * slot + 1u] = p1;
@@ -513,25 +529,26 @@ void launch_integrate(const LaunchCtx &L, uint32_t tiles) {
   launch_step_kernel(L, k_integrate, dim3(body_grid(L, tiles)), dim3(kTile), 0, L.scenes,
                      L.tile_scene, L.part, (const uint4 *)L.mom, (const float4 *)L.src,
                      (const float4 *)L.aux, (const uint32_t *)L.choice, (const float *)L.fields,
-                     L.mom_next, tiles);
+                     L.mom_next, tiles, L.tile_list, (const Counters *)L.ctr);
 }
 
 void launch_deposit(const LaunchCtx &L, uint4 *moments, uint32_t tiles) {
   k_deposit<<<body_grid(L, tiles), kTile, 0, L.stream>>>(L.scenes, L.tile_scene, L.part, moments,
-                                                         tiles);
+                                                         tiles, L.tile_list, L.ctr);
 }
 
 void launch_keys(const LaunchCtx &L, uint32_t *keys, uint32_t *vals, uint32_t *ids, int fresh_ids,
-                 uint32_t tiles) {
-  k_keys<<<tiles, kTile, 0, L.stream>>>(L.scenes, L.tile_scene, L.part, keys, vals, ids, fresh_ids);
+                 uint32_t tiles, uint32_t tile_base) {
+  k_keys<<<tiles, kTile, 0, L.stream>>>(L.scenes, L.tile_scene, L.part, keys, vals, ids, fresh_ids,
+                                        tile_base);
 }
 
 void launch_gather(const LaunchCtx &L, const uint32_t *perm, const float4 *part_in,
                    const uint32_t *ids_in, float4 *part_out, uint32_t *ids_out, uint4 *deposit_into,
-                   uint32_t tiles) {
+                   uint32_t tiles, uint32_t tile_base) {
   const uint32_t grid = deposit_into != nullptr ? body_grid(L, tiles) : tiles;
   k_gather<<<grid, kTile, 0, L.stream>>>(L.scenes, L.tile_scene, perm, part_in, ids_in, part_out,
-                                         ids_out, deposit_into, tiles);
+                                         ids_out, deposit_into, tiles, tile_base);
 }
 
 void launch_unpermute(const LaunchCtx &L, const uint32_t *ids, float4 *out, uint32_t tile_base,

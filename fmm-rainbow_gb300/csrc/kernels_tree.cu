@@ -47,53 +47,19 @@ __device__ __forceinline__ void store_cell(const SceneDesc &S, uint32_t local_ce
   aux[g] = make_aux(m.x, S.gravity, S.n_f);
 }
 
-__global__ void __launch_bounds__(256) k_upward(const SceneDesc *__restrict__ scenes,
-                                                const uint32_t *__restrict__ task_scene,
-                                                uint4 *__restrict__ mom, uint4 *__restrict__ mom_next,
-                                                float4 *__restrict__ src, float4 *__restrict__ aux,
-                                                uint32_t *__restrict__ choice,
-                                                float *__restrict__ fields,
-                                                WorkItem *__restrict__ plist, uint32_t plist_cap,
-                                                const WorkItem *__restrict__ plist_prev,
-                                                Counters *__restrict__ ctr, uint32_t list_par,
-                                                uint32_t *__restrict__ tickets) {
-  __shared__ uint4 s0[512];
-  __shared__ uint4 s1[64];
-  __shared__ uint4 s2[8];
-  __shared__ WorkItem s_items[80];
-  __shared__ uint32_t s_nitems, s_base, s_last, s_root;
-
+// Body of one upward task: the 8x8x8-leaf subtree `sub` of scene `scene`.
+__device__ __forceinline__ void upward_task(
+    const SceneDesc &S, uint32_t scene, uint32_t sub, uint4 *__restrict__ mom,
+    uint4 *__restrict__ mom_next, float4 *__restrict__ src, float4 *__restrict__ aux,
+    uint32_t *__restrict__ choice, WorkItem *__restrict__ plist, uint32_t plist_cap,
+    Counters *__restrict__ ctr, uint32_t list_par, uint32_t *__restrict__ tickets, uint4 *s0,
+    uint4 *s1, uint4 *s2, WorkItem *s_items, uint32_t &s_nitems, uint32_t &s_base,
+    uint32_t &s_last, uint32_t &s_root) {
   const uint32_t tid = threadIdx.x;
-  const uint32_t scene = task_scene[blockIdx.x];
-  const SceneDesc S = scenes[scene];
   const uint32_t D = S.depth, r = S.sub_level;
-  const uint32_t sub = blockIdx.x - S.task_off;
   const uint32_t rdim = 1u << r;
   const uint32_t sx = sub % rdim, sy = (sub / rdim) % rdim, sz = sub / (rdim * rdim);
   if (tid == 0) s_nitems = 0;
-  grid_dependency_wait();  // the previous integrate deposited and read the fields
-
-  // Clear the fields of the previous step's targets (children of listed parents).
-  {
-    const uint32_t prev_n = min(ctr->parents[list_par ^ 1u], plist_cap);
-    const uint32_t wpb = blockDim.x >> 5;
-    const uint32_t warp = blockIdx.x * wpb + (tid >> 5), lane = tid & 31u;
-    for (uint32_t i = warp; i < prev_n; i += gridDim.x * wpb) {
-      const WorkItem w = plist_prev[i];
-      const SceneDesc &P = scenes[w.scene];
-      const uint32_t lp = w.cell == 0u ? 0u : level_of_d(w.cell);
-      const uint32_t pdim = 1u << lp, dim = pdim << 1;
-      const uint32_t pl = w.cell - level_offset_d(lp);
-      const uint32_t px = pl % pdim, py = (pl / pdim) % pdim, pz = pl / (pdim * pdim);
-      for (uint32_t e = lane; e < 96u; e += 32u) {
-        const uint32_t ch = e / 12u, comp = e % 12u;
-        const uint32_t c = P.cell_off + level_offset_d(lp + 1u) +
-                           lin3(2u * px + (ch & 1u), 2u * py + ((ch >> 1) & 1u),
-                                2u * pz + (ch >> 2), dim);
-        fields[(size_t)c * 12u + comp] = 0.0f;
-      }
-    }
-  }
 
   // Leaves of this subtree: 8x8x8 block, x fastest (rows of 128 B); two per thread.
 #pragma unroll
@@ -189,8 +155,8 @@ __global__ void __launch_bounds__(256) k_upward(const SceneDesc *__restrict__ sc
   __syncthreads();
   for (uint32_t i = tid; i < s_nitems; i += blockDim.x) plist[s_base + i] = s_items[i];
 
-  // The last subtree CTA of the scene reduces levels r-1 .. 0.  Only thread 0
-  // wrote the level-r cell the last CTA reads, so only it fences.
+  // The scene's last finished subtree reduces levels r-1 .. 0.  Only thread 0
+  // wrote the level-r cell that reduction reads, so only it fences.
   __syncthreads();
   if (tid == 0) {
     __threadfence();
@@ -200,40 +166,99 @@ __global__ void __launch_bounds__(256) k_upward(const SceneDesc *__restrict__ sc
     if (s_last) tickets[scene] = 0u;
   }
   __syncthreads();
-  if (!s_last) return;
-  __threadfence();
-  if (tid == 0) s_nitems = 0;
-  // Level r has at most 512 cells: stage it (written by other CTAs) via L2.
-  const uint32_t nr = 1u << (3u * r);
-  for (uint32_t i = tid; i < nr; i += blockDim.x) s0[i] = __ldcg(&mom[S.cell_off + level_offset_d(r) + i]);
-  __syncthreads();
-  for (int l = (int)r - 1; l >= 0; l--) {
-    const uint32_t dim = 1u << l, cdim = dim << 1, nl = 1u << (3u * l);
-    uint4 acc = make_uint4(0u, 0u, 0u, 0u);
-    if (tid < nl) {
-      const uint32_t x = tid % dim, y = (tid / dim) % dim, z = tid / (dim * dim);
-      for (uint32_t dz = 0; dz < 2u; dz++)
-        for (uint32_t dy = 0; dy < 2u; dy++)
-          for (uint32_t dx = 0; dx < 2u; dx++)
-            acc = add_moment(acc, s0[lin3(2u * x + dx, 2u * y + dy, 2u * z + dz, cdim)]);
-      const uint32_t cell = level_offset_d((uint32_t)l) + tid;
-      store_cell(S, cell, acc, mom, src, aux);
-      if ((int32_t)acc.x > (int32_t)kAdaptive) s_items[atomicAdd(&s_nitems, 1u)] = {scene, cell};
+  if (s_last) {
+    __threadfence();
+    if (tid == 0) s_nitems = 0;
+    // Level r has at most 512 cells: stage it (written by other CTAs) via L2.
+    const uint32_t nr = 1u << (3u * r);
+    for (uint32_t i = tid; i < nr; i += blockDim.x)
+      s0[i] = __ldcg(&mom[S.cell_off + level_offset_d(r) + i]);
+    __syncthreads();
+    for (int l = (int)r - 1; l >= 0; l--) {
+      const uint32_t dim = 1u << l, cdim = dim << 1, nl = 1u << (3u * l);
+      uint4 acc = make_uint4(0u, 0u, 0u, 0u);
+      if (tid < nl) {
+        const uint32_t x = tid % dim, y = (tid / dim) % dim, z = tid / (dim * dim);
+        for (uint32_t dz = 0; dz < 2u; dz++)
+          for (uint32_t dy = 0; dy < 2u; dy++)
+            for (uint32_t dx = 0; dx < 2u; dx++)
+              acc = add_moment(acc, s0[lin3(2u * x + dx, 2u * y + dy, 2u * z + dz, cdim)]);
+        const uint32_t cell = level_offset_d((uint32_t)l) + tid;
+        store_cell(S, cell, acc, mom, src, aux);
+        if ((int32_t)acc.x > (int32_t)kAdaptive) s_items[atomicAdd(&s_nitems, 1u)] = {scene, cell};
+      }
+      __syncthreads();
+      if (tid < nl) s0[tid] = acc;
+      __syncthreads();
+    }
+    if (tid == 0) {
+      uint32_t base = atomicAdd(&ctr->parents[list_par], s_nitems);
+      if (base + s_nitems > plist_cap) {
+        atomicCAS(&ctr->error, 0u, (uint32_t)kDevErrListOverflow);
+        s_nitems = base < plist_cap ? plist_cap - base : 0u;
+      }
+      s_base = base;
     }
     __syncthreads();
-    if (tid < nl) s0[tid] = acc;
-    __syncthreads();
-  }
-  if (tid == 0) {
-    uint32_t base = atomicAdd(&ctr->parents[list_par], s_nitems);
-    if (base + s_nitems > plist_cap) {
-      atomicCAS(&ctr->error, 0u, (uint32_t)kDevErrListOverflow);
-      s_nitems = base < plist_cap ? plist_cap - base : 0u;
-    }
-    s_base = base;
+    for (uint32_t i = tid; i < s_nitems; i += blockDim.x) plist[s_base + i] = s_items[i];
   }
   __syncthreads();
-  for (uint32_t i = tid; i < s_nitems; i += blockDim.x) plist[s_base + i] = s_items[i];
+}
+
+// Persistent upward pass over the active subtree tasks (task_list, or every
+// task when null).
+__global__ void __launch_bounds__(256) k_upward(const SceneDesc *__restrict__ scenes,
+                                                const uint32_t *__restrict__ task_scene,
+                                                const uint32_t *__restrict__ task_list,
+                                                uint32_t ntasks_all,
+                                                uint4 *__restrict__ mom, uint4 *__restrict__ mom_next,
+                                                float4 *__restrict__ src, float4 *__restrict__ aux,
+                                                uint32_t *__restrict__ choice,
+                                                float *__restrict__ fields,
+                                                WorkItem *__restrict__ plist, uint32_t plist_cap,
+                                                const WorkItem *__restrict__ plist_prev,
+                                                Counters *__restrict__ ctr, uint32_t list_par,
+                                                uint32_t *__restrict__ tickets) {
+  __shared__ uint4 s0[512];
+  __shared__ uint4 s1[64];
+  __shared__ uint4 s2[8];
+  __shared__ WorkItem s_items[80];
+  __shared__ uint32_t s_nitems, s_base, s_last, s_root;
+  __shared__ SceneDesc sS;
+  const uint32_t tid = threadIdx.x;
+  grid_dependency_wait();  // the previous integrate deposited and read the fields
+
+  // Clear the fields of the previous step's targets (children of listed parents).
+  {
+    const uint32_t prev_n = min(ctr->parents[list_par ^ 1u], plist_cap);
+    const uint32_t wpb = blockDim.x >> 5;
+    const uint32_t warp = blockIdx.x * wpb + (tid >> 5), lane = tid & 31u;
+    for (uint32_t i = warp; i < prev_n; i += gridDim.x * wpb) {
+      const WorkItem w = plist_prev[i];
+      const SceneDesc &P = scenes[w.scene];
+      const uint32_t lp = w.cell == 0u ? 0u : level_of_d(w.cell);
+      const uint32_t pdim = 1u << lp, dim = pdim << 1;
+      const uint32_t pl = w.cell - level_offset_d(lp);
+      const uint32_t px = pl % pdim, py = (pl / pdim) % pdim, pz = pl / (pdim * pdim);
+      for (uint32_t e = lane; e < 96u; e += 32u) {
+        const uint32_t ch = e / 12u, comp = e % 12u;
+        const uint32_t c = P.cell_off + level_offset_d(lp + 1u) +
+                           lin3(2u * px + (ch & 1u), 2u * py + ((ch >> 1) & 1u),
+                                2u * pz + (ch >> 2), dim);
+        fields[(size_t)c * 12u + comp] = 0.0f;
+      }
+    }
+  }
+
+  const uint32_t ntasks = task_list != nullptr ? min(ctr->tasks_active, ntasks_all) : ntasks_all;
+  for (uint32_t it = blockIdx.x; it < ntasks; it += gridDim.x) {
+    const uint32_t task = task_list != nullptr ? task_list[it] : it;
+    const uint32_t scene = task_scene[task];
+    load_scene(sS, scenes, scene);
+    upward_task(sS, scene, task - sS.task_off, mom, mom_next, src, aux, choice, plist, plist_cap,
+                ctr, list_par, tickets, s0, s1, s2, s_items, s_nitems, s_base, s_last, s_root);
+  }
+  grid_dependents_may_launch();
 }
 
 // -------------------------------------------------------------------- M2L
@@ -506,9 +531,10 @@ __global__ void __launch_bounds__(256) k_l2l_near(const SceneDesc *__restrict__ 
 // --------------------------------------------------------------- launches
 
 void launch_upward(const LaunchCtx &L, uint32_t list_par, uint32_t tasks) {
-  launch_step_kernel(L, k_upward, dim3(tasks), dim3(256), 0, L.scenes, L.task_scene, L.mom,
-                     L.mom_next, L.src, L.aux, L.choice, L.fields, L.plist, L.plist_cap, L.plist_prev,
-                     L.ctr, list_par, L.tickets);
+  const uint32_t grid = tasks < L.tree_ctas ? tasks : L.tree_ctas;
+  launch_step_kernel(L, k_upward, dim3(grid), dim3(256), 0, L.scenes, L.task_scene, L.task_list,
+                     tasks, L.mom, L.mom_next, L.src, L.aux, L.choice, L.fields, L.plist,
+                     L.plist_cap, L.plist_prev, L.ctr, list_par, L.tickets);
 }
 
 size_t m2l_smem_bytes() { return sizeof(M2LShared) + 128; }

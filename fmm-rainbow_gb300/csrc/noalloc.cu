@@ -184,6 +184,8 @@ extern "C" int rfmm_solve_fields_noalloc(const void *device_particles, uint32_t 
     d.control_axis_mode[k] = p.control_axis_mode[k];
   }
   d.key_level = 10u;
+  d.max_depth = depth;
+  d.tile_cap = (n + kTile - 1u) / kTile;
   const uint32_t tiles = (n + kTile - 1u) / kTile;
   const uint32_t tasks = 1u << (3u * d.sub_level);
 
@@ -218,6 +220,9 @@ extern "C" int rfmm_solve_fields_noalloc(const void *device_particles, uint32_t 
   L.tickets = S->tickets;
   L.tmaps = S->tmaps;
   L.body_ctas = st.body_ctas;
+  L.tree_ctas = (uint32_t)st.sms * 6u;
+  L.tile_list = nullptr;
+  L.task_list = nullptr;
   L.pdl = false;
 
   launch_deposit(L, L.mom, tiles);

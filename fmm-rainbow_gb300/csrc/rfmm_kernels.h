@@ -32,6 +32,9 @@ struct LaunchCtx {
   uint32_t *tickets;
   const CUtensorMap *tmaps;    // 8 per scene (levels 0..7; 3..6 used)
   uint32_t body_ctas;          // persistent grid of the body passes (resident CTAs)
+  uint32_t tree_ctas;          // persistent grid of the upward pass
+  const uint32_t *tile_list;   // active body tiles (null: every tile)
+  const uint32_t *task_list;   // active upward tasks (null: every task)
   bool pdl;                    // launch step kernels with programmatic stream serialization
 };
 
@@ -72,11 +75,13 @@ cudaError_t configure_tree_kernels();
 // Body passes (kernels_body.cu).
 void launch_integrate(const LaunchCtx &L, uint32_t tiles);
 void launch_deposit(const LaunchCtx &L, uint4 *moments, uint32_t tiles);
+// keys/vals of tiles [tile_base, tile_base + tiles), written from index 0.
 void launch_keys(const LaunchCtx &L, uint32_t *keys, uint32_t *vals, uint32_t *ids, int fresh_ids,
-                 uint32_t tiles);
+                 uint32_t tiles, uint32_t tile_base);
+// Permute the bodies of tiles [tile_base, tile_base + tiles) (perm from index 0).
 void launch_gather(const LaunchCtx &L, const uint32_t *perm, const float4 *part_in,
                    const uint32_t *ids_in, float4 *part_out, uint32_t *ids_out, uint4 *deposit_into,
-                   uint32_t tiles);
+                   uint32_t tiles, uint32_t tile_base);
 void launch_unpermute(const LaunchCtx &L, const uint32_t *ids, float4 *out, uint32_t tile_base,
                       uint32_t tiles);
 void launch_initialize(const LaunchCtx &L, float4 *part_out, uint32_t tile_base, uint32_t tiles);

@@ -30,7 +30,9 @@ struct alignas(16) SceneDesc {
   float control_point[4];      // wgsl:45
   float control_axis_mode[4];  // wgsl:47
   uint32_t key_level;  // level of the fine Morton cells the resident order sorts by (>= depth)
-  uint32_t pad_[3];
+  uint32_t max_depth;  // deepest tree this scene's buffers hold (serving slots)
+  uint32_t tile_cap;   // body tiles reserved for this scene
+  uint32_t pad_;
 };
 static_assert(sizeof(SceneDesc) == 112, "SceneDesc layout");
 
@@ -39,7 +41,9 @@ struct Counters {
   uint32_t parents[2];   // length of the parent work list, per step parity
   uint32_t error;        // first error code raised by a kernel (0 = none)
   uint32_t error_info;   // kernel-specific detail for `error`
-  uint32_t pad[4];
+  uint32_t tiles_active; // entries of the active body-tile list (when one is used)
+  uint32_t tasks_active; // entries of the active upward-task list (when one is used)
+  uint32_t pad[2];
 };
 
 enum DeviceError : uint32_t {

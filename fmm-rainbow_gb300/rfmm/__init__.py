@@ -53,6 +53,19 @@ class Params(C.Structure):
     ]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("memory_budget_bytes", C.c_uint64), ("max_bodies", C.c_uint32),
+                ("max_slots", C.c_uint32), ("max_chunk_steps", C.c_uint32)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("queued", C.c_uint64),
+                ("in_flight", C.c_uint64), ("slots", C.c_uint32), ("slot_capacity", C.c_uint32),
+                ("device_bytes", C.c_uint64), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
+                ("mean_ms", C.c_double), ("max_ms", C.c_double),
+                ("body_steps_per_s", C.c_double), ("body_steps", C.c_double)]
+
+
 class Plan(C.Structure):
     _fields_ = [("particles", C.c_uint32), ("depth", C.c_uint32), ("cells", C.c_uint32),
                 ("fixed_point_scale", C.c_float)]
@@ -118,6 +131,13 @@ SIGNATURES = {
     "rfmm_batch_launch_count": (_i, [_vp, C.POINTER(C.c_uint64)]),
     "rfmm_batch_profile_steps": (_i, [_vp, _u32, C.POINTER(_f32), C.POINTER(_u32)]),
     "rfmm_batch_set_resort_interval": (_i, [_vp, _u32]),
+    "rfmm_server_create": (_i, [C.POINTER(ServerConfig), C.POINTER(_vp)]),
+    "rfmm_server_destroy": (_i, [_vp]),
+    "rfmm_server_submit": (_i, [_vp, _vp, _u32, _P, _u32, C.POINTER(C.c_uint64)]),
+    "rfmm_server_status": (_i, [_vp, C.c_uint64, C.POINTER(_i)]),
+    "rfmm_server_wait": (_i, [_vp, C.c_uint64, _u32]),
+    "rfmm_server_result": (_i, [_vp, C.c_uint64, _vp, _sz]),
+    "rfmm_server_get_stats": (_i, [_vp, C.POINTER(ServerStats)]),
 }
 KERNEL_KINDS = ("upward", "m2l", "l2l_near", "integrate", "resort")
 
@@ -400,3 +420,59 @@ class Batch:
         cnt = (C.c_uint32 * len(KERNEL_KINDS))()
         _check(lib().rfmm_batch_profile_steps(self._h, steps, ms, cnt), "rfmm_batch_profile_steps")
         return {k: (ms[i], cnt[i]) for i, k in enumerate(KERNEL_KINDS)}
+
+
+class Server:
+    """Continuous-batching solve server (the `rfmm_server_*` handle)."""
+
+    def __init__(self, max_bodies, memory_budget_bytes=8 << 30, max_slots=0, max_chunk_steps=0):
+        cfg = ServerConfig(memory_budget_bytes, max_bodies, max_slots, max_chunk_steps)
+        self._h = C.c_void_p()
+        _check(lib().rfmm_server_create(C.byref(cfg), C.byref(self._h)), "rfmm_server_create")
+        self._n = {}
+
+    def close(self):
+        if self._h:
+            lib().rfmm_server_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def submit(self, particles, steps, params=None):
+        a = np.ascontiguousarray(particles)
+        assert a.dtype == PARTICLE_DTYPE
+        rid = C.c_uint64()
+        _check(lib().rfmm_server_submit(self._h, a.ctypes.data, len(a),
+                                        C.byref(params) if params is not None else None, steps,
+                                        C.byref(rid)), "rfmm_server_submit")
+        self._n[rid.value] = len(a)
+        return rid.value
+
+    def status(self, rid):
+        st = C.c_int()
+        _check(lib().rfmm_server_status(self._h, rid, C.byref(st)), "rfmm_server_status")
+        return st.value
+
+    def wait(self, rid, timeout_ms=60000):
+        _check(lib().rfmm_server_wait(self._h, rid, timeout_ms), "rfmm_server_wait")
+
+    def result(self, rid):
+        out = np.empty(self._n.pop(rid), PARTICLE_DTYPE)
+        _check(lib().rfmm_server_result(self._h, rid, out.ctypes.data, out.nbytes),
+               "rfmm_server_result")
+        return out
+
+    def stats(self):
+        st = ServerStats()
+        _check(lib().rfmm_server_get_stats(self._h, C.byref(st)), "rfmm_server_get_stats")
+        return {k: getattr(st, k) for k, _ in ServerStats._fields_}

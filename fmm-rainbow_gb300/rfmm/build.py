@@ -37,6 +37,7 @@ SOURCES = [
     "engine.cpp",
     "capi.cpp",
     "capi_batch.cpp",
+    "server.cpp",
     "planner.cpp",
 ]
 # Text embedded as the "shader" payload of rainbow_shader_ptr().

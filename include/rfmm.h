@@ -207,6 +207,48 @@ int rfmm_batch_launch_count(rfmm_batch *b, uint64_t *out);
 int rfmm_batch_profile_steps(rfmm_batch *b, uint32_t steps, float *kernel_ms, uint32_t *launches);
 int rfmm_batch_set_resort_interval(rfmm_batch *b, uint32_t steps);
 
+/* ------------------------------------------------------------------ serving
+ *
+ * Continuous batching of solve requests (scene + parameters + step count).
+ * The server preallocates slots of `max_bodies` capacity within the device
+ * memory budget; a request waits until a slot is free, is admitted at the
+ * next step boundary while other requests keep running, and every step
+ * advances all occupied slots in the same launches.  Results are
+ * bit-identical to a plain solve of the same scene.  Submit, status, wait and
+ * result may be called from any thread. */
+typedef struct rfmm_server rfmm_server;
+
+typedef struct rfmm_server_config {
+  uint64_t memory_budget_bytes; /* device memory the slots may use */
+  uint32_t max_bodies;          /* slot capacity = largest admissible request */
+  uint32_t max_slots;           /* 0 = as many as the budget allows (<= 4096) */
+  uint32_t max_chunk_steps;     /* steps between admission points (0 = 4) */
+} rfmm_server_config;
+
+typedef struct rfmm_server_stats {
+  uint64_t submitted, completed, queued, in_flight;
+  uint32_t slots, slot_capacity;
+  uint64_t device_bytes;
+  double p50_ms, p99_ms, mean_ms, max_ms; /* submit -> result on host */
+  double body_steps_per_s;                /* completed work / (last done - first submit) */
+  double body_steps;
+} rfmm_server_stats;
+
+enum rfmm_request_state { RFMM_REQ_QUEUED = 0, RFMM_REQ_RUNNING = 1, RFMM_REQ_DONE = 2, RFMM_REQ_FAILED = 3 };
+
+int rfmm_server_create(const rfmm_server_config *config, rfmm_server **out);
+int rfmm_server_destroy(rfmm_server *server);
+/* Copies the n bodies (n x 32 B); returns RFMM_ERR_BUDGET if n exceeds the
+ * slot capacity. */
+int rfmm_server_submit(rfmm_server *server, const void *host_aos, uint32_t n,
+                       const rfmm_params *params, uint32_t steps, uint64_t *request_id);
+int rfmm_server_status(rfmm_server *server, uint64_t request_id, int *state);
+/* RFMM_ERR_TIMEOUT if the request is not done within timeout_ms. */
+int rfmm_server_wait(rfmm_server *server, uint64_t request_id, uint32_t timeout_ms);
+/* Copies the final bodies (caller's order, n x 32 B) and forgets the request. */
+int rfmm_server_result(rfmm_server *server, uint64_t request_id, void *host_dst, size_t bytes);
+int rfmm_server_get_stats(rfmm_server *server, rfmm_server_stats *out);
+
 /* Allocation-free field solve (this entry point has no counterpart in the
  * reference).  For callers that cannot allocate device memory -- a plugin
  * whose device memory is owned by the host framework, or code running where

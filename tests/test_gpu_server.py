@@ -1,0 +1,69 @@
+"""Served form: requests admitted while others run, each result bit-identical
+to the same scene solved alone through a plain handle."""
+import threading
+import time
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _bits(a):
+    return np.ascontiguousarray(a).view(np.uint32)
+
+
+def _requests():
+    from rfmm import scenes
+    rng = np.random.default_rng(31)
+    out = []
+    for i in range(24):
+        n = int(np.exp(rng.uniform(np.log(17), np.log(120000))))
+        kind = ["uniform", "plummer", "clusters4"][i % 3]
+        steps = int(rng.integers(1, 13))
+        out.append((scenes.make(kind, n, 500 + i), steps, 0.5 + 0.1 * (i % 5)))
+    return out
+
+
+def test_served_results_match_plain_alone(rfmm_mod):
+    R = rfmm_mod
+    reqs = _requests()
+    results = {}
+    with R.Server(max_bodies=131072, memory_budget_bytes=2 << 30, max_slots=6,
+                  max_chunk_steps=3) as srv:
+        ids = []
+
+        def client(chunk):
+            for p, steps, g in chunk:
+                ids.append((srv.submit(p, steps, R.default_params(gravity=g, softening=1e-3,
+                                                                  dt=5e-4)), p, steps, g))
+                time.sleep(0.002)  # arrivals while earlier requests are on the GPU
+
+        threads = [threading.Thread(target=client, args=(reqs[k::3],)) for k in range(3)]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+        for rid, p, steps, g in ids:
+            srv.wait(rid, 120000)
+            results[rid] = (srv.result(rid), p, steps, g)
+        st = srv.stats()
+        assert st["completed"] == len(reqs) and st["slots"] == 6
+        assert st["p99_ms"] >= st["p50_ms"] > 0
+    for rid, (got, p, steps, g) in results.items():
+        with R.Solver(len(p), R.default_params(gravity=g, softening=1e-3, dt=5e-4)) as s:
+            s.upload(p)
+            s.step(steps)
+            ref = s.particles()
+        assert np.array_equal(_bits(got), _bits(ref)), (rid, len(p), steps)
+
+
+def test_server_rejects_oversize_request(rfmm_mod):
+    R = rfmm_mod
+    from rfmm import scenes
+    with R.Server(max_bodies=4096, memory_budget_bytes=1 << 28, max_slots=2) as srv:
+        with pytest.raises(R.RFMMError):
+            srv.submit(scenes.uniform(5000, seed=1), 2)
+        rid = srv.submit(scenes.uniform(4096, seed=1), 2)
+        srv.wait(rid)
+        assert srv.result(rid).shape == (4096,)
