@@ -83,6 +83,7 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=8)
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--requests", type=int, default=0, help="served: requests per rate point")
     ap.add_argument("--rates", type=float, nargs="*", default=None, help="served: arrival rates /s")
     return ap.parse_args()
@@ -271,6 +272,10 @@ def run_gpu(args, w):
         solver.upload_device(pristine.data_ptr(), pristine.numel())
         solver.step(fmm_steps)
 
+    tuning = solver.tuning()
+    if not args.no_autotune:  # project autotuner: launch shapes timed on this scene
+        solver.upload_device(pristine.data_ptr(), pristine.numel())
+        tuning = solver.autotune(20)
     for _ in range(args.warmup):
         bench_step()
     torch.cuda.synchronize()
@@ -333,6 +338,15 @@ def run_gpu(args, w):
                "h2d_bytes_per_step": n * 32, "d2h_bytes_per_step": n * 32,
                "ms_per_step": 1e3 * e2e_s, "timer": "host wall clock"}
 
+    # Accuracy of the state the bench ends on (outside every timed region):
+    # FP64 direct-sum force error on a seeded target sample, FP64 energy.
+    rms, mx = solver.force_error(4096, 1)
+    diag = solver.diagnostics()
+    accuracy = {"force_rms_rel": rms, "force_max_rel": mx, "targets": min(4096, n),
+                "reference": "FP64 softened direct sum on the GPU (all N sources)",
+                "energy_total": diag["total"], "kinetic": diag["kinetic"],
+                "potential": diag["potential"]}
+
     line = {
         "metric": "body-steps/s", "value": value, "unit": "body-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
@@ -344,7 +358,7 @@ def run_gpu(args, w):
                    "l2": "flushed between timed steps (512 MiB write outside the events)",
                    "parallelism": "replicas x%d" % world},
         "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
-        "kernel_avg_ms": kernel_ms,
+        "kernel_avg_ms": kernel_ms, "tuning": tuning.as_dict(), "accuracy": accuracy,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds)
@@ -402,6 +416,10 @@ def run_gpu_batched(args, w):
         torch.cuda.synchronize()
         return sum(a.elapsed_time(b) for a, b in zip(st, en))
 
+    batched_step()
+    tuning = batch.tuning()
+    if not args.no_autotune:
+        tuning = batch.autotune(5)
     for _ in range(args.warmup):
         batched_step()
     torch.cuda.synchronize()
@@ -483,7 +501,7 @@ def run_gpu_batched(args, w):
                    "l2": "flushed between timed steps (512 MiB write outside the events)",
                    "parallelism": "scenes sharded over %d rank(s)" % world},
         "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
-        "kernel_avg_ms": kernel_ms,
+        "kernel_avg_ms": kernel_ms, "tuning": tuning.as_dict(),
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

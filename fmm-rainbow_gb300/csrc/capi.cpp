@@ -192,4 +192,45 @@ int rfmm_launch_count(rfmm_handle *h, uint64_t *out) {
   return RFMM_OK;
 }
 
+int rfmm_accelerations(rfmm_handle *h, float *host_out, size_t bytes) {
+  if (guard(h) || bytes != 16ull * h->engine->scene(0).n) return RFMM_ERR_INVALID;
+  return h->engine->accelerations(0, host_out);
+}
+
+int rfmm_force_error(rfmm_handle *h, uint32_t targets, uint64_t seed, double *rms_rel,
+                     double *max_rel) {
+  if (guard(h)) return RFMM_ERR_INVALID;
+  return h->engine->force_error(0, targets, seed, rms_rel, max_rel);
+}
+
+int rfmm_get_diagnostics(rfmm_handle *h, rfmm_diagnostics *out) {
+  if (guard(h) || out == nullptr) return RFMM_ERR_INVALID;
+  double v[9];
+  const int st = h->engine->diagnostics(0, v);
+  if (st != RFMM_OK) return st;
+  out->kinetic = v[0];
+  out->potential = v[1];
+  out->total = v[0] + v[1];
+  for (int k = 0; k < 3; k++) {
+    out->momentum[k] = v[2 + k];
+    out->angular_momentum[k] = v[5 + k];
+  }
+  return RFMM_OK;
+}
+
+int rfmm_get_tuning(rfmm_handle *h, rfmm_tuning *out) {
+  if (guard(h)) return RFMM_ERR_INVALID;
+  return h->engine->get_tuning(out);
+}
+
+int rfmm_set_tuning(rfmm_handle *h, const rfmm_tuning *tuning) {
+  if (guard(h) || tuning == nullptr) return RFMM_ERR_INVALID;
+  return h->engine->set_tuning(*tuning);
+}
+
+int rfmm_autotune(rfmm_handle *h, uint32_t steps_per_trial, rfmm_tuning *best) {
+  if (guard(h)) return RFMM_ERR_INVALID;
+  return h->engine->autotune(steps_per_trial, best);
+}
+
 }  // extern "C"

@@ -141,4 +141,25 @@ int rfmm_batch_set_resort_interval(rfmm_batch *b, uint32_t steps) {
   return b->engine->set_resort_interval(steps);
 }
 
+int rfmm_batch_force_error(rfmm_batch *b, uint32_t scene, uint32_t targets, uint64_t seed,
+                           double *rms_rel, double *max_rel) {
+  if (bad_scene(b, scene)) return RFMM_ERR_INVALID;
+  return b->engine->force_error(scene, targets, seed, rms_rel, max_rel);
+}
+
+int rfmm_batch_get_tuning(rfmm_batch *b, rfmm_tuning *out) {
+  if (bad(b)) return RFMM_ERR_INVALID;
+  return b->engine->get_tuning(out);
+}
+
+int rfmm_batch_set_tuning(rfmm_batch *b, const rfmm_tuning *tuning) {
+  if (bad(b) || tuning == nullptr) return RFMM_ERR_INVALID;
+  return b->engine->set_tuning(*tuning);
+}
+
+int rfmm_batch_autotune(rfmm_batch *b, uint32_t steps_per_trial, rfmm_tuning *best) {
+  if (bad(b)) return RFMM_ERR_INVALID;
+  return b->engine->autotune(steps_per_trial, best);
+}
+
 }  // extern "C"

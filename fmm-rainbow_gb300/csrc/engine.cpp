@@ -2,6 +2,7 @@
 #include "engine.h"
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <vector>
 
@@ -11,7 +12,6 @@ namespace rfmm {
 
 namespace {
 
-constexpr uint32_t kMaxGraphSteps = 16u;  // steps per captured graph
 constexpr uint32_t kMaxScenes = 1u << 14; // scene rank must fit above the 18 Morton bits
 
 uint32_t pad_tiles(uint32_t n) { return (n + kTile - 1u) / kTile; }
@@ -197,9 +197,19 @@ int Engine::create(const std::vector<SceneSpec> &specs, Engine **out) {
       if (e == cudaSuccess) e = cudaEventCreate(&ev);
   }
   if (e == cudaSuccess) e = configure_tree_kernels();
-  if (e == cudaSuccess) E->body_ctas_ = (uint32_t)E->sms_ * body_ctas_per_sm();
-  E->tree_ctas_ = (uint32_t)E->sms_ * 6u;
-  if (E->use_lists_) E->resort_interval_ = 0;  // slots are sorted when they are filled
+  if (e == cudaSuccess) E->body_limit_ = body_ctas_per_sm();
+  {
+    rfmm_tuning t{};
+    t.upward_ctas_per_sm = 6;
+    t.m2l_ctas_per_sm = 6;
+    t.l2l_ctas_per_sm = 5;
+    t.integrate_ctas_per_sm = E->body_limit_;
+    t.integrate_dynamic = 0;
+    t.resort_interval = E->use_lists_ ? 0u : 64u;  // slots are sorted when they are filled
+    t.graph_steps = 16;
+    t.pdl = 1;
+    if (e == cudaSuccess) e = E->set_tuning(t) == RFMM_OK ? cudaSuccess : cudaErrorInvalidValue;
+  }
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(E->d_scenes_, E->scenes_.data(), sizeof(SceneDesc) * specs.size(),
                         cudaMemcpyHostToDevice, E->stream_);
@@ -263,6 +273,7 @@ int Engine::build_tensor_maps() {
 Engine::~Engine() {
   if (stream_ != nullptr) cudaStreamSynchronize(stream_);
   for (auto &kv : graphs_) cudaGraphExecDestroy(kv.second.exec);
+  graphs_.clear();
   for (auto &ev : ev_)
     if (ev != nullptr) cudaEventDestroy(ev);
   for (void *p : allocations_) cudaFree(p);
@@ -297,8 +308,97 @@ int Engine::set_params(uint32_t scene, const rfmm_params &p) {
 
 int Engine::set_resort_interval(uint32_t steps) {
   resort_interval_ = steps;
+  tuning_.resort_interval = steps;
   since_sort_ = 0;
   return RFMM_OK;
+}
+
+void Engine::clear_graphs() {
+  if (stream_ != nullptr) cudaStreamSynchronize(stream_);
+  for (auto &kv : graphs_) cudaGraphExecDestroy(kv.second.exec);
+  graphs_.clear();
+}
+
+int Engine::get_tuning(rfmm_tuning *out) const {
+  if (out == nullptr) return RFMM_ERR_INVALID;
+  *out = tuning_;
+  return RFMM_OK;
+}
+
+int Engine::set_tuning(const rfmm_tuning &t) {
+  if (t.upward_ctas_per_sm < 1u || t.upward_ctas_per_sm > 16u || t.m2l_ctas_per_sm < 1u ||
+      t.m2l_ctas_per_sm > 6u || t.l2l_ctas_per_sm < 1u || t.l2l_ctas_per_sm > 8u ||
+      t.integrate_ctas_per_sm < 1u || t.integrate_ctas_per_sm > body_limit_ || t.graph_steps < 1u ||
+      t.graph_steps > 64u || t.integrate_dynamic > 1u || t.pdl > 1u)
+    return RFMM_ERR_INVALID;
+  clear_graphs();  // captured launch shapes change
+  tuning_ = t;
+  body_ctas_ = (uint32_t)sms_ * t.integrate_ctas_per_sm;
+  tree_ctas_ = (uint32_t)sms_ * t.upward_ctas_per_sm;
+  pdl_ = t.pdl != 0u;
+  if (resort_interval_ != t.resort_interval) {
+    resort_interval_ = t.resort_interval;
+    since_sort_ = 0;
+  }
+  return RFMM_OK;
+}
+
+int Engine::autotune(uint32_t steps_per_trial, rfmm_tuning *best) {
+  if (!committed_ || steps_per_trial == 0u) return RFMM_ERR_STATE;
+  cudaEvent_t a = nullptr, b = nullptr;
+  RF_CK(cudaEventCreate(&a));
+  RF_CK(cudaEventCreate(&b));
+  auto trial = [&](const rfmm_tuning &t, float *ms) -> int {
+    int st = set_tuning(t);
+    if (st == RFMM_OK) st = step(t.graph_steps);  // capture + warm
+    if (st != RFMM_OK) return st;
+    RF_CK(cudaEventRecord(a, stream_));
+    st = step(steps_per_trial);
+    if (st != RFMM_OK) return st;
+    RF_CK(cudaEventRecord(b, stream_));
+    RF_CK(cudaEventSynchronize(b));
+    RF_CK(cudaEventElapsedTime(ms, a, b));
+    return check_device_error();
+  };
+  rfmm_tuning cur = tuning_;
+  float cur_ms = 0.0f;
+  int st = trial(cur, &cur_ms);
+  // Coordinate descent, two sweeps over the knobs.
+  for (int sweep = 0; sweep < 2 && st == RFMM_OK; sweep++) {
+    for (int knob = 0; knob < 7 && st == RFMM_OK; knob++) {
+      std::vector<uint32_t> values;
+      switch (knob) {
+        case 0: values = {2, 4, 6, 8}; break;
+        case 1: values = {2, 4, 6}; break;
+        case 2: values = {2, 4, 5, 8}; break;
+        case 3: for (uint32_t v = 1; v <= body_limit_; v++) values.push_back(v); break;
+        case 4: values = {0, 1}; break;
+        case 5: values = {0, 1}; break;
+        case 6: values = {4, 8, 16, 32}; break;
+      }
+      for (uint32_t v : values) {
+        rfmm_tuning t = cur;
+        uint32_t *field[7] = {&t.upward_ctas_per_sm, &t.m2l_ctas_per_sm, &t.l2l_ctas_per_sm,
+                              &t.integrate_ctas_per_sm, &t.integrate_dynamic, &t.pdl,
+                              &t.graph_steps};
+        if (*field[knob] == v) continue;
+        *field[knob] = v;
+        float ms = 0.0f;
+        st = trial(t, &ms);
+        if (st != RFMM_OK) break;
+        if (ms < cur_ms * 0.995f) {
+          cur = t;
+          cur_ms = ms;
+        }
+      }
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (st != RFMM_OK) return st;
+  st = set_tuning(cur);
+  if (best != nullptr) *best = cur;
+  return st;
 }
 
 LaunchCtx Engine::ctx(uint32_t mpar, uint32_t lpar, uint32_t ppar) const {
@@ -323,6 +423,9 @@ LaunchCtx Engine::ctx(uint32_t mpar, uint32_t lpar, uint32_t ppar) const {
   L.tmaps = d_tmaps_;
   L.body_ctas = body_ctas_;
   L.tree_ctas = tree_ctas_;
+  L.m2l_ctas = (uint32_t)sms_ * tuning_.m2l_ctas_per_sm;
+  L.l2l_ctas = (uint32_t)sms_ * tuning_.l2l_ctas_per_sm;
+  L.integrate_dynamic = tuning_.integrate_dynamic != 0u;
   L.tile_list = use_lists_ ? d_tile_list_ : nullptr;
   L.task_list = use_lists_ ? d_task_list_ : nullptr;
   L.pdl = pdl_;
@@ -480,8 +583,8 @@ int Engine::commit() {
 void Engine::enqueue_step(uint32_t mpar, uint32_t lpar, uint32_t ppar) {
   LaunchCtx L = ctx(mpar, lpar, ppar);
   launch_upward(L, lpar, tasks_);
-  launch_m2l(L, lpar, (uint32_t)sms_ * 3u);
-  launch_l2l_near(L, lpar, (uint32_t)sms_ * 8u);
+  launch_m2l(L, lpar);
+  launch_l2l_near(L, lpar);
   launch_integrate(L, tiles_);
 }
 
@@ -489,8 +592,8 @@ int Engine::solve_fields() {
   if (!committed_) return RFMM_ERR_STATE;
   LaunchCtx L = ctx(mcur_, lpar_, pcur_);
   launch_upward(L, lpar_, tasks_);
-  launch_m2l(L, lpar_, (uint32_t)sms_ * 3u);
-  launch_l2l_near(L, lpar_, (uint32_t)sms_ * 8u);
+  launch_m2l(L, lpar_);
+  launch_l2l_near(L, lpar_);
   RF_CK(cudaGetLastError());
   launches_ += 3;
   lpar_ ^= 1u;
@@ -539,7 +642,7 @@ int Engine::step(uint32_t steps) {
       pcur_ ^= 1u;
       since_sort_ = 0;
     }
-    uint32_t len = std::min(steps, kMaxGraphSteps);
+    uint32_t len = std::min(steps, tuning_.graph_steps);
     bool sort_at_end = false;
     if (resort_interval_ > 0) {
       const uint32_t until = resort_interval_ - since_sort_;
@@ -645,9 +748,9 @@ int Engine::phase_times(float ms[7]) {
   RF_CK(cudaEventRecord(ev_[0], stream_));
   launch_upward(L, lpar_, tasks_);
   RF_CK(cudaEventRecord(ev_[1], stream_));
-  launch_m2l(L, lpar_, (uint32_t)sms_ * 3u);
+  launch_m2l(L, lpar_);
   RF_CK(cudaEventRecord(ev_[2], stream_));
-  launch_l2l_near(L, lpar_, (uint32_t)sms_ * 8u);
+  launch_l2l_near(L, lpar_);
   RF_CK(cudaEventRecord(ev_[3], stream_));
   launch_integrate(L, tiles_);
   RF_CK(cudaEventRecord(ev_[4], stream_));
@@ -707,8 +810,8 @@ int Engine::profile_steps(uint32_t steps, float ms[kKernelKinds], uint32_t launc
     }
     LaunchCtx L = ctx(mcur_, lpar_, pcur_);
     timed(kKUpward, [&] { launch_upward(L, lpar_, tasks_); });
-    timed(kKM2L, [&] { launch_m2l(L, lpar_, (uint32_t)sms_ * 3u); });
-    timed(kKL2LNear, [&] { launch_l2l_near(L, lpar_, (uint32_t)sms_ * 8u); });
+    timed(kKM2L, [&] { launch_m2l(L, lpar_); });
+    timed(kKL2LNear, [&] { launch_l2l_near(L, lpar_); });
     timed(kKIntegrate, [&] { launch_integrate(L, tiles_); });
     launches_ += kernels_per_step();
     tree_buf_ = (int)mcur_;
@@ -731,6 +834,111 @@ int Engine::profile_steps(uint32_t steps, float ms[kKernelKinds], uint32_t launc
   }
   if (st != RFMM_OK) return st;
   return check_device_error();
+}
+
+int Engine::diag_prepare(uint32_t scene, size_t doubles) {
+  if (scene >= scenes_.size() || !committed_) return RFMM_ERR_STATE;
+  if (d_accphi_ == nullptr) {
+    const int st = alloc((void **)&d_accphi_, 16ull * slots_);
+    if (st != RFMM_OK) return st;
+  }
+  if (doubles > diag_doubles_) {
+    const int st = alloc((void **)&d_diag_, 8ull * doubles);
+    if (st != RFMM_OK) return st;
+    diag_doubles_ = doubles;
+  }
+  // Field solve of the current positions, then per-body acceleration and
+  // potential in the caller's order, and the bodies themselves in that order.
+  int st = solve_fields();
+  if (st != RFMM_OK) return st;
+  const SceneDesc &d = scenes_[scene];
+  LaunchCtx L = ctx(tree_buf_ < 0 ? mcur_ : (uint32_t)tree_buf_, lpar_, pcur_);
+  launch_accel(L, d_ids_[pcur_], d_accphi_ + d.body_off, d.tile_off, pad_tiles(d.n));
+  launch_unpermute(L, d_ids_[pcur_], d_part_[pcur_ ^ 1u], d.tile_off, pad_tiles(d.n));
+  RF_CK(cudaGetLastError());
+  launches_ += 2;
+  return RFMM_OK;
+}
+
+int Engine::accelerations(uint32_t scene, float *host_out) {
+  if (host_out == nullptr) return RFMM_ERR_INVALID;
+  const int st = diag_prepare(scene, 0);
+  if (st != RFMM_OK) return st;
+  const SceneDesc &d = scenes_[scene];
+  RF_CK(cudaMemcpyAsync(host_out, d_accphi_ + d.body_off, 16ull * d.n, cudaMemcpyDeviceToHost,
+                        stream_));
+  return sync();
+}
+
+int Engine::force_error(uint32_t scene, uint32_t targets, uint64_t seed, double *rms_rel,
+                        double *max_rel) {
+  if (scene >= scenes_.size() || targets == 0u) return RFMM_ERR_INVALID;
+  const SceneDesc &d = scenes_[scene];
+  const uint32_t nt = std::min(targets, d.n);
+  const uint32_t splits = 64u;
+  // doubles: partial [splits][nt][3], reference [nt][3], and the target ids.
+  const size_t doubles = (size_t)splits * nt * 3u + (size_t)nt * 3u + nt;
+  int st = diag_prepare(scene, doubles);
+  if (st != RFMM_OK) return st;
+  // Uniform sample without replacement (splitmix64 partial Fisher-Yates).
+  std::vector<uint32_t> idx(d.n);
+  for (uint32_t i = 0; i < d.n; i++) idx[i] = i;
+  uint64_t x = seed;
+  for (uint32_t i = 0; i < nt; i++) {
+    x += 0x9E3779B97F4A7C15ull;
+    uint64_t z = x;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    const uint32_t j = i + (uint32_t)(z % (uint64_t)(d.n - i));
+    std::swap(idx[i], idx[j]);
+  }
+  double *partial = d_diag_;
+  double *ref = d_diag_ + (size_t)splits * nt * 3u;
+  uint32_t *tgt = reinterpret_cast<uint32_t *>(ref + (size_t)nt * 3u);
+  RF_CK(cudaMemcpyAsync(tgt, idx.data(), 4ull * nt, cudaMemcpyHostToDevice, stream_));
+  launch_direct_sum_f64(stream_, d_part_[pcur_ ^ 1u] + 2ull * d.body_off, d.n, tgt, nt,
+                        (double)d.gravity, (double)d.softening, partial, splits, ref);
+  RF_CK(cudaGetLastError());
+  launches_ += 2;
+  std::vector<double> href((size_t)nt * 3u);
+  std::vector<float> acc((size_t)d.n * 4u);
+  RF_CK(cudaMemcpyAsync(href.data(), ref, 8ull * nt * 3u, cudaMemcpyDeviceToHost, stream_));
+  RF_CK(cudaMemcpyAsync(acc.data(), d_accphi_ + d.body_off, 16ull * d.n, cudaMemcpyDeviceToHost,
+                        stream_));
+  st = sync();
+  if (st != RFMM_OK) return st;
+  double num = 0.0, den = 0.0, mx = 0.0;
+  for (uint32_t t = 0; t < nt; t++) {
+    const uint32_t i = idx[t];
+    double e2 = 0.0, r2 = 0.0;
+    for (int k = 0; k < 3; k++) {
+      const double df = (double)acc[4u * i + k] - href[3u * t + k];
+      e2 += df * df;
+      r2 += href[3u * t + k] * href[3u * t + k];
+    }
+    num += e2;
+    den += r2;
+    if (r2 > 0.0) mx = std::max(mx, std::sqrt(e2 / r2));
+  }
+  if (rms_rel) *rms_rel = den > 0.0 ? std::sqrt(num / den) : 0.0;
+  if (max_rel) *max_rel = mx;
+  return RFMM_OK;
+}
+
+int Engine::diagnostics(uint32_t scene, double out[9]) {
+  if (out == nullptr) return RFMM_ERR_INVALID;
+  const uint32_t blocks = 4u * (uint32_t)sms_;
+  int st = diag_prepare(scene, 9u * blocks + 9u);
+  if (st != RFMM_OK) return st;
+  const SceneDesc &d = scenes_[scene];
+  launch_diagnostics(stream_, d_part_[pcur_ ^ 1u] + 2ull * d.body_off, d_accphi_ + d.body_off, d.n,
+                     d_diag_, blocks, d_diag_ + 9u * blocks);
+  RF_CK(cudaGetLastError());
+  launches_ += 2;
+  RF_CK(cudaMemcpyAsync(out, d_diag_ + 9u * blocks, 9 * sizeof(double), cudaMemcpyDeviceToHost,
+                        stream_));
+  return sync();
 }
 
 }  // namespace rfmm

@@ -40,6 +40,9 @@ class Engine {
   cudaStream_t stream() const { return stream_; }
   int set_params(uint32_t scene, const rfmm_params &p);
   int set_resort_interval(uint32_t steps);
+  int get_tuning(rfmm_tuning *out) const;
+  int set_tuning(const rfmm_tuning &t);
+  int autotune(uint32_t steps_per_trial, rfmm_tuning *best);
 
   // Copy a scene's bodies (caller order) into the resident buffer; the new
   // bodies take effect at the next commit().
@@ -76,6 +79,11 @@ class Engine {
   uint64_t launch_count() const { return launches_; }
   int device_error(uint32_t *code, uint32_t *info);
 
+  // Diagnostics on the current positions (each runs a field solve first).
+  int accelerations(uint32_t scene, float *host_out);  // n x (ax, ay, az, phi), caller order
+  int force_error(uint32_t scene, uint32_t targets, uint64_t seed, double *rms_rel, double *max_rel);
+  int diagnostics(uint32_t scene, double out[9]);
+
   uint32_t num_scenes() const { return (uint32_t)scenes_.size(); }
   const SceneDesc &scene(uint32_t s) const { return scenes_[s]; }
   size_t buffer_bytes(uint32_t scene, int which) const;
@@ -99,6 +107,9 @@ class Engine {
   int sms_ = 0;
   uint32_t body_ctas_ = 0;
   uint32_t tree_ctas_ = 0;
+  uint32_t body_limit_ = 1;   // resident integrate CTAs per SM
+  rfmm_tuning tuning_{};
+  void clear_graphs();
   bool use_lists_ = false;  // serving: kernels walk the active tile/task lists
   cudaStream_t stream_ = nullptr;
   cudaStream_t own_stream_ = nullptr;
@@ -114,6 +125,10 @@ class Engine {
   uint32_t *d_ids_[2] = {nullptr, nullptr};
   uint4 *d_mom_[2] = {nullptr, nullptr};
   uint4 *d_mom_scratch_ = nullptr;
+  float4 *d_accphi_ = nullptr;    // diagnostics: per-body acceleration + potential
+  double *d_diag_ = nullptr;      // diagnostics: FP64 partial sums
+  size_t diag_doubles_ = 0;
+  int diag_prepare(uint32_t scene, size_t doubles);
   float4 *d_src_ = nullptr;
   float4 *d_aux_ = nullptr;
   uint32_t *d_tile_list_ = nullptr, *d_task_list_ = nullptr;

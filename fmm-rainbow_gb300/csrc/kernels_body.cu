@@ -45,23 +45,24 @@ __device__ __forceinline__ void soft_wall(float &p, float &v, float world_edge, 
   }
 }
 
-// One body's integrate (wgsl:613-771).  Writes the new state into p0/p1 and
-// the new position's leaf cell and fixed-point coordinates (the next deposit).
-__device__ __forceinline__ void integrate_body(const SceneDesc &S, float4 &p0, float4 &p1,
-                                               const uint4 *__restrict__ mom,
-                                               const float4 *__restrict__ src,
-                                               const float4 *__restrict__ aux,
-                                               const uint32_t *__restrict__ choice,
-                                               const float *__restrict__ fields, uint32_t &key,
-                                               int32_t &qx, int32_t &qy, int32_t &qz) {
-    float px = p0.x, py = p0.y, pz = p0.z;
-    float vx = p1.x, vy = p1.y, vz = p1.z;
+// FMM acceleration at a body (wgsl:619-657): adaptive descent to the sample
+// cell, local expansion about its centre, softened self-leaf monopole.  With
+// `phi`, also the potential of the same expansion (diagnostics only; integrate
+// never evaluates it).  Returns the sample cell's count.
+template <bool kPhi>
+__device__ __forceinline__ uint32_t body_acceleration(const SceneDesc &S, float px, float py, float pz,
+                                                      const uint4 *__restrict__ mom,
+                                                      const float4 *__restrict__ src,
+                                                      const float4 *__restrict__ aux,
+                                                      const uint32_t *__restrict__ choice,
+                                                      const float *__restrict__ fields, float &ax,
+                                                      float &ay, float &az, float &pulse,
+                                                      float *phi) {
     const uint32_t D = S.depth;
     // Leaf coordinates; floor(u * 2^l) == floor(u * 2^D) >> (D - l).
     const uint32_t dimD = 1u << D;
     const uint32_t lx = cell_of_unit(unit_coord(px), dimD), ly = cell_of_unit(unit_coord(py), dimD),
                    lz = cell_of_unit(unit_coord(pz), dimD);
-
     // Adaptive descent (wgsl:625-639): first level whose cell holds at most
     // 16 bodies, else the leaf level.  Resolved once per leaf by the upward
     // pass; bodies of unresolved leaves (sparse subtrees) descend here.
@@ -94,9 +95,9 @@ __device__ __forceinline__ void integrate_body(const SceneDesc &S, float4 &p0, f
     const float4 *fp = reinterpret_cast<const float4 *>(fields + (size_t)cell_index * 12u);
     const float4 fa = __ldg(fp), fj0 = __ldg(fp + 1), fj1 = __ldg(fp + 2);
     const float rx = px - cx, ry = py - cy, rz = pz - cz;
-    float ax = fa.x + (fj0.x * rx + fj0.y * ry + fj0.z * rz);
-    float ay = fa.y + (fj0.y * rx + fj0.w * ry + fj1.x * rz);
-    float az = fa.z + (fj0.z * rx + fj1.x * ry + fj1.y * rz);
+    ax = fa.x + (fj0.x * rx + fj0.y * ry + fj0.z * rz);
+    ay = fa.y + (fj0.y * rx + fj0.w * ry + fj1.x * rz);
+    az = fa.z + (fj0.z * rx + fj1.x * ry + fj1.y * rz);
 
     // Self leaf: softened monopole of the other count-1 bodies (wgsl:646-657).
     // x / 2^l == x * 2^-l exactly, so the eps division is a scaling.
@@ -110,6 +111,36 @@ __device__ __forceinline__ void integrate_body(const SceneDesc &S, float4 &p0, f
       ay = ay + gsm * dy * inv_r * inv_r * inv_r;
       az = az + gsm * dz * inv_r * inv_r * inv_r;
     }
+
+    if (kPhi) {
+      float p = fa.w - ((fa.x * rx + fa.y * ry) + fa.z * rz);
+      if (count > 1u) {
+        const float4 s = __ldg(&src[cell_index]);
+        const float dx = s.x - px, dy = s.y - py, dz = s.z - pz;
+        const float eps = fmaxf(S.softening, (0.62f * kHalf) * pow2_neg(chosen));
+        p = p - ax4.x / sqrtf((dx * dx + dy * dy) + dz * dz + eps * eps);
+      }
+      *phi = p;
+    }
+    pulse = ax4.y;  // clamp((f32(count) - 16) / 72, 0, 1)
+    return count;
+}
+
+// One body's integrate (wgsl:613-771).  Writes the new state into p0/p1 and
+// the new position's leaf cell and fixed-point coordinates (the next deposit).
+__device__ __forceinline__ void integrate_body(const SceneDesc &S, float4 &p0, float4 &p1,
+                                               const uint4 *__restrict__ mom,
+                                               const float4 *__restrict__ src,
+                                               const float4 *__restrict__ aux,
+                                               const uint32_t *__restrict__ choice,
+                                               const float *__restrict__ fields, uint32_t &key,
+                                               int32_t &qx, int32_t &qy, int32_t &qz) {
+    float px = p0.x, py = p0.y, pz = p0.z;
+    float vx = p1.x, vy = p1.y, vz = p1.z;
+    const uint32_t D = S.depth;
+    float ax, ay, az, density_pulse;
+    const uint32_t count = body_acceleration<false>(S, px, py, pz, mom, src, aux, choice, fields, ax,
+                                                    ay, az, density_pulse, nullptr);
 
     // Interactive control field (wgsl:659-689); off unless control_point.w > 0.5.
     float control_influence = 0.0f;
@@ -153,7 +184,6 @@ __device__ __forceinline__ void integrate_body(const SceneDesc &S, float4 &p0, f
     const float signed_radial = clampf_d(pv / (radius * vlen), -1.0f, 1.0f);
     const float rf = fabsf(signed_radial);
     const float radial_shock = rf * rf * rf;
-    const float density_pulse = ax4.y;  // clamp((f32(count) - 16) / 72, 0, 1)
     const float field_strength = clampf_d(length3(ax, ay, az) * (radius + 0.12f) * 0.58f, 0.0f, 1.0f);
     const float target_exc = clampf_d(0.025f + radial_shock * 0.56f + density_pulse * 0.26f +
                                           field_strength * 0.13f + control_influence * 0.42f,
@@ -205,31 +235,44 @@ __global__ void __launch_bounds__(256) k_integrate(const SceneDesc *__restrict__
                                                    const float *__restrict__ fields,
                                                    uint4 *__restrict__ mom_next, uint32_t tiles,
                                                    const uint32_t *__restrict__ tile_list,
-                                                   const Counters *__restrict__ ctr) {
+                                                   Counters *__restrict__ ctr, int dynamic) {
   __shared__ DepositTable T;
   __shared__ SceneDesc S;
+  __shared__ uint32_t s_next;
   T.clear();
   grid_dependency_wait();  // fields of this step are complete
   const uint32_t ntiles = tile_list != nullptr ? min(ctr->tiles_active, tiles) : tiles;
+  // Static schedule: a contiguous slice per CTA.  Dynamic: tiles are taken
+  // one at a time from a counter (reset by this step's upward pass).
   uint32_t t0, t1;
   cta_tile_range(ntiles, t0, t1);
+  auto grab = [&]() -> uint32_t {
+    __syncthreads();
+    if (threadIdx.x == 0) s_next = atomicAdd(&ctr->tile_cursor, 1u);
+    __syncthreads();
+    return s_next;
+  };
+  uint32_t i = dynamic ? grab() : t0;
+  const uint32_t end = dynamic ? ntiles : t1;
   uint32_t cur = 0xFFFFFFFFu;
   // The next tile's bodies are loaded one iteration ahead.
   float4 n0 = make_float4(0.f, 0.f, 0.f, 0.f), n1 = n0;
-  uint32_t next_tile = t0 < t1 ? (tile_list != nullptr ? tile_list[t0] : t0) : 0u;
-  if (t0 < t1) {
+  uint32_t next_tile = i < end ? (tile_list != nullptr ? tile_list[i] : i) : 0u;
+  if (i < end) {
     n0 = part[2u * (next_tile * kTile + threadIdx.x)];
     n1 = part[2u * (next_tile * kTile + threadIdx.x) + 1u];
   }
-  for (uint32_t i = t0; i < t1; i++) {
+  while (i < end) {
     const uint32_t tile = next_tile;
     const uint32_t slot = tile * kTile + threadIdx.x;
     float4 p0 = n0, p1 = n1;
-    if (i + 1u < t1) {
-      next_tile = tile_list != nullptr ? tile_list[i + 1u] : i + 1u;
+    const uint32_t ni = dynamic ? grab() : i + 1u;
+    if (ni < end) {
+      next_tile = tile_list != nullptr ? tile_list[ni] : ni;
       n0 = part[2u * (next_tile * kTile + threadIdx.x)];
       n1 = part[2u * (next_tile * kTile + threadIdx.x) + 1u];
     }
+    i = ni;
     const uint32_t sc = tile_scene[tile];
     if (sc != cur) {
       load_scene(S, scenes, sc);
@@ -287,6 +330,36 @@ __global__ void __launch_bounds__(256) k_deposit(const SceneDesc *__restrict__ s
   }
   __syncthreads();
   T.flush(moments);
+}
+
+// FMM acceleration and potential of every body of one scene, written in the
+// caller's body order (diagnostics and force-error checks; not on the step).
+__global__ void __launch_bounds__(256) k_accel(const SceneDesc *__restrict__ scenes,
+                                               const uint32_t *__restrict__ tile_scene,
+                                               const float4 *__restrict__ part,
+                                               const uint32_t *__restrict__ ids,
+                                               const uint4 *__restrict__ mom,
+                                               const float4 *__restrict__ src,
+                                               const float4 *__restrict__ aux,
+                                               const uint32_t *__restrict__ choice,
+                                               const float *__restrict__ fields,
+                                               float4 *__restrict__ out, uint32_t tile_base) {
+  const uint32_t tile = tile_base + blockIdx.x;
+  const SceneDesc &S = scenes[tile_scene[tile]];
+  const uint32_t slot = tile * kTile + threadIdx.x;
+  if (slot - S.body_off >= S.n) return;
+  const uint32_t id = ids[slot];
+  if (id >= S.n) return;
+  const float4 p = part[2u * slot];
+  float ax, ay, az, pulse, phi;
+  body_acceleration<true>(S, p.x, p.y, p.z, mom, src, aux, choice, fields, ax, ay, az, pulse, &phi);
+  out[id] = make_float4(ax, ay, az, phi);
+}
+
+void launch_accel(const LaunchCtx &L, const uint32_t *ids, float4 *out, uint32_t tile_base,
+                  uint32_t tiles) {
+  k_accel<<<tiles, kTile, 0, L.stream>>>(L.scenes, L.tile_scene, L.part, ids, L.mom, L.src, L.aux,
+                                         L.choice, L.fields, out, tile_base);
 }
 
 // 3-D Morton interleave of leaf coordinates (x in bit 0).
@@ -529,7 +602,7 @@ void launch_integrate(const LaunchCtx &L, uint32_t tiles) {
   launch_step_kernel(L, k_integrate, dim3(body_grid(L, tiles)), dim3(kTile), 0, L.scenes,
                      L.tile_scene, L.part, (const uint4 *)L.mom, (const float4 *)L.src,
                      (const float4 *)L.aux, (const uint32_t *)L.choice, (const float *)L.fields,
-                     L.mom_next, tiles, L.tile_list, (const Counters *)L.ctr);
+                     L.mom_next, tiles, L.tile_list, L.ctr, L.integrate_dynamic ? 1 : 0);
 }
 
 void launch_deposit(const LaunchCtx &L, uint4 *moments, uint32_t tiles) {

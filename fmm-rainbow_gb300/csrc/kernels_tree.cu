@@ -227,6 +227,7 @@ __global__ void __launch_bounds__(256) k_upward(const SceneDesc *__restrict__ sc
   __shared__ SceneDesc sS;
   const uint32_t tid = threadIdx.x;
   grid_dependency_wait();  // the previous integrate deposited and read the fields
+  if (blockIdx.x == 0 && tid == 0) ctr->tile_cursor = 0u;  // for this step's integrate
 
   // Clear the fields of the previous step's targets (children of listed parents).
   {
@@ -264,7 +265,8 @@ __global__ void __launch_bounds__(256) k_upward(const SceneDesc *__restrict__ sc
 // -------------------------------------------------------------------- M2L
 
 constexpr uint32_t kTileCells = 216u;   // 6x6x6 children of a 3x3x3 parent block
-constexpr uint32_t kSlotStride = 217u;  // padded so the 10 summing lanes hit distinct banks
+constexpr uint32_t kChunk = 54u;        // stencil slots evaluated per pass (216 = 4 x 54)
+constexpr uint32_t kSlotStride = 55u;   // padded so the 80 summing threads hit distinct banks
 constexpr uint32_t kTmaBytes = kTileCells * 16u;
 
 struct M2LShared {
@@ -373,51 +375,55 @@ __global__ void __launch_bounds__(256) k_m2l(const SceneDesc *__restrict__ scene
     __syncthreads();
     if (sh.stop) return;
 
-    // Warp w evaluates the stencil of child w of the parent.
+    // Warp w evaluates the stencil of child w of the parent, a chunk of slots
+    // at a time; 80 threads (8 children x 10 components) then add the chunk to
+    // their running sums, strictly in slot order.
     const int cx = (int)(warp & 1u), cy = (int)((warp >> 1) & 1u), cz = (int)(warp >> 2);
     const uint32_t tx = (uint32_t)(2 * pcx + cx), ty = (uint32_t)(2 * pcy + cy), tz = (uint32_t)(2 * pcz + cz);
     const uint32_t target = lvl_base + lin3(tx, ty, tz, dim);
     const bool live = mom[target].x != 0u;  // empty children are not targets
     if (lane == 0) sh.live[warp] = live ? target : 0xFFFFFFFFu;
-    if (live) {
-      const float ctx = cell_center_lv(tx, l), cty = cell_center_lv(ty, l),
-                  ctz = cell_center_lv(tz, l);
-      const float eps = (0.06f * kHalf) * pow2_neg(l);  // wgsl:507, / 2^l as an exact scaling
-      for (uint32_t k = lane; k < kTileCells; k += 32u) {
-        // Reference loop order: source parent (pz, py, px) then child (cz, cy, cx).
-        const uint32_t pidx = k >> 3, ch = k & 7u;
-        const int ux = 2 * (int)(pidx % 3u) + (int)(ch & 1u);
-        const int uy = 2 * (int)((pidx / 3u) % 3u) + (int)((ch >> 1) & 1u);
-        const int uz = 2 * (int)(pidx / 9u) + (int)(ch >> 2);
-        // Source child coordinate minus target coordinate = u - 2 - child.
-        const int sx = ux - 2 - cx, sy = uy - 2 - cy, sz = uz - 2 - cz;
-        const bool near = sx >= -1 && sx <= 1 && sy >= -1 && sy <= 1 && sz >= -1 && sz <= 1;
-        const float4 s = sh.tile[ux + 6 * (uy + 6 * uz)];
-        float out[10];
-        if (!near && s.w != 0.0f) {
-          pair_field_d(s, ctx, cty, ctz, eps, out);
-        } else {
+    const float ctx = cell_center_lv(tx, l), cty = cell_center_lv(ty, l), ctz = cell_center_lv(tz, l);
+    const float eps = (0.06f * kHalf) * pow2_neg(l);  // wgsl:507, / 2^l as an exact scaling
+    float acc = 0.0f;                                 // running sum of (child tid/10, comp tid%10)
+    for (uint32_t c0 = 0; c0 < kTileCells; c0 += kChunk) {
+      if (live) {
+        for (uint32_t kk = lane; kk < kChunk; kk += 32u) {
+          const uint32_t k = c0 + kk;
+          // Reference loop order: source parent (pz, py, px) then child (cz, cy, cx).
+          const uint32_t pidx = k >> 3, ch = k & 7u;
+          const int ux = 2 * (int)(pidx % 3u) + (int)(ch & 1u);
+          const int uy = 2 * (int)((pidx / 3u) % 3u) + (int)((ch >> 1) & 1u);
+          const int uz = 2 * (int)(pidx / 9u) + (int)(ch >> 2);
+          // Source child coordinate minus target coordinate = u - 2 - child.
+          const int sx = ux - 2 - cx, sy = uy - 2 - cy, sz = uz - 2 - cz;
+          const bool near = sx >= -1 && sx <= 1 && sy >= -1 && sy <= 1 && sz >= -1 && sz <= 1;
+          const float4 src4 = sh.tile[ux + 6 * (uy + 6 * uz)];
+          float out[10];
+          if (!near && src4.w != 0.0f) {
+            pair_field_d(src4, ctx, cty, ctz, eps, out);
+          } else {
 #pragma unroll
-          for (int c = 0; c < 10; c++) out[c] = 0.0f;
+            for (int c = 0; c < 10; c++) out[c] = 0.0f;
+          }
+#pragma unroll
+          for (int c = 0; c < 10; c++) sh.vals[warp][c][kk] = out[c];
         }
-#pragma unroll
-        for (int c = 0; c < 10; c++) sh.vals[warp][c][k] = out[c];
       }
+      __syncthreads();
+      if (tid < 80u && sh.live[tid / 10u] != 0xFFFFFFFFu) {
+        const float *row = sh.vals[tid / 10u][tid % 10u];
+#pragma unroll 6
+        for (uint32_t kk = 0; kk < kChunk; kk++) acc = acc + row[kk];
+      }
+      __syncthreads();
     }
-    __syncthreads();
-    // 80 threads sum the 8 children x 10 components, each strictly in slot
-    // order (loads run ahead of the dependent adds); 16 more write the pads.
     if (tid < 96u) {
       const uint32_t t = tid < 80u ? tid / 10u : (tid - 80u) >> 1;
       const uint32_t tgt = sh.live[t];
       if (tgt != 0xFFFFFFFFu) {
         if (tid < 80u) {
-          const uint32_t c = tid % 10u;
-          const float *row = sh.vals[t][c];
-          float acc = 0.0f;
-#pragma unroll 8
-          for (uint32_t k = 0; k < kTileCells; k++) acc = acc + row[k];
-          lfield[(size_t)tgt * 12u + c] = acc;
+          lfield[(size_t)tgt * 12u + tid % 10u] = acc;
         } else {
           lfield[(size_t)tgt * 12u + 10u + (tid & 1u)] = 0.0f;
         }
@@ -539,14 +545,14 @@ void launch_upward(const LaunchCtx &L, uint32_t list_par, uint32_t tasks) {
 
 size_t m2l_smem_bytes() { return sizeof(M2LShared) + 128; }
 
-void launch_m2l(const LaunchCtx &L, uint32_t list_par, uint32_t grid) {
-  launch_step_kernel(L, k_m2l, dim3(grid), dim3(256), m2l_smem_bytes(), L.scenes,
+void launch_m2l(const LaunchCtx &L, uint32_t list_par) {
+  launch_step_kernel(L, k_m2l, dim3(L.m2l_ctas), dim3(256), m2l_smem_bytes(), L.scenes,
                      (const WorkItem *)L.plist, L.plist_cap, L.ctr, list_par, (const uint4 *)L.mom,
                      (const float4 *)L.src, L.lfield, L.tmaps);
 }
 
-void launch_l2l_near(const LaunchCtx &L, uint32_t list_par, uint32_t grid) {
-  launch_step_kernel(L, k_l2l_near, dim3(grid), dim3(256), 0, L.scenes, (const WorkItem *)L.plist,
+void launch_l2l_near(const LaunchCtx &L, uint32_t list_par) {
+  launch_step_kernel(L, k_l2l_near, dim3(L.l2l_ctas), dim3(256), 0, L.scenes, (const WorkItem *)L.plist,
                      L.plist_cap, (const Counters *)L.ctr, list_par, (const uint4 *)L.mom,
                      (const float4 *)L.src, (const float *)L.lfield, L.fields);
 }

@@ -221,13 +221,16 @@ extern "C" int rfmm_solve_fields_noalloc(const void *device_particles, uint32_t 
   L.tmaps = S->tmaps;
   L.body_ctas = st.body_ctas;
   L.tree_ctas = (uint32_t)st.sms * 6u;
+  L.m2l_ctas = (uint32_t)st.sms * 6u;
+  L.l2l_ctas = (uint32_t)st.sms * 5u;
+  L.integrate_dynamic = false;
   L.tile_list = nullptr;
   L.task_list = nullptr;
   L.pdl = false;
 
   launch_deposit(L, L.mom, tiles);
   launch_upward(L, 0u, tasks);
-  launch_m2l(L, 0u, (uint32_t)st.sms * 3u);
-  launch_l2l_near(L, 0u, (uint32_t)st.sms * 8u);
+  launch_m2l(L, 0u);
+  launch_l2l_near(L, 0u);
   return cuda_rc(cudaGetLastError());
 }

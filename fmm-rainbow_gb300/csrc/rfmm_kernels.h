@@ -33,6 +33,9 @@ struct LaunchCtx {
   const CUtensorMap *tmaps;    // 8 per scene (levels 0..7; 3..6 used)
   uint32_t body_ctas;          // persistent grid of the body passes (resident CTAs)
   uint32_t tree_ctas;          // persistent grid of the upward pass
+  uint32_t m2l_ctas;           // persistent grid of the M2L pass
+  uint32_t l2l_ctas;           // persistent grid of the L2L + near pass
+  bool integrate_dynamic;      // integrate CTAs grab tiles from a counter
   const uint32_t *tile_list;   // active body tiles (null: every tile)
   const uint32_t *task_list;   // active upward tasks (null: every task)
   bool pdl;                    // launch step kernels with programmatic stream serialization
@@ -68,8 +71,8 @@ inline void launch_step_kernel(const LaunchCtx &L, void (*kernel)(K...), dim3 gr
 
 // Tree passes (kernels_tree.cu).
 void launch_upward(const LaunchCtx &L, uint32_t list_par, uint32_t tasks);
-void launch_m2l(const LaunchCtx &L, uint32_t list_par, uint32_t grid);
-void launch_l2l_near(const LaunchCtx &L, uint32_t list_par, uint32_t grid);
+void launch_m2l(const LaunchCtx &L, uint32_t list_par);
+void launch_l2l_near(const LaunchCtx &L, uint32_t list_par);
 cudaError_t configure_tree_kernels();
 
 // Body passes (kernels_body.cu).
@@ -87,6 +90,16 @@ void launch_unpermute(const LaunchCtx &L, const uint32_t *ids, float4 *out, uint
 void launch_initialize(const LaunchCtx &L, float4 *part_out, uint32_t tile_base, uint32_t tiles);
 void launch_iota(cudaStream_t stream, uint32_t *ids, uint32_t count);
 uint32_t body_ctas_per_sm();  // resident 256-thread CTAs per SM of the persistent body passes
+// FMM acceleration + potential per body of tiles [tile_base, +tiles), caller order.
+void launch_accel(const LaunchCtx &L, const uint32_t *ids, float4 *out, uint32_t tile_base,
+                  uint32_t tiles);
+
+// FP64 diagnostics (kernels_diag.cu).
+void launch_direct_sum_f64(cudaStream_t stream, const float4 *part_caller, uint32_t n,
+                           const uint32_t *targets, uint32_t nt, double gravity, double eps,
+                           double *partial, uint32_t splits, double *out);
+void launch_diagnostics(cudaStream_t stream, const float4 *part_caller, const float4 *accphi,
+                        uint32_t n, double *partial, uint32_t blocks, double *out);
 
 // LSD radix sort of (key, value) pairs, 8-bit digits (kernels_sort.cu).
 struct SortScratch {

@@ -43,7 +43,8 @@ struct Counters {
   uint32_t error_info;   // kernel-specific detail for `error`
   uint32_t tiles_active; // entries of the active body-tile list (when one is used)
   uint32_t tasks_active; // entries of the active upward-task list (when one is used)
-  uint32_t pad[2];
+  uint32_t tile_cursor;  // next body tile for dynamically scheduled integrate CTAs
+  uint32_t pad;
 };
 
 enum DeviceError : uint32_t {

@@ -66,6 +66,23 @@ class ServerStats(C.Structure):
                 ("body_steps_per_s", C.c_double), ("body_steps", C.c_double)]
 
 
+class Tuning(C.Structure):
+    """`rfmm_tuning` (include/rfmm.h): launch shapes; results never depend on them."""
+
+    _fields_ = [("upward_ctas_per_sm", C.c_uint32), ("m2l_ctas_per_sm", C.c_uint32),
+                ("l2l_ctas_per_sm", C.c_uint32), ("integrate_ctas_per_sm", C.c_uint32),
+                ("integrate_dynamic", C.c_uint32), ("resort_interval", C.c_uint32),
+                ("graph_steps", C.c_uint32), ("pdl", C.c_uint32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Diagnostics(C.Structure):
+    _fields_ = [("kinetic", C.c_double), ("potential", C.c_double), ("total", C.c_double),
+                ("momentum", C.c_double * 3), ("angular_momentum", C.c_double * 3)]
+
+
 class Plan(C.Structure):
     _fields_ = [("particles", C.c_uint32), ("depth", C.c_uint32), ("cells", C.c_uint32),
                 ("fixed_point_scale", C.c_float)]
@@ -131,6 +148,17 @@ SIGNATURES = {
     "rfmm_batch_launch_count": (_i, [_vp, C.POINTER(C.c_uint64)]),
     "rfmm_batch_profile_steps": (_i, [_vp, _u32, C.POINTER(_f32), C.POINTER(_u32)]),
     "rfmm_batch_set_resort_interval": (_i, [_vp, _u32]),
+    "rfmm_accelerations": (_i, [_vp, _vp, _sz]),
+    "rfmm_force_error": (_i, [_vp, _u32, C.c_uint64, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "rfmm_get_diagnostics": (_i, [_vp, C.POINTER(Diagnostics)]),
+    "rfmm_batch_force_error": (_i, [_vp, _u32, _u32, C.c_uint64, C.POINTER(C.c_double),
+                                    C.POINTER(C.c_double)]),
+    "rfmm_get_tuning": (_i, [_vp, C.POINTER(Tuning)]),
+    "rfmm_set_tuning": (_i, [_vp, C.POINTER(Tuning)]),
+    "rfmm_autotune": (_i, [_vp, _u32, C.POINTER(Tuning)]),
+    "rfmm_batch_get_tuning": (_i, [_vp, C.POINTER(Tuning)]),
+    "rfmm_batch_set_tuning": (_i, [_vp, C.POINTER(Tuning)]),
+    "rfmm_batch_autotune": (_i, [_vp, _u32, C.POINTER(Tuning)]),
     "rfmm_server_create": (_i, [C.POINTER(ServerConfig), C.POINTER(_vp)]),
     "rfmm_server_destroy": (_i, [_vp]),
     "rfmm_server_submit": (_i, [_vp, _vp, _u32, _P, _u32, C.POINTER(C.c_uint64)]),
@@ -329,6 +357,37 @@ class Solver:
         _check(lib().rfmm_launch_count(self._h, C.byref(out)), "rfmm_launch_count")
         return out.value
 
+    def accelerations(self) -> np.ndarray:
+        """(N, 4) float32: FMM ax, ay, az, phi of the current positions (caller order)."""
+        out = np.empty((self.n, 4), np.float32)
+        _check(lib().rfmm_accelerations(self._h, out.ctypes.data, out.nbytes), "rfmm_accelerations")
+        return out
+
+    def force_error(self, targets: int = 4096, seed: int = 1):
+        rms, mx = C.c_double(), C.c_double()
+        _check(lib().rfmm_force_error(self._h, targets, seed, C.byref(rms), C.byref(mx)),
+               "rfmm_force_error")
+        return rms.value, mx.value
+
+    def diagnostics(self) -> dict:
+        d = Diagnostics()
+        _check(lib().rfmm_get_diagnostics(self._h, C.byref(d)), "rfmm_get_diagnostics")
+        return {"kinetic": d.kinetic, "potential": d.potential, "total": d.total,
+                "momentum": list(d.momentum), "angular_momentum": list(d.angular_momentum)}
+
+    def tuning(self) -> Tuning:
+        t = Tuning()
+        _check(lib().rfmm_get_tuning(self._h, C.byref(t)), "rfmm_get_tuning")
+        return t
+
+    def set_tuning(self, t: Tuning):
+        _check(lib().rfmm_set_tuning(self._h, C.byref(t)), "rfmm_set_tuning")
+
+    def autotune(self, steps_per_trial: int = 20) -> Tuning:
+        t = Tuning()
+        _check(lib().rfmm_autotune(self._h, steps_per_trial, C.byref(t)), "rfmm_autotune")
+        return t
+
     def device_error(self):
         code, info = C.c_uint32(), C.c_uint32()
         _check(lib().rfmm_device_error(self._h, C.byref(code), C.byref(info)), "rfmm_device_error")
@@ -414,6 +473,25 @@ class Batch:
         out = C.c_uint64()
         _check(lib().rfmm_batch_launch_count(self._h, C.byref(out)), "rfmm_batch_launch_count")
         return out.value
+
+    def force_error(self, scene, targets=1024, seed=1):
+        rms, mx = C.c_double(), C.c_double()
+        _check(lib().rfmm_batch_force_error(self._h, scene, targets, seed, C.byref(rms), C.byref(mx)),
+               "rfmm_batch_force_error")
+        return rms.value, mx.value
+
+    def tuning(self):
+        t = Tuning()
+        _check(lib().rfmm_batch_get_tuning(self._h, C.byref(t)), "rfmm_batch_get_tuning")
+        return t
+
+    def set_tuning(self, t):
+        _check(lib().rfmm_batch_set_tuning(self._h, C.byref(t)), "rfmm_batch_set_tuning")
+
+    def autotune(self, steps_per_trial=10):
+        t = Tuning()
+        _check(lib().rfmm_batch_autotune(self._h, steps_per_trial, C.byref(t)), "rfmm_batch_autotune")
+        return t
 
     def profile_steps(self, steps):
         ms = (C.c_float * len(KERNEL_KINDS))()

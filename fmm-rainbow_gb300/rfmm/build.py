@@ -33,6 +33,7 @@ SOURCES = [
     "kernels_tree.cu",
     "kernels_body.cu",
     "kernels_sort.cu",
+    "kernels_diag.cu",
     "noalloc.cu",
     "engine.cpp",
     "capi.cpp",

@@ -172,6 +172,54 @@ int rfmm_profile_steps(rfmm_handle *h, uint32_t steps, float *kernel_ms, uint32_
  * CUDA graphs included). */
 int rfmm_launch_count(rfmm_handle *h, uint64_t *out);
 
+/* ---------------------------------------------------------------- accuracy
+ *
+ * Each runs a field solve of the current positions first (like
+ * rfmm_solve_fields) and does not advance the simulation.  FP64 is used only
+ * here: the direct-sum reference and the compensated reductions. */
+typedef struct rfmm_diagnostics {
+  double kinetic;             /* sum 1/2 m v^2, m = 1/N */
+  double potential;           /* sum 1/2 m phi, phi from the FMM expansion */
+  double total;
+  double momentum[3];         /* sum m v */
+  double angular_momentum[3]; /* sum m x cross v */
+} rfmm_diagnostics;
+
+/* FMM acceleration and potential per body (N x 4 floats: ax ay az phi) in
+ * the caller's order, as integrate applies them (wgsl:619-657). */
+int rfmm_accelerations(rfmm_handle *h, float *host_out, size_t bytes);
+/* Relative force error of the FMM against an FP64 softened direct sum
+ * (softening = params.softening, masses 1/N) on `targets` bodies sampled
+ * uniformly without replacement (seeded): rms = sqrt(sum|da|^2 / sum|a|^2). */
+int rfmm_force_error(rfmm_handle *h, uint32_t targets, uint64_t seed, double *rms_rel,
+                     double *max_rel);
+/* Energy and momentum with FP64 compensated (Neumaier) reductions. */
+int rfmm_get_diagnostics(rfmm_handle *h, rfmm_diagnostics *out);
+
+/* ------------------------------------------------------------------- tuning
+ *
+ * Launch shapes and scheduling of the step kernels.  Results never depend on
+ * them (every choice computes the same bits); only speed does.
+ * rfmm_autotune picks them by timing candidate settings on the resident
+ * scene (coordinate descent), which advances the simulation by the trial
+ * steps. */
+typedef struct rfmm_tuning {
+  uint32_t upward_ctas_per_sm;    /* persistent upward grid, 1..16 */
+  uint32_t m2l_ctas_per_sm;       /* persistent M2L grid, 1..6 */
+  uint32_t l2l_ctas_per_sm;       /* persistent L2L + near grid, 1..8 */
+  uint32_t integrate_ctas_per_sm; /* persistent integrate grid, 1..resident limit */
+  uint32_t integrate_dynamic;     /* 0: contiguous tile slices, 1: tiles from a counter */
+  uint32_t resort_interval;       /* steps between resident-order refreshes, 0 = never */
+  uint32_t graph_steps;           /* steps per captured CUDA graph, 1..64 */
+  uint32_t pdl;                   /* programmatic dependent launch between step kernels */
+} rfmm_tuning;
+
+int rfmm_get_tuning(rfmm_handle *h, rfmm_tuning *out);
+int rfmm_set_tuning(rfmm_handle *h, const rfmm_tuning *tuning);
+/* `steps_per_trial` steps are timed per candidate; the best setting is
+ * applied and returned in `best` (may be NULL). */
+int rfmm_autotune(rfmm_handle *h, uint32_t steps_per_trial, rfmm_tuning *best);
+
 /* ------------------------------------------------------------------ batches
  *
  * Many independent scenes of uneven size in one set of launches: every
@@ -206,6 +254,11 @@ int rfmm_batch_digest(rfmm_batch *b, uint32_t scene, int which, uint32_t *out);
 int rfmm_batch_launch_count(rfmm_batch *b, uint64_t *out);
 int rfmm_batch_profile_steps(rfmm_batch *b, uint32_t steps, float *kernel_ms, uint32_t *launches);
 int rfmm_batch_set_resort_interval(rfmm_batch *b, uint32_t steps);
+int rfmm_batch_get_tuning(rfmm_batch *b, rfmm_tuning *out);
+int rfmm_batch_set_tuning(rfmm_batch *b, const rfmm_tuning *tuning);
+int rfmm_batch_autotune(rfmm_batch *b, uint32_t steps_per_trial, rfmm_tuning *best);
+int rfmm_batch_force_error(rfmm_batch *b, uint32_t scene, uint32_t targets, uint64_t seed,
+                           double *rms_rel, double *max_rel);
 
 /* ------------------------------------------------------------------ serving
  *

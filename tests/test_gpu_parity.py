@@ -209,3 +209,33 @@ def test_golden_digests_on_gpu(rfmm_mod, oracle_mod):
             assert s.digest(R.BUF_FIELDS) == g["step_fields"], name
         checked += 1
     assert checked >= 1
+
+
+def test_tuning_never_changes_results(rfmm_mod, oracle_mod):
+    """Launch shapes, schedules, PDL and graph length change speed, not bits."""
+    O, R = oracle_mod, rfmm_mod
+    from rfmm import scenes
+    n = 60000
+    p = scenes.plummer(n, seed=21)
+    st = O.OracleState(p, _oracle_params(O, n))
+    st.step(6)
+    variants = [dict(), dict(integrate_dynamic=1, graph_steps=4, pdl=0),
+                dict(upward_ctas_per_sm=2, m2l_ctas_per_sm=1, l2l_ctas_per_sm=1,
+                     integrate_ctas_per_sm=1, resort_interval=3, graph_steps=1)]
+    for v in variants:
+        with _solver(R, n) as s:
+            t = s.tuning()
+            for k, val in v.items():
+                setattr(t, k, val)
+            s.set_tuning(t)
+            s.upload(p)
+            s.step(6)
+            _assert_same(s.particles(), st.particles, "particles %r" % v)
+            _assert_same(s.fields(), st.fields, "fields %r" % v)
+    with _solver(R, n) as s:
+        s.upload(p)
+        best = s.autotune(4)
+        assert 1 <= best.integrate_ctas_per_sm
+        s.upload(p)
+        s.step(6)
+        _assert_same(s.particles(), st.particles, "particles after autotune")
