@@ -176,6 +176,11 @@ int rfmm_set_resort_interval(rfmm_handle *h, uint32_t steps) {
   return h->engine->set_resort_interval(steps);
 }
 
+int rfmm_set_near_mode(rfmm_handle *h, uint32_t mode) {
+  if (guard(h)) return RFMM_ERR_INVALID;
+  return h->engine->set_near_mode(mode);
+}
+
 int rfmm_device_error(rfmm_handle *h, uint32_t *code, uint32_t *info) {
   if (guard(h)) return RFMM_ERR_INVALID;
   return h->engine->device_error(code, info);

@@ -141,6 +141,11 @@ int rfmm_batch_set_resort_interval(rfmm_batch *b, uint32_t steps) {
   return b->engine->set_resort_interval(steps);
 }
 
+int rfmm_batch_set_near_mode(rfmm_batch *b, uint32_t mode) {
+  if (bad(b)) return RFMM_ERR_INVALID;
+  return b->engine->set_near_mode(mode);
+}
+
 int rfmm_batch_force_error(rfmm_batch *b, uint32_t scene, uint32_t targets, uint64_t seed,
                            double *rms_rel, double *max_rel) {
   if (bad_scene(b, scene)) return RFMM_ERR_INVALID;

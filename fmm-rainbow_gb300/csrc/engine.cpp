@@ -429,6 +429,9 @@ LaunchCtx Engine::ctx(uint32_t mpar, uint32_t lpar, uint32_t ppar) const {
   L.tile_list = use_lists_ ? d_tile_list_ : nullptr;
   L.task_list = use_lists_ ? d_task_list_ : nullptr;
   L.pdl = pdl_;
+  L.p2p = near_mode_ == kNearP2P;
+  L.pos4 = d_pos4_;
+  L.starts_out = d_starts_;
   return L;
 }
 
@@ -569,9 +572,13 @@ int Engine::commit() {
   const int r = radix_sort(stream_, sort_, slots_, key_bits_);
   RF_CK(cudaMemsetAsync(d_mom_[mcur_], 0, 16ull * cells_, stream_));
   launch_gather(L, sort_.vals[r], d_part_[pcur_], d_ids_[pcur_], d_part_[pcur_ ^ 1u],
-                d_ids_[pcur_ ^ 1u], d_mom_[mcur_], tiles_, 0u);
-  RF_CK(cudaGetLastError());
+                d_ids_[pcur_ ^ 1u], d_mom_[mcur_], tiles_, 0u, d_pos4_);
   launches_ += resort_kernels();
+  if (near_mode_ == kNearP2P) {
+    launch_leaf_starts(L, sort_.keys[r], (uint32_t)scenes_.size());
+    launches_ += 1;
+  }
+  RF_CK(cudaGetLastError());
   pcur_ ^= 1u;
   committed_ = true;
   solved_ = false;
@@ -586,6 +593,48 @@ void Engine::enqueue_step(uint32_t mpar, uint32_t lpar, uint32_t ppar) {
   launch_m2l(L, lpar);
   launch_l2l_near(L, lpar);
   launch_integrate(L, tiles_);
+  if (near_mode_ == kNearP2P) enqueue_p2p_sort(mpar, lpar, ppar, d_mom_[mpar ^ 1u]);
+}
+
+void Engine::enqueue_p2p_sort(uint32_t mpar, uint32_t lpar, uint32_t ppar, uint4 *mom_into) {
+  // Sorting from the caller's order makes the order inside a leaf the caller
+  // order, whatever the history: the pair sums run in a fixed order.
+  LaunchCtx L = ctx(mpar, lpar, ppar);
+  launch_unpermute(L, d_ids_[ppar], d_part_[ppar ^ 1u], 0u, tiles_);
+  LaunchCtx C = ctx(mpar, lpar, ppar ^ 1u);
+  launch_keys(C, sort_.keys[0], sort_.vals[0], d_ids_[ppar ^ 1u], 1, tiles_, 0u);
+  const int r = radix_sort(stream_, sort_, slots_, key_bits_);
+  launch_gather(L, sort_.vals[r], d_part_[ppar ^ 1u], d_ids_[ppar ^ 1u], d_part_[ppar],
+                d_ids_[ppar], mom_into, tiles_, 0u, d_pos4_);
+  launch_leaf_starts(L, sort_.keys[r], (uint32_t)scenes_.size());
+}
+
+int Engine::set_near_mode(uint32_t mode) {
+  if (mode != kNearReference && mode != kNearP2P) return RFMM_ERR_INVALID;
+  if (use_lists_) return RFMM_ERR_INVALID;  // serving slots run the reference near field
+  for (const SceneDesc &d : scenes_)
+    if (d.key_level < d.depth) return RFMM_ERR_INVALID;
+  if (mode == near_mode_) return RFMM_OK;
+  if (mode == kNearP2P && d_pos4_ == nullptr) {
+    int st = alloc((void **)&d_pos4_, 16ull * slots_);
+    if (st == RFMM_OK) st = alloc((void **)&d_starts_, 4ull * cells_);
+    if (st != RFMM_OK) return st;
+  }
+  clear_graphs();
+  for (SceneDesc &d : scenes_) d.near_mode = mode;
+  RF_CK(cudaMemcpyAsync(d_scenes_, scenes_.data(), sizeof(SceneDesc) * scenes_.size(),
+                        cudaMemcpyHostToDevice, stream_));
+  near_mode_ = mode;
+  if (!committed_) return RFMM_OK;
+  // Re-sort the committed bodies for the new mode, starting from the caller's order.
+  LaunchCtx L = ctx(mcur_, lpar_, pcur_);
+  launch_unpermute(L, d_ids_[pcur_], d_part_[pcur_ ^ 1u], 0u, tiles_);
+  pcur_ ^= 1u;
+  for (const SceneDesc &d : scenes_)
+    if (d.n != 0u) launch_iota(stream_, d_ids_[pcur_] + d.body_off, pad_tiles(d.n) * kTile);
+  RF_CK(cudaGetLastError());
+  launches_ += 1u + (uint64_t)scenes_.size();
+  return commit();
 }
 
 int Engine::solve_fields() {
@@ -634,6 +683,12 @@ int Engine::launch_chunk(uint32_t len, bool sort_at_end) {
 
 int Engine::step(uint32_t steps) {
   if (!committed_) return RFMM_ERR_STATE;
+  while (steps > 0 && near_mode_ == kNearP2P) {  // every step ends with its own sort
+    const uint32_t len = std::min(steps, tuning_.graph_steps);
+    const int st = launch_chunk(len, false);
+    if (st != RFMM_OK) return st;
+    steps -= len;
+  }
   while (steps > 0) {
     if (resort_interval_ > 0 && since_sort_ >= resort_interval_) {
       enqueue_resort(pcur_);
@@ -754,6 +809,10 @@ int Engine::phase_times(float ms[7]) {
   RF_CK(cudaEventRecord(ev_[3], stream_));
   launch_integrate(L, tiles_);
   RF_CK(cudaEventRecord(ev_[4], stream_));
+  if (near_mode_ == kNearP2P) {
+    enqueue_p2p_sort(mcur_, lpar_, pcur_, d_mom_[mcur_ ^ 1u]);
+    launches_ += p2p_sort_kernels();
+  }
   RF_CK(cudaGetLastError());
   launches_ += 5;
   tree_buf_ = (int)mcur_;
@@ -802,7 +861,7 @@ int Engine::profile_steps(uint32_t steps, float ms[kKernelKinds], uint32_t launc
     if (e != cudaSuccess) st = cuda_status(e);
   };
   for (uint32_t s = 0; s < steps && st == RFMM_OK; s++) {
-    if (resort_interval_ > 0 && since_sort_ >= resort_interval_) {
+    if (near_mode_ == kNearReference && resort_interval_ > 0 && since_sort_ >= resort_interval_) {
       timed(kKResort, [&] { enqueue_resort(pcur_); });
       launches_ += resort_kernels();
       pcur_ ^= 1u;
@@ -813,6 +872,8 @@ int Engine::profile_steps(uint32_t steps, float ms[kKernelKinds], uint32_t launc
     timed(kKM2L, [&] { launch_m2l(L, lpar_); });
     timed(kKL2LNear, [&] { launch_l2l_near(L, lpar_); });
     timed(kKIntegrate, [&] { launch_integrate(L, tiles_); });
+    if (near_mode_ == kNearP2P)
+      timed(kKResort, [&] { enqueue_p2p_sort(mcur_, lpar_, pcur_, d_mom_[mcur_ ^ 1u]); });
     launches_ += kernels_per_step();
     tree_buf_ = (int)mcur_;
     mcur_ ^= 1u;
@@ -853,7 +914,7 @@ int Engine::diag_prepare(uint32_t scene, size_t doubles) {
   if (st != RFMM_OK) return st;
   const SceneDesc &d = scenes_[scene];
   LaunchCtx L = ctx(tree_buf_ < 0 ? mcur_ : (uint32_t)tree_buf_, lpar_, pcur_);
-  launch_accel(L, d_ids_[pcur_], d_accphi_ + d.body_off, d.tile_off, pad_tiles(d.n));
+  launch_accel(L, d_ids_[pcur_], d_accphi_, d.tile_off, pad_tiles(d.n));
   launch_unpermute(L, d_ids_[pcur_], d_part_[pcur_ ^ 1u], d.tile_off, pad_tiles(d.n));
   RF_CK(cudaGetLastError());
   launches_ += 2;

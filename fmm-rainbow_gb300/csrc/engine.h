@@ -88,7 +88,11 @@ class Engine {
   const SceneDesc &scene(uint32_t s) const { return scenes_[s]; }
   size_t buffer_bytes(uint32_t scene, int which) const;
   size_t device_bytes() const { return device_bytes_; }
-  uint32_t kernels_per_step() const { return 4u; }
+  uint32_t kernels_per_step() const { return near_mode_ == kNearP2P ? 4u + p2p_sort_kernels() : 4u; }
+  // Near-field mode of every scene (kNearReference / kNearP2P); a committed
+  // state is re-sorted for the new mode.
+  int set_near_mode(uint32_t mode);
+  uint32_t near_mode() const { return near_mode_; }
   uint32_t total_tiles() const { return tiles_; }
 
  private:
@@ -98,6 +102,13 @@ class Engine {
   LaunchCtx ctx(uint32_t mpar, uint32_t lpar, uint32_t ppar) const;
   void enqueue_step(uint32_t mpar, uint32_t lpar, uint32_t ppar);
   void enqueue_resort(uint32_t ppar);
+  // kNearP2P end of step: bodies back to caller order, leaf-key sort, gather
+  // with the deposit into `mom_into`, position snapshot and leaf starts.
+  void enqueue_p2p_sort(uint32_t mpar, uint32_t lpar, uint32_t ppar, uint4 *mom_into);
+  uint32_t p2p_sort_kernels() const { return 4u + 3u * ((key_bits_ + 7u) / 8u); }
+  uint32_t near_mode_ = kNearReference;
+  float4 *d_pos4_ = nullptr;      // kNearP2P: leaf-sorted positions
+  uint32_t *d_starts_ = nullptr;  // kNearP2P: per-leaf start slots
   int launch_chunk(uint32_t len, bool sort_at_end);
   int commit_scene(uint32_t scene);
   int rebuild_lists();

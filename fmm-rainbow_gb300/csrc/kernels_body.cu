@@ -28,6 +28,20 @@ __device__ __forceinline__ uint32_t leaf_cell(float x, float y, float z, uint32_
                                          cell_of_unit(unit_coord(z), dim), depth);
 }
 
+// 3-D Morton interleave of leaf coordinates (x in bit 0).
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {
+  v &= 0x3FFu;
+  v = (v | (v << 16)) & 0x030000FFu;
+  v = (v | (v << 8)) & 0x0300F00Fu;
+  v = (v | (v << 4)) & 0x030C30C3u;
+  v = (v | (v << 2)) & 0x09249249u;
+  return v;
+}
+
+__device__ __forceinline__ uint32_t morton3(uint32_t x, uint32_t y, uint32_t z) {
+  return spread3(x) | (spread3(y) << 1) | (spread3(z) << 2);
+}
+
 __device__ __forceinline__ float length3(float x, float y, float z) {
   return sqrtf((x * x + y * y) + z * z);
 }
@@ -45,11 +59,64 @@ __device__ __forceinline__ void soft_wall(float &p, float &v, float world_edge, 
   }
 }
 
-// FMM acceleration at a body (wgsl:619-657): adaptive descent to the sample
-// cell, local expansion about its centre, softened self-leaf monopole.  With
-// `phi`, also the potential of the same expansion (diagnostics only; integrate
-// never evaluates it).  Returns the sample cell's count.
+// Near-field P2P inputs: the leaf-sorted position snapshot, the per-leaf
+// start table (Morton order, absolute slots, 8^depth + 1 entries per scene at
+// the scene's cell offset) and the body's own slot.
+struct P2PView {
+  const float4 *pos;
+  const uint32_t *starts;
+  uint32_t self;
+};
+
+// Softened pair sums over the bodies of the 3x3x3 cells (level `l`) around
+// cell (cx, cy, cz): cells z-, y-, x-major from -1 to +1, bodies of a cell in
+// (leaf Morton code, caller id) order, the body itself skipped.
 template <bool kPhi>
+__device__ __forceinline__ void p2p_sums(const SceneDesc &S, const P2PView &V, uint32_t l,
+                                         uint32_t cx, uint32_t cy, uint32_t cz, float px, float py,
+                                         float pz, float &sx, float &sy, float &sz, float &sp) {
+  const int dim = 1 << l;
+  const uint32_t sh3 = 3u * (S.depth - l);
+  const float eps2 = S.softening * S.softening;
+  sx = 0.0f;
+  sy = 0.0f;
+  sz = 0.0f;
+  sp = 0.0f;
+  for (int oz = -1; oz <= 1; oz++) {
+    const int nz = (int)cz + oz;
+    if (nz < 0 || nz >= dim) continue;
+    for (int oy = -1; oy <= 1; oy++) {
+      const int ny = (int)cy + oy;
+      if (ny < 0 || ny >= dim) continue;
+      for (int ox = -1; ox <= 1; ox++) {
+        const int nx = (int)cx + ox;
+        if (nx < 0 || nx >= dim) continue;
+        const uint32_t m = morton3((uint32_t)nx, (uint32_t)ny, (uint32_t)nz);
+        const uint32_t lo = __ldg(&V.starts[S.cell_off + (m << sh3)]);
+        const uint32_t hi = __ldg(&V.starts[S.cell_off + ((m + 1u) << sh3)]);
+        for (uint32_t j = lo; j < hi; j++) {
+          if (j == V.self) continue;
+          const float4 q = __ldg(&V.pos[j]);
+          const float dx = q.x - px, dy = q.y - py, dz = q.z - pz;
+          const float r2 = ((dx * dx + dy * dy) + dz * dz) + eps2;
+          const float inv = 1.0f / sqrtf(r2);
+          const float w = (inv * inv) * inv;
+          sx = sx + dx * w;
+          sy = sy + dy * w;
+          sz = sz + dz * w;
+          if (kPhi) sp = sp + inv;
+        }
+      }
+    }
+  }
+}
+
+// FMM acceleration at a body (wgsl:619-657): adaptive descent to the sample
+// cell, local expansion about its centre, softened self-leaf monopole (or,
+// with kP2P, the exact near-field pair sums instead).  With `phi`, also the
+// potential of the same expansion (diagnostics only; integrate never
+// evaluates it).  Returns the sample cell's count.
+template <bool kPhi, bool kP2P = false>
 __device__ __forceinline__ uint32_t body_acceleration(const SceneDesc &S, float px, float py, float pz,
                                                       const uint4 *__restrict__ mom,
                                                       const float4 *__restrict__ src,
@@ -57,7 +124,7 @@ __device__ __forceinline__ uint32_t body_acceleration(const SceneDesc &S, float 
                                                       const uint32_t *__restrict__ choice,
                                                       const float *__restrict__ fields, float &ax,
                                                       float &ay, float &az, float &pulse,
-                                                      float *phi) {
+                                                      float *phi, const P2PView *V = nullptr) {
     const uint32_t D = S.depth;
     // Leaf coordinates; floor(u * 2^l) == floor(u * 2^D) >> (D - l).
     const uint32_t dimD = 1u << D;
@@ -99,6 +166,18 @@ __device__ __forceinline__ uint32_t body_acceleration(const SceneDesc &S, float 
     ay = fa.y + (fj0.y * rx + fj0.w * ry + fj1.x * rz);
     az = fa.z + (fj0.z * rx + fj1.x * ry + fj1.y * rz);
 
+    if (kP2P) {
+      float sx, sy, sz, sp;
+      p2p_sums<kPhi>(S, *V, chosen, lx >> csh, ly >> csh, lz >> csh, px, py, pz, sx, sy, sz, sp);
+      const float gm = S.gravity / S.n_f;
+      ax = ax + gm * sx;
+      ay = ay + gm * sy;
+      az = az + gm * sz;
+      if (kPhi) *phi = (fa.w - ((fa.x * rx + fa.y * ry) + fa.z * rz)) - gm * sp;
+      pulse = ax4.y;
+      return count;
+    }
+
     // Self leaf: softened monopole of the other count-1 bodies (wgsl:646-657).
     // x / 2^l == x * 2^-l exactly, so the eps division is a scaling.
     if (count > 1u) {
@@ -128,19 +207,21 @@ __device__ __forceinline__ uint32_t body_acceleration(const SceneDesc &S, float 
 
 // One body's integrate (wgsl:613-771).  Writes the new state into p0/p1 and
 // the new position's leaf cell and fixed-point coordinates (the next deposit).
+template <bool kP2P>
 __device__ __forceinline__ void integrate_body(const SceneDesc &S, float4 &p0, float4 &p1,
                                                const uint4 *__restrict__ mom,
                                                const float4 *__restrict__ src,
                                                const float4 *__restrict__ aux,
                                                const uint32_t *__restrict__ choice,
                                                const float *__restrict__ fields, uint32_t &key,
-                                               int32_t &qx, int32_t &qy, int32_t &qz) {
+                                               int32_t &qx, int32_t &qy, int32_t &qz,
+                                               const P2PView *V) {
     float px = p0.x, py = p0.y, pz = p0.z;
     float vx = p1.x, vy = p1.y, vz = p1.z;
     const uint32_t D = S.depth;
     float ax, ay, az, density_pulse;
-    const uint32_t count = body_acceleration<false>(S, px, py, pz, mom, src, aux, choice, fields, ax,
-                                                    ay, az, density_pulse, nullptr);
+    body_acceleration<false, kP2P>(S, px, py, pz, mom, src, aux, choice, fields, ax, ay, az,
+                                   density_pulse, nullptr, V);
 
     // Interactive control field (wgsl:659-689); off unless control_point.w > 0.5.
     float control_influence = 0.0f;
@@ -225,6 +306,10 @@ __device__ __forceinline__ void integrate_body(const SceneDesc &S, float4 &p0, f
 // (leaf-sorted, so its bodies are spatially compact), integrates every body
 // and accumulates the next step's deposit in a shared-memory table flushed
 // once at the end.
+//
+// kP2P: near field by exact pair sums over the leaf-sorted position snapshot;
+// no deposit (the end-of-step sort deposits the new positions).
+template <bool kP2P>
 __global__ void __launch_bounds__(256) k_integrate(const SceneDesc *__restrict__ scenes,
                                                    const uint32_t *__restrict__ tile_scene,
                                                    float4 *__restrict__ part,
@@ -235,11 +320,13 @@ __global__ void __launch_bounds__(256) k_integrate(const SceneDesc *__restrict__
                                                    const float *__restrict__ fields,
                                                    uint4 *__restrict__ mom_next, uint32_t tiles,
                                                    const uint32_t *__restrict__ tile_list,
-                                                   Counters *__restrict__ ctr, int dynamic) {
+                                                   Counters *__restrict__ ctr, int dynamic,
+                                                   const float4 *__restrict__ pos4,
+                                                   const uint32_t *__restrict__ starts) {
   __shared__ DepositTable T;
   __shared__ SceneDesc S;
   __shared__ uint32_t s_next;
-  T.clear();
+  if (!kP2P) T.clear();
   grid_dependency_wait();  // fields of this step are complete
   const uint32_t ntiles = tile_list != nullptr ? min(ctr->tiles_active, tiles) : tiles;
   // Static schedule: a contiguous slice per CTA.  Dynamic: tiles are taken
@@ -282,14 +369,17 @@ __global__ void __launch_bounds__(256) k_integrate(const SceneDesc *__restrict__
     uint32_t key = DepositTable::kEmpty;
     int32_t qx = 0, qy = 0, qz = 0;
     if (active) {
-      integrate_body(S, p0, p1, mom, src, aux, choice, fields, key, qx, qy, qz);
+      const P2PView V{pos4, starts, slot};
+      integrate_body<kP2P>(S, p0, p1, mom, src, aux, choice, fields, key, qx, qy, qz, &V);
       part[2u * slot] = p0;
       part[2u * slot + 1u] = p1;
     }
-    deposit_body(T, key, active, qx, qy, qz, mom_next);
+    if (!kP2P) deposit_body(T, key, active, qx, qy, qz, mom_next);
   }
-  __syncthreads();
-  T.flush(mom_next);
+  if (!kP2P) {
+    __syncthreads();
+    T.flush(mom_next);
+  }
   grid_dependents_may_launch();
 }
 
@@ -343,7 +433,9 @@ __global__ void __launch_bounds__(256) k_accel(const SceneDesc *__restrict__ sce
                                                const float4 *__restrict__ aux,
                                                const uint32_t *__restrict__ choice,
                                                const float *__restrict__ fields,
-                                               float4 *__restrict__ out, uint32_t tile_base) {
+                                               float4 *__restrict__ out, uint32_t tile_base,
+                                               const float4 *__restrict__ pos4,
+                                               const uint32_t *__restrict__ starts) {
   const uint32_t tile = tile_base + blockIdx.x;
   const SceneDesc &S = scenes[tile_scene[tile]];
   const uint32_t slot = tile * kTile + threadIdx.x;
@@ -352,24 +444,20 @@ __global__ void __launch_bounds__(256) k_accel(const SceneDesc *__restrict__ sce
   if (id >= S.n) return;
   const float4 p = part[2u * slot];
   float ax, ay, az, pulse, phi;
-  body_acceleration<true>(S, p.x, p.y, p.z, mom, src, aux, choice, fields, ax, ay, az, pulse, &phi);
-  out[id] = make_float4(ax, ay, az, phi);
+  if (S.near_mode == kNearP2P) {
+    const P2PView V{pos4, starts, slot};
+    body_acceleration<true, true>(S, p.x, p.y, p.z, mom, src, aux, choice, fields, ax, ay, az, pulse,
+                                  &phi, &V);
+  } else {
+    body_acceleration<true>(S, p.x, p.y, p.z, mom, src, aux, choice, fields, ax, ay, az, pulse, &phi);
+  }
+  out[S.body_off + id] = make_float4(ax, ay, az, phi);
 }
 
 void launch_accel(const LaunchCtx &L, const uint32_t *ids, float4 *out, uint32_t tile_base,
                   uint32_t tiles) {
   k_accel<<<tiles, kTile, 0, L.stream>>>(L.scenes, L.tile_scene, L.part, ids, L.mom, L.src, L.aux,
-                                         L.choice, L.fields, out, tile_base);
-}
-
-// 3-D Morton interleave of leaf coordinates (x in bit 0).
-__device__ __forceinline__ uint32_t spread3(uint32_t v) {
-  v &= 0x3FFu;
-  v = (v | (v << 16)) & 0x030000FFu;
-  v = (v | (v << 8)) & 0x0300F00Fu;
-  v = (v | (v << 4)) & 0x030C30C3u;
-  v = (v | (v << 2)) & 0x09249249u;
-  return v;
+                                         L.choice, L.fields, out, tile_base, L.pos4, L.starts_out);
 }
 
 __global__ void __launch_bounds__(256) k_keys(const SceneDesc *__restrict__ scenes,
@@ -385,7 +473,14 @@ __global__ void __launch_bounds__(256) k_keys(const SceneDesc *__restrict__ scen
   const uint32_t local = slot - S.body_off;
   const uint32_t F = S.key_level;
   uint32_t key = S.key_base | ((1u << (3u * F)) - 1u);  // padding sorts after its scene's bodies
-  if (local < S.n) {
+  if (local < S.n && S.near_mode == kNearP2P) {
+    // Leaf key only: bodies of a leaf keep their input (caller) order.
+    const float4 p = part[2u * slot];
+    const uint32_t dim = 1u << S.depth;
+    key = S.key_base | (morton3(cell_of_unit(unit_coord(p.x), dim), cell_of_unit(unit_coord(p.y), dim),
+                                cell_of_unit(unit_coord(p.z), dim))
+                        << (3u * (F - S.depth)));
+  } else if (local < S.n) {
     const float4 p = part[2u * slot];
     const uint32_t dim = 1u << F;
     // floor(u * 2^F) >> (F - depth) == floor(u * 2^depth): the fine key refines the leaf key.
@@ -409,7 +504,7 @@ __global__ void __launch_bounds__(256) k_gather(const SceneDesc *__restrict__ sc
                                                 float4 *__restrict__ part_out,
                                                 uint32_t *__restrict__ ids_out,
                                                 uint4 *__restrict__ deposit_into, uint32_t tiles,
-                                                uint32_t tile_base) {
+                                                uint32_t tile_base, float4 *__restrict__ pos_out) {
   __shared__ DepositTable T;
   __shared__ SceneDesc S;
   // Slots [tile_base * 256, (tile_base + tiles) * 256) are permuted among
@@ -430,6 +525,7 @@ __global__ void __launch_bounds__(256) k_gather(const SceneDesc *__restrict__ sc
     part_out[2u * slot] = p0;
     part_out[2u * slot + 1u] = p1;
     ids_out[slot] = ids_in[from];
+    if (pos_out != nullptr) pos_out[slot] = p0;
     if (deposit_into != nullptr) {
       const uint32_t sc = tile_scene[tile];
       if (sc != cur) {
@@ -588,7 +684,7 @@ __global__ void __launch_bounds__(256) k_initialize(const SceneDesc *__restrict_
 
 uint32_t body_ctas_per_sm() {
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_integrate, kTile, 0) != cudaSuccess || n < 1)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_integrate<false>, kTile, 0) != cudaSuccess || n < 1)
     n = 1;
   return (uint32_t)n;
 }
@@ -599,10 +695,11 @@ static uint32_t body_grid(const LaunchCtx &L, uint32_t tiles) {
 }
 
 void launch_integrate(const LaunchCtx &L, uint32_t tiles) {
-  launch_step_kernel(L, k_integrate, dim3(body_grid(L, tiles)), dim3(kTile), 0, L.scenes,
-                     L.tile_scene, L.part, (const uint4 *)L.mom, (const float4 *)L.src,
-                     (const float4 *)L.aux, (const uint32_t *)L.choice, (const float *)L.fields,
-                     L.mom_next, tiles, L.tile_list, L.ctr, L.integrate_dynamic ? 1 : 0);
+  launch_step_kernel(L, L.p2p ? k_integrate<true> : k_integrate<false>, dim3(body_grid(L, tiles)),
+                     dim3(kTile), 0, L.scenes, L.tile_scene, L.part, (const uint4 *)L.mom,
+                     (const float4 *)L.src, (const float4 *)L.aux, (const uint32_t *)L.choice,
+                     (const float *)L.fields, L.mom_next, tiles, L.tile_list, L.ctr,
+                     L.integrate_dynamic ? 1 : 0, L.pos4, (const uint32_t *)L.starts_out);
 }
 
 void launch_deposit(const LaunchCtx &L, uint4 *moments, uint32_t tiles) {
@@ -618,10 +715,40 @@ void launch_keys(const LaunchCtx &L, uint32_t *keys, uint32_t *vals, uint32_t *i
 
 void launch_gather(const LaunchCtx &L, const uint32_t *perm, const float4 *part_in,
                    const uint32_t *ids_in, float4 *part_out, uint32_t *ids_out, uint4 *deposit_into,
-                   uint32_t tiles, uint32_t tile_base) {
+                   uint32_t tiles, uint32_t tile_base, float4 *pos_out) {
   const uint32_t grid = deposit_into != nullptr ? body_grid(L, tiles) : tiles;
   k_gather<<<grid, kTile, 0, L.stream>>>(L.scenes, L.tile_scene, perm, part_in, ids_in, part_out,
-                                         ids_out, deposit_into, tiles, tile_base);
+                                         ids_out, deposit_into, tiles, tile_base, pos_out);
+}
+
+// Per-leaf body ranges of the leaf-sorted scenes (kNearP2P): entry m of a
+// scene's table (at its cell offset) is the first slot whose leaf Morton code
+// is >= m, for m in [0, 8^depth]; found by binary search in the sorted keys.
+__global__ void __launch_bounds__(256) k_leaf_starts(const SceneDesc *__restrict__ scenes,
+                                                     const uint32_t *__restrict__ keys,
+                                                     uint32_t *__restrict__ starts) {
+  const SceneDesc &S = scenes[blockIdx.y];
+  if (S.n == 0u || S.near_mode != kNearP2P) return;
+  const uint32_t leaves = 1u << (3u * S.depth);
+  for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m <= leaves; m += gridDim.x * blockDim.x) {
+    uint32_t lo = m < leaves ? 0u : S.n, hi = S.n;  // entry 8^depth ends the last leaf
+    if (m < leaves) {
+      const uint32_t target = S.key_base | (m << (3u * (S.key_level - S.depth)));
+      while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (keys[S.body_off + mid] < target) {
+          lo = mid + 1u;
+        } else {
+          hi = mid;
+        }
+      }
+    }
+    starts[S.cell_off + m] = S.body_off + lo;
+  }
+}
+
+void launch_leaf_starts(const LaunchCtx &L, const uint32_t *sorted_keys, uint32_t scenes) {
+  k_leaf_starts<<<dim3(64, scenes), 256, 0, L.stream>>>(L.scenes, sorted_keys, L.starts_out);
 }
 
 void launch_unpermute(const LaunchCtx &L, const uint32_t *ids, float4 *out, uint32_t tile_base,

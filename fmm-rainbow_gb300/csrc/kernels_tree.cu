@@ -504,7 +504,7 @@ __global__ void __launch_bounds__(256) k_l2l_near(const SceneDesc *__restrict__ 
     }
 
     const bool leaf = tcount <= kAdaptive || l == S.depth;  // wgsl:537-541
-    if (leaf) {
+    if (leaf && S.near_mode == kNearReference) {
       const float ctx = cell_center_lv(tx, l), cty = cell_center_lv(ty, l),
                   ctz = cell_center_lv(tz, l);
       const float near_eps = fmaxf(S.softening, (0.72f * kHalf) * pow2_neg(l));

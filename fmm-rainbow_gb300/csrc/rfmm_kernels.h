@@ -39,6 +39,9 @@ struct LaunchCtx {
   const uint32_t *tile_list;   // active body tiles (null: every tile)
   const uint32_t *task_list;   // active upward tasks (null: every task)
   bool pdl;                    // launch step kernels with programmatic stream serialization
+  bool p2p;                    // near field by exact pair sums (every scene in kNearP2P)
+  float4 *pos4;                // leaf-sorted position snapshot (kNearP2P)
+  uint32_t *starts_out;        // per-leaf start table (kNearP2P)
 };
 
 // Launch `kernel` on L.stream, with programmatic dependent launch when L.pdl:
@@ -82,9 +85,12 @@ void launch_deposit(const LaunchCtx &L, uint4 *moments, uint32_t tiles);
 void launch_keys(const LaunchCtx &L, uint32_t *keys, uint32_t *vals, uint32_t *ids, int fresh_ids,
                  uint32_t tiles, uint32_t tile_base);
 // Permute the bodies of tiles [tile_base, tile_base + tiles) (perm from index 0).
+// With `pos_out`, also writes each permuted body's position float4 there.
 void launch_gather(const LaunchCtx &L, const uint32_t *perm, const float4 *part_in,
                    const uint32_t *ids_in, float4 *part_out, uint32_t *ids_out, uint4 *deposit_into,
-                   uint32_t tiles, uint32_t tile_base);
+                   uint32_t tiles, uint32_t tile_base, float4 *pos_out = nullptr);
+// Leaf start tables of every kNearP2P scene from the sorted keys.
+void launch_leaf_starts(const LaunchCtx &L, const uint32_t *sorted_keys, uint32_t scenes);
 void launch_unpermute(const LaunchCtx &L, const uint32_t *ids, float4 *out, uint32_t tile_base,
                       uint32_t tiles);
 void launch_initialize(const LaunchCtx &L, float4 *part_out, uint32_t tile_base, uint32_t tiles);

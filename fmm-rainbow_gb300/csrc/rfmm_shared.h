@@ -9,6 +9,14 @@ namespace rfmm {
 // starts on a tile boundary, so a tile (one integrate CTA) never mixes scenes.
 constexpr uint32_t kTile = 256u;
 
+// Near-field modes.  Reference: 26 neighbour-cell monopoles at each adaptive
+// leaf's centre plus the self-cell monopole (wgsl:521-572, 646-657).  P2P:
+// neither; instead every body sums the exact softened pair forces of the
+// bodies in the 3x3x3 block of cells around its sample cell (an accuracy
+// mode without a reference counterpart).
+constexpr uint32_t kNearReference = 0u;
+constexpr uint32_t kNearP2P = 1u;
+
 // One independent scene (a plain solve is a batch of one scene).
 struct alignas(16) SceneDesc {
   uint32_t n;          // bodies (particle_count, wgsl:19)
@@ -32,7 +40,7 @@ struct alignas(16) SceneDesc {
   uint32_t key_level;  // level of the fine Morton cells the resident order sorts by (>= depth)
   uint32_t max_depth;  // deepest tree this scene's buffers hold (serving slots)
   uint32_t tile_cap;   // body tiles reserved for this scene
-  uint32_t pad_;
+  uint32_t near_mode;  // kNearReference or kNearP2P
 };
 static_assert(sizeof(SceneDesc) == 112, "SceneDesc layout");
 

@@ -30,6 +30,7 @@ STATUS = {
     -7: "kernel reported an error", -8: "request exceeds the memory budget",
 }
 BUF_PARTICLES, BUF_MOMENTS, BUF_FIELDS = 0, 1, 2
+NEAR_REFERENCE, NEAR_P2P = 0, 1
 PHASES = ("clear", "deposit", "upward", "m2l", "downward", "near", "integrate")
 
 # Every symbol the headers in include/ declare, with its ctypes signature.
@@ -126,6 +127,7 @@ SIGNATURES = {
     "rfmm_phase_times": (_i, [_vp, C.POINTER(_f32)]),
     "rfmm_check_finite": (_i, [_vp, _u32, C.POINTER(_u32), C.POINTER(_f32)]),
     "rfmm_set_resort_interval": (_i, [_vp, _u32]),
+    "rfmm_set_near_mode": (_i, [_vp, _u32]),
     "rfmm_device_error": (_i, [_vp, C.POINTER(_u32), C.POINTER(_u32)]),
     "rfmm_profile_steps": (_i, [_vp, _u32, C.POINTER(_f32), C.POINTER(_u32)]),
     "rfmm_launch_count": (_i, [_vp, C.POINTER(C.c_uint64)]),
@@ -148,6 +150,7 @@ SIGNATURES = {
     "rfmm_batch_launch_count": (_i, [_vp, C.POINTER(C.c_uint64)]),
     "rfmm_batch_profile_steps": (_i, [_vp, _u32, C.POINTER(_f32), C.POINTER(_u32)]),
     "rfmm_batch_set_resort_interval": (_i, [_vp, _u32]),
+    "rfmm_batch_set_near_mode": (_i, [_vp, _u32]),
     "rfmm_accelerations": (_i, [_vp, _vp, _sz]),
     "rfmm_force_error": (_i, [_vp, _u32, C.c_uint64, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "rfmm_get_diagnostics": (_i, [_vp, C.POINTER(Diagnostics)]),
@@ -308,6 +311,9 @@ class Solver:
     def set_resort_interval(self, steps: int):
         _check(lib().rfmm_set_resort_interval(self._h, steps), "rfmm_set_resort_interval")
 
+    def set_near_mode(self, mode: int):
+        _check(lib().rfmm_set_near_mode(self._h, mode), "rfmm_set_near_mode")
+
     def download(self, which: int = BUF_PARTICLES) -> np.ndarray:
         dtype, count = {BUF_PARTICLES: (PARTICLE_DTYPE, self.n), BUF_MOMENTS: (MOMENT_DTYPE, self.cells),
                         BUF_FIELDS: (FIELD_DTYPE, self.cells)}[which]
@@ -434,6 +440,9 @@ class Batch:
 
     def set_resort_interval(self, steps):
         _check(lib().rfmm_batch_set_resort_interval(self._h, steps), "rfmm_batch_set_resort_interval")
+
+    def set_near_mode(self, mode):
+        _check(lib().rfmm_batch_set_near_mode(self._h, mode), "rfmm_batch_set_near_mode")
 
     def upload(self, scene, particles):
         a = np.ascontiguousarray(particles)

@@ -148,6 +148,20 @@ int rfmm_check_finite(rfmm_handle *h, uint32_t probe, uint32_t *non_finite, floa
  * 64).  Results do not depend on it. */
 int rfmm_set_resort_interval(rfmm_handle *h, uint32_t steps);
 
+/* Near-field mode.  RFMM_NEAR_REFERENCE (default) is the reference's: 26
+ * neighbour-cell monopoles at each adaptive leaf's centre plus the self-cell
+ * monopole (wgsl:521-572, 646-657).  RFMM_NEAR_P2P has no reference
+ * counterpart: the fields carry M2L + L2L only, and each body adds the exact
+ * softened pair forces (softening = params.softening, masses 1/N) of every
+ * body in the 3x3x3 cells around its sample cell.  Every P2P step ends with a
+ * leaf sort from the caller's order, so the pair sums run in a fixed order
+ * (cells z-, y-, x-major; bodies by leaf, then caller index) and results are
+ * reproducible.  Switching re-sorts the uploaded bodies; positions and
+ * velocities are kept. */
+#define RFMM_NEAR_REFERENCE 0u
+#define RFMM_NEAR_P2P 1u
+int rfmm_set_near_mode(rfmm_handle *h, uint32_t mode);
+
 /* Last kernel error word (0 = none) and its detail. */
 int rfmm_device_error(rfmm_handle *h, uint32_t *code, uint32_t *info);
 
@@ -254,6 +268,7 @@ int rfmm_batch_digest(rfmm_batch *b, uint32_t scene, int which, uint32_t *out);
 int rfmm_batch_launch_count(rfmm_batch *b, uint64_t *out);
 int rfmm_batch_profile_steps(rfmm_batch *b, uint32_t steps, float *kernel_ms, uint32_t *launches);
 int rfmm_batch_set_resort_interval(rfmm_batch *b, uint32_t steps);
+int rfmm_batch_set_near_mode(rfmm_batch *b, uint32_t mode);
 int rfmm_batch_get_tuning(rfmm_batch *b, rfmm_tuning *out);
 int rfmm_batch_set_tuning(rfmm_batch *b, const rfmm_tuning *tuning);
 int rfmm_batch_autotune(rfmm_batch *b, uint32_t steps_per_trial, rfmm_tuning *best);

@@ -39,6 +39,7 @@ class OParams(C.Structure):
         ("control_axis_mode", C.c_float * 4),
         ("control_strength", C.c_float),
         ("control_radius", C.c_float),
+        ("near_mode", C.c_uint32),  # 0 reference near field, 1 exact P2P
     ]
 
 
@@ -100,7 +101,7 @@ def plan(n: int):
 
 def make_params(n, dt=0.0009, gravity=0.34, softening=0.012, speed=1.0, depth=None, scale=None,
                 control_point=(0.0, 0.0, 0.0, 0.0), control_axis_mode=(0.0, 0.0, 0.0, 0.0),
-                control_strength=0.7, control_radius=0.22) -> OParams:
+                control_strength=0.7, control_radius=0.22, near_mode=0) -> OParams:
     """Params with the native harness's defaults (native/main.rs:57-81)."""
     d, _, s = plan(n)
     p = OParams()
@@ -111,6 +112,7 @@ def make_params(n, dt=0.0009, gravity=0.34, softening=0.012, speed=1.0, depth=No
     p.control_point[:] = control_point
     p.control_axis_mode[:] = control_axis_mode
     p.control_strength, p.control_radius = control_strength, control_radius
+    p.near_mode = near_mode
     return p
 
 

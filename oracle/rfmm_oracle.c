@@ -90,7 +90,10 @@ typedef struct {
   float control_axis_mode[4];
   float control_strength; /* control_settings.x */
   float control_radius;   /* control_settings.y */
+  uint32_t near_mode;     /* 0: reference near field; 1: exact P2P (no reference counterpart) */
 } OParams;
+
+#define O_NEAR_P2P 1u
 
 /* ---------------------------------------------------------------- planner */
 
@@ -460,11 +463,90 @@ static float fractf(float x) { return x - floorf(x); }
 
 static float length3(const float v[3]) { return sqrtf((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]); }
 
+/* ---------------------------------------------------- P2P near field */
+
+/* The near-field P2P mode (no reference counterpart): the fields carry M2L
+ * and L2L only, and each body adds the exact softened pair forces of every
+ * body in the 3x3x3 cells around its sample cell.  Bodies are visited cell by
+ * cell (z-, y-, x-major offsets -1..1) and, inside a cell, by the Morton code
+ * of their leaf (x in bit 0) and then by index. */
+typedef struct {
+  const OParticle *snap; /* positions the sums read (the state before the step) */
+  uint32_t *order;       /* body indices sorted by (leaf Morton code, index) */
+  uint32_t *starts;      /* 8^depth + 1 entries: first rank of each leaf code */
+} ONear;
+
+static uint32_t spread3(uint32_t v) {
+  uint32_t r = 0;
+  for (uint32_t b = 0; b < 10u; b++) r |= ((v >> b) & 1u) << (3u * b);
+  return r;
+}
+
+static uint32_t morton3(const uint32_t c[3]) {
+  return spread3(c[0]) | (spread3(c[1]) << 1) | (spread3(c[2]) << 2);
+}
+
+static void near_build(const OParticle *particles, const OParams *P, ONear *nr) {
+  const uint32_t n = P->n, depth = P->depth, dim = 1u << depth, leaves = 1u << (3u * depth);
+  uint32_t *code = (uint32_t *)malloc(sizeof(uint32_t) * (n ? n : 1u));
+  nr->snap = particles;
+  nr->order = (uint32_t *)malloc(sizeof(uint32_t) * (n ? n : 1u));
+  nr->starts = (uint32_t *)calloc(leaves + 1u, sizeof(uint32_t));
+  for (uint32_t i = 0; i < n; i++) {
+    float pos[3] = {particles[i].px, particles[i].py, particles[i].pz};
+    uint32_t c[3];
+    position_cell(pos, dim, c);
+    code[i] = morton3(c);
+    nr->starts[code[i] + 1u]++;
+  }
+  for (uint32_t m = 0; m < leaves; m++) nr->starts[m + 1u] += nr->starts[m];
+  uint32_t *fill = (uint32_t *)malloc(sizeof(uint32_t) * leaves);
+  memcpy(fill, nr->starts, sizeof(uint32_t) * leaves);
+  for (uint32_t i = 0; i < n; i++) nr->order[fill[code[i]]++] = i; /* stable: by index */
+  free(fill);
+  free(code);
+}
+
+static void near_free(ONear *nr) {
+  free(nr->order);
+  free(nr->starts);
+}
+
+/* Sums over the 3x3x3 cells at `level` around cell c; gm * sum is added. */
+static void near_p2p(const ONear *nr, const OParams *P, uint32_t self, const float pos[3],
+                     uint32_t level, const uint32_t c[3], float s[3]) {
+  const int dim = 1 << level;
+  const uint32_t sh3 = 3u * (P->depth - level);
+  const float eps2 = P->softening * P->softening;
+  s[0] = s[1] = s[2] = 0.0f;
+  for (int oz = -1; oz <= 1; oz++)
+    for (int oy = -1; oy <= 1; oy++)
+      for (int ox = -1; ox <= 1; ox++) {
+        const int nx = (int)c[0] + ox, ny = (int)c[1] + oy, nz = (int)c[2] + oz;
+        if (nx < 0 || ny < 0 || nz < 0 || nx >= dim || ny >= dim || nz >= dim) continue;
+        const uint32_t nc[3] = {(uint32_t)nx, (uint32_t)ny, (uint32_t)nz};
+        const uint32_t m = morton3(nc);
+        const uint32_t lo = nr->starts[m << sh3], hi = nr->starts[(m + 1u) << sh3];
+        for (uint32_t k = lo; k < hi; k++) {
+          const uint32_t j = nr->order[k];
+          if (j == self) continue;
+          const OParticle *q = &nr->snap[j];
+          const float d[3] = {q->px - pos[0], q->py - pos[1], q->pz - pos[2]};
+          const float r2 = ((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]) + eps2;
+          const float inv = 1.0f / sqrtf(r2);
+          const float w = (inv * inv) * inv;
+          for (int a = 0; a < 3; a++) s[a] = s[a] + d[a] * w;
+        }
+      }
+}
+
 /* The FMM acceleration integrate applies before the control field
- * (wgsl:619-657): adaptive descent, local expansion, self-leaf monopole.
- * Returns the chosen cell's count. */
+ * (wgsl:619-657): adaptive descent, local expansion, self-leaf monopole (or,
+ * with `nr`, the P2P near field of body `self`).  Returns the chosen cell's
+ * count. */
 static uint32_t fmm_acceleration(const OParticle *particle, const OMoment *moments,
-                                 const OField *fields, const OParams *P, float acc[3]) {
+                                 const OField *fields, const OParams *P, float acc[3],
+                                 const ONear *nr, uint32_t self) {
   const uint32_t depth = P->depth;
   float pos[3] = {particle->px, particle->py, particle->pz};
   uint32_t chosen_dim = 1u << depth, chosen_cell[3], cell_index;
@@ -492,6 +574,15 @@ static uint32_t fmm_acceleration(const OParticle *particle, const OMoment *momen
   for (int k = 0; k < 3; k++) acc[k] = field->a[k] + jm[k];
 
   const uint32_t count = moments[cell_index].count;
+  if (nr != NULL) {
+    uint32_t level = 0;
+    while ((1u << level) != chosen_dim) level++;
+    float s[3];
+    near_p2p(nr, P, self, pos, level, chosen_cell, s);
+    const float gm = P->gravity / (float)P->n;
+    for (int k = 0; k < 3; k++) acc[k] = acc[k] + gm * s[k];
+    return count;
+  }
   if (count > 1u) {
     float com[3], delta[3];
     moment_com(&moments[cell_index], count, P->scale, com);
@@ -510,20 +601,36 @@ static uint32_t fmm_acceleration(const OParticle *particle, const OMoment *momen
 /* FMM accelerations of every body (no update). */
 void oracle_accelerations(const OParticle *particles, const OMoment *moments, const OField *fields,
                           const OParams *P, float *acc_out) {
-#pragma omp parallel for schedule(static) if (P->n >= 8192u)
-  for (int64_t i = 0; i < (int64_t)P->n; i++) fmm_acceleration(&particles[i], moments, fields, P, &acc_out[3 * i]);
+  ONear nr;
+  const int p2p = P->near_mode == O_NEAR_P2P;
+  if (p2p) near_build(particles, P, &nr);
+#pragma omp parallel for schedule(dynamic, 256) if (P->n >= 8192u)
+  for (int64_t i = 0; i < (int64_t)P->n; i++)
+    fmm_acceleration(&particles[i], moments, fields, P, &acc_out[3 * i], p2p ? &nr : NULL,
+                     (uint32_t)i);
+  if (p2p) near_free(&nr);
 }
 
 void oracle_integrate(OParticle *particles, const OMoment *moments, const OField *fields,
                       const OParams *P) { /* wgsl:613-771 */
   const uint32_t n = P->n;
-#pragma omp parallel for schedule(static) if (n >= 8192u)
+  /* P2P reads every body's pre-step position: sums run on a snapshot. */
+  ONear nr;
+  OParticle *snap = NULL;
+  const int p2p = P->near_mode == O_NEAR_P2P;
+  if (p2p) {
+    snap = (OParticle *)malloc(sizeof(OParticle) * (n ? n : 1u));
+    memcpy(snap, particles, sizeof(OParticle) * n);
+    near_build(snap, P, &nr);
+  }
+#pragma omp parallel for schedule(dynamic, 256) if (n >= 8192u)
   for (int64_t ii = 0; ii < (int64_t)n; ii++) {
     OParticle particle = particles[ii];
     float pos[3] = {particle.px, particle.py, particle.pz};
     float velocity[3] = {particle.vx, particle.vy, particle.vz};
     float acc[3];
-    const uint32_t count = fmm_acceleration(&particle, moments, fields, P, acc);
+    const uint32_t count =
+        fmm_acceleration(&particle, moments, fields, P, acc, p2p ? &nr : NULL, (uint32_t)ii);
 
     float control_influence = 0.0f;
     if (P->control_point[3] > 0.5f) { /* wgsl:659-689 */
@@ -599,6 +706,10 @@ void oracle_integrate(OParticle *particles, const OMoment *moments, const OField
     particle.vz = velocity[2];
     particle.exc = excitation;
     particles[ii] = particle;
+  }
+  if (p2p) {
+    near_free(&nr);
+    free(snap);
   }
 }
 
@@ -727,7 +838,7 @@ void oracle_solve_fields(const OParticle *particles, OMoment *moments, OField *f
   oracle_upward(moments, P);
   oracle_m2l_all(moments, fields, P);
   oracle_downward(moments, fields, P);
-  oracle_near_all(moments, fields, P);
+  if (P->near_mode != O_NEAR_P2P) oracle_near_all(moments, fields, P);
 }
 
 /* `steps` full solver frames (native/main.rs:411-421). */
