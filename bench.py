@@ -71,6 +71,7 @@ WORKLOADS = {
 PEAKS_FILE = os.path.join(REPO, "MEASURED_PEAKS.json")
 TRAFFIC_FILE = os.path.join(REPO, "profiles", "ncu_traffic.json")
 FALLBACK_HBM_GBS = 6800.0
+P2P_MAX_BODIES = 1 << 18
 
 
 def parse_args():
@@ -86,6 +87,8 @@ def parse_args():
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--requests", type=int, default=0, help="served: requests per rate point")
     ap.add_argument("--rates", type=float, nargs="*", default=None, help="served: arrival rates /s")
+    ap.add_argument("--near", default="reference", choices=["reference", "p2p"],
+                    help="near field: the reference's cell monopoles, or exact pair sums")
     return ap.parse_args()
 
 
@@ -180,24 +183,32 @@ def traffic_for(workload):
         return None
 
 
-def cpu_baseline(w, seconds, threads=None):
-    """The CPU oracle (the reference algorithm restated in C, OpenMP) on this host."""
-    import numpy as np  # noqa: F401
+def cpu_baseline(w, seconds, near="reference"):
+    """The CPU oracle (the reference algorithm restated in C, OpenMP) on this
+    host: all host threads, then one thread on a shorter sample."""
     from oracle import oracle as O
-    cores = O.set_threads(threads or os.cpu_count() or 1)
     scene = make_scene(w)
-    st = O.OracleState(scene, O.make_params(w["n"], gravity=w["G"], softening=w["eps"], dt=w["dt"]))
-    st.step(1)  # warm
-    done, t0 = 0, time.perf_counter()
-    while True:
-        st.step(1)
-        done += 1
-        el = time.perf_counter() - t0
-        if el >= seconds or done >= w["fmm_steps"]:
-            break
-    return {"value": w["n"] * done / el, "unit": "body-steps/s", "cores": cores, "kind": "port",
-            "sample": "%d FMM step(s) of the %s workload (%d bodies) on %d host threads, %.1f s"
-                      % (done, "same", w["n"], cores, el)}
+
+    def sample(threads, budget):
+        cores = O.set_threads(threads)
+        st = O.OracleState(scene, O.make_params(w["n"], gravity=w["G"], softening=w["eps"], dt=w["dt"],
+                                                near_mode=1 if near == "p2p" else 0))
+        done, t0 = 0, time.perf_counter()
+        while True:
+            st.step(1)
+            done += 1
+            el = time.perf_counter() - t0
+            if el >= budget or done >= w["fmm_steps"]:
+                break
+        return w["n"] * done / el, cores, done, el
+
+    value, cores, done, el = sample(os.cpu_count() or 1, seconds)
+    v1, _, d1, e1 = sample(1, seconds / 3.0)
+    O.set_threads(os.cpu_count() or 1)
+    return {"value": value, "unit": "body-steps/s", "cores": cores, "kind": "port",
+            "sample": "%d FMM step(s) of the same workload (%d bodies, %s near field) on %d host "
+                      "threads, %.1f s" % (done, w["n"], near, cores, el),
+            "single_thread": {"value": v1, "sample": "%d step(s), %.1f s" % (d1, e1)}}
 
 
 def run_reference(args, w):
@@ -258,6 +269,9 @@ def run_gpu(args, w):
     import rfmm
 
     n, fmm_steps = w["n"], w["fmm_steps"]
+    if args.near == "p2p" and n > P2P_MAX_BODIES:
+        raise SystemExit("--near p2p: at most %d bodies (the depth-6 cap leaves Plummer cores with "
+                         "thousands of bodies per leaf, ~1e5 pairs per body)" % P2P_MAX_BODIES)
     scene = make_scene(w)
     params = rfmm.default_params(gravity=w["G"], softening=w["eps"], dt=w["dt"])
     # A real (non-default) stream shared by torch's events/flush and the solver.
@@ -265,6 +279,8 @@ def run_gpu(args, w):
     torch.cuda.set_stream(stream)
     solver = rfmm.Solver(n, params)
     solver.set_stream(stream.cuda_stream)
+    if args.near == "p2p":
+        solver.set_near_mode(rfmm.NEAR_P2P)
     pristine = torch.from_numpy(scene.view(np.uint8).copy()).cuda()
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
 
@@ -342,10 +358,16 @@ def run_gpu(args, w):
     # FP64 direct-sum force error on a seeded target sample, FP64 energy.
     rms, mx = solver.force_error(4096, 1)
     diag = solver.diagnostics()
-    accuracy = {"force_rms_rel": rms, "force_max_rel": mx, "targets": min(4096, n),
+    accuracy = {"near_field": args.near, "force_rms_rel": rms, "force_max_rel": mx,
+                "targets": min(4096, n),
                 "reference": "FP64 softened direct sum on the GPU (all N sources)",
                 "energy_total": diag["total"], "kinetic": diag["kinetic"],
                 "potential": diag["potential"]}
+    if args.near == "reference":  # the same final state with exact near-field pair sums
+        solver.set_near_mode(rfmm.NEAR_P2P)
+        prms, pmx = solver.force_error(4096, 1)
+        accuracy["p2p_mode"] = {"force_rms_rel": prms, "force_max_rel": pmx}
+        solver.set_near_mode(rfmm.NEAR_REFERENCE)
 
     line = {
         "metric": "body-steps/s", "value": value, "unit": "body-steps/s", "n_gpus": world,
@@ -353,6 +375,7 @@ def run_gpu(args, w):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded, numpy PCG64): " + w["desc"],
         "config": {"workload": args.workload, "form": "plain single-scene solve",
+                   "near_field": args.near,
                    "bodies": n, "fmm_steps_per_bench_step": fmm_steps, "depth": solver.depth,
                    "cells": solver.cells, "fixed_point_scale": solver.scale,
                    "l2": "flushed between timed steps (512 MiB write outside the events)",
@@ -361,7 +384,7 @@ def run_gpu(args, w):
         "kernel_avg_ms": kernel_ms, "tuning": tuning.as_dict(), "accuracy": accuracy,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds)
+        line["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds, args.near)
     if rank == 0:
         print(json.dumps(line), flush=True)
     solver.close()

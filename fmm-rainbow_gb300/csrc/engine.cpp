@@ -897,10 +897,11 @@ int Engine::profile_steps(uint32_t steps, float ms[kKernelKinds], uint32_t launc
   return check_device_error();
 }
 
-int Engine::diag_prepare(uint32_t scene, size_t doubles) {
+int Engine::diag_prepare(uint32_t scene, size_t doubles, bool all_bodies) {
   if (scene >= scenes_.size() || !committed_) return RFMM_ERR_STATE;
   if (d_accphi_ == nullptr) {
-    const int st = alloc((void **)&d_accphi_, 16ull * slots_);
+    int st = alloc((void **)&d_accphi_, 16ull * slots_);
+    if (st == RFMM_OK) st = alloc((void **)&d_slot_of_, 4ull * slots_);
     if (st != RFMM_OK) return st;
   }
   if (doubles > diag_doubles_) {
@@ -914,16 +915,16 @@ int Engine::diag_prepare(uint32_t scene, size_t doubles) {
   if (st != RFMM_OK) return st;
   const SceneDesc &d = scenes_[scene];
   LaunchCtx L = ctx(tree_buf_ < 0 ? mcur_ : (uint32_t)tree_buf_, lpar_, pcur_);
-  launch_accel(L, d_ids_[pcur_], d_accphi_, d.tile_off, pad_tiles(d.n));
+  if (all_bodies) launch_accel(L, d_ids_[pcur_], d_accphi_, d.tile_off, pad_tiles(d.n));
   launch_unpermute(L, d_ids_[pcur_], d_part_[pcur_ ^ 1u], d.tile_off, pad_tiles(d.n));
   RF_CK(cudaGetLastError());
-  launches_ += 2;
+  launches_ += all_bodies ? 2u : 1u;
   return RFMM_OK;
 }
 
 int Engine::accelerations(uint32_t scene, float *host_out) {
   if (host_out == nullptr) return RFMM_ERR_INVALID;
-  const int st = diag_prepare(scene, 0);
+  const int st = diag_prepare(scene, 0, true);
   if (st != RFMM_OK) return st;
   const SceneDesc &d = scenes_[scene];
   RF_CK(cudaMemcpyAsync(host_out, d_accphi_ + d.body_off, 16ull * d.n, cudaMemcpyDeviceToHost,
@@ -939,7 +940,7 @@ int Engine::force_error(uint32_t scene, uint32_t targets, uint64_t seed, double 
   const uint32_t splits = 64u;
   // doubles: partial [splits][nt][3], reference [nt][3], and the target ids.
   const size_t doubles = (size_t)splits * nt * 3u + (size_t)nt * 3u + nt;
-  int st = diag_prepare(scene, doubles);
+  int st = diag_prepare(scene, doubles, false);
   if (st != RFMM_OK) return st;
   // Uniform sample without replacement (splitmix64 partial Fisher-Yates).
   std::vector<uint32_t> idx(d.n);
@@ -958,23 +959,27 @@ int Engine::force_error(uint32_t scene, uint32_t targets, uint64_t seed, double 
   double *ref = d_diag_ + (size_t)splits * nt * 3u;
   uint32_t *tgt = reinterpret_cast<uint32_t *>(ref + (size_t)nt * 3u);
   RF_CK(cudaMemcpyAsync(tgt, idx.data(), 4ull * nt, cudaMemcpyHostToDevice, stream_));
+  {
+    LaunchCtx L = ctx(tree_buf_ < 0 ? mcur_ : (uint32_t)tree_buf_, lpar_, pcur_);
+    launch_accel_targets(L, scene, d.tile_off, pad_tiles(d.n), d_ids_[pcur_], d_slot_of_, tgt, nt,
+                         d_accphi_);
+    launches_ += 2;
+  }
   launch_direct_sum_f64(stream_, d_part_[pcur_ ^ 1u] + 2ull * d.body_off, d.n, tgt, nt,
                         (double)d.gravity, (double)d.softening, partial, splits, ref);
   RF_CK(cudaGetLastError());
   launches_ += 2;
   std::vector<double> href((size_t)nt * 3u);
-  std::vector<float> acc((size_t)d.n * 4u);
+  std::vector<float> acc((size_t)nt * 4u);
   RF_CK(cudaMemcpyAsync(href.data(), ref, 8ull * nt * 3u, cudaMemcpyDeviceToHost, stream_));
-  RF_CK(cudaMemcpyAsync(acc.data(), d_accphi_ + d.body_off, 16ull * d.n, cudaMemcpyDeviceToHost,
-                        stream_));
+  RF_CK(cudaMemcpyAsync(acc.data(), d_accphi_, 16ull * nt, cudaMemcpyDeviceToHost, stream_));
   st = sync();
   if (st != RFMM_OK) return st;
   double num = 0.0, den = 0.0, mx = 0.0;
   for (uint32_t t = 0; t < nt; t++) {
-    const uint32_t i = idx[t];
     double e2 = 0.0, r2 = 0.0;
     for (int k = 0; k < 3; k++) {
-      const double df = (double)acc[4u * i + k] - href[3u * t + k];
+      const double df = (double)acc[4u * t + k] - href[3u * t + k];
       e2 += df * df;
       r2 += href[3u * t + k] * href[3u * t + k];
     }
@@ -990,7 +995,7 @@ int Engine::force_error(uint32_t scene, uint32_t targets, uint64_t seed, double 
 int Engine::diagnostics(uint32_t scene, double out[9]) {
   if (out == nullptr) return RFMM_ERR_INVALID;
   const uint32_t blocks = 4u * (uint32_t)sms_;
-  int st = diag_prepare(scene, 9u * blocks + 9u);
+  int st = diag_prepare(scene, 9u * blocks + 9u, true);
   if (st != RFMM_OK) return st;
   const SceneDesc &d = scenes_[scene];
   launch_diagnostics(stream_, d_part_[pcur_ ^ 1u] + 2ull * d.body_off, d_accphi_ + d.body_off, d.n,

@@ -139,7 +139,8 @@ class Engine {
   float4 *d_accphi_ = nullptr;    // diagnostics: per-body acceleration + potential
   double *d_diag_ = nullptr;      // diagnostics: FP64 partial sums
   size_t diag_doubles_ = 0;
-  int diag_prepare(uint32_t scene, size_t doubles);
+  uint32_t *d_slot_of_ = nullptr;  // diagnostics: caller id -> resident slot
+  int diag_prepare(uint32_t scene, size_t doubles, bool all_bodies);
   float4 *d_src_ = nullptr;
   float4 *d_aux_ = nullptr;
   uint32_t *d_tile_list_ = nullptr, *d_task_list_ = nullptr;

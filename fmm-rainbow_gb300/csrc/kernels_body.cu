@@ -454,6 +454,51 @@ __global__ void __launch_bounds__(256) k_accel(const SceneDesc *__restrict__ sce
   out[S.body_off + id] = make_float4(ax, ay, az, phi);
 }
 
+// Resident slot of every body of one scene: slot_of[body_off + id] = slot.
+__global__ void __launch_bounds__(256) k_slot_of(const SceneDesc *__restrict__ scenes,
+                                                 const uint32_t *__restrict__ tile_scene,
+                                                 const uint32_t *__restrict__ ids,
+                                                 uint32_t *__restrict__ slot_of, uint32_t tile_base) {
+  const uint32_t tile = tile_base + blockIdx.x;
+  const SceneDesc &S = scenes[tile_scene[tile]];
+  const uint32_t slot = tile * kTile + threadIdx.x;
+  if (slot - S.body_off >= S.n) return;
+  const uint32_t id = ids[slot];
+  if (id < S.n) slot_of[S.body_off + id] = slot;
+}
+
+// FMM acceleration + potential of selected bodies (caller ids) of one scene.
+__global__ void __launch_bounds__(256) k_accel_targets(
+    const SceneDesc *__restrict__ scenes, uint32_t scene, const float4 *__restrict__ part,
+    const uint32_t *__restrict__ slot_of, const uint32_t *__restrict__ targets, uint32_t nt,
+    const uint4 *__restrict__ mom, const float4 *__restrict__ src, const float4 *__restrict__ aux,
+    const uint32_t *__restrict__ choice, const float *__restrict__ fields, float4 *__restrict__ out,
+    const float4 *__restrict__ pos4, const uint32_t *__restrict__ starts) {
+  const SceneDesc &S = scenes[scene];
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nt || targets[t] >= S.n) return;
+  const uint32_t slot = slot_of[S.body_off + targets[t]];
+  const float4 p = part[2u * slot];
+  float ax, ay, az, pulse, phi;
+  if (S.near_mode == kNearP2P) {
+    const P2PView V{pos4, starts, slot};
+    body_acceleration<true, true>(S, p.x, p.y, p.z, mom, src, aux, choice, fields, ax, ay, az, pulse,
+                                  &phi, &V);
+  } else {
+    body_acceleration<true>(S, p.x, p.y, p.z, mom, src, aux, choice, fields, ax, ay, az, pulse, &phi);
+  }
+  out[t] = make_float4(ax, ay, az, phi);
+}
+
+void launch_accel_targets(const LaunchCtx &L, uint32_t scene, uint32_t tile_base, uint32_t tiles,
+                          const uint32_t *ids, uint32_t *slot_of, const uint32_t *targets,
+                          uint32_t nt, float4 *out) {
+  k_slot_of<<<tiles, kTile, 0, L.stream>>>(L.scenes, L.tile_scene, ids, slot_of, tile_base);
+  k_accel_targets<<<(nt + 255u) / 256u, 256, 0, L.stream>>>(
+      L.scenes, scene, L.part, slot_of, targets, nt, L.mom, L.src, L.aux, L.choice, L.fields, out,
+      L.pos4, L.starts_out);
+}
+
 void launch_accel(const LaunchCtx &L, const uint32_t *ids, float4 *out, uint32_t tile_base,
                   uint32_t tiles) {
   k_accel<<<tiles, kTile, 0, L.stream>>>(L.scenes, L.tile_scene, L.part, ids, L.mom, L.src, L.aux,

@@ -99,6 +99,11 @@ uint32_t body_ctas_per_sm();  // resident 256-thread CTAs per SM of the persiste
 // FMM acceleration + potential per body of tiles [tile_base, +tiles), caller order.
 void launch_accel(const LaunchCtx &L, const uint32_t *ids, float4 *out, uint32_t tile_base,
                   uint32_t tiles);
+// The same for `nt` bodies of one scene given by caller id (out[t] for
+// targets[t]); slot_of (one entry per slot) receives the id -> slot map.
+void launch_accel_targets(const LaunchCtx &L, uint32_t scene, uint32_t tile_base, uint32_t tiles,
+                          const uint32_t *ids, uint32_t *slot_of, const uint32_t *targets,
+                          uint32_t nt, float4 *out);
 
 // FP64 diagnostics (kernels_diag.cu).
 void launch_direct_sum_f64(cudaStream_t stream, const float4 *part_caller, uint32_t n,
