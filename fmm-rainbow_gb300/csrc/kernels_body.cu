@@ -286,7 +286,8 @@ __device__ __forceinline__ void integrate_body(const SceneDesc &S, float4 &p0, f
     soft_wall(px, vx, world_edge, edge_band);
     soft_wall(py, vy, world_edge, edge_band);
     soft_wall(pz, vz, world_edge, edge_band);
-    const float st = clampf_d((exc - 0.30f) / (0.70f - 0.30f), 0.0f, 1.0f);
+    constexpr float kWidth = 0.70f - 0.30f, kWidthRcp = 0x1.400002p+1f;  // RN(1 / kWidth)
+    const float st = clampf_d(div_by_const(exc - 0.30f, kWidth, kWidthRcp), 0.0f, 1.0f);
     const float hue_drift = 1.0f - st * st * (3.0f - 2.0f * st);
     const float hsum = p0.w + dt * hue_drift *
                                   (0.012f + signed_radial * 0.030f + exc * 0.036f +

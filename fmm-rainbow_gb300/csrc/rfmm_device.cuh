@@ -39,8 +39,26 @@ __device__ __forceinline__ int32_t f2i_rn_sat(float x) { return __float2int_rn(x
 // position_cell (wgsl:144-152); the cell at side `dim` is floor(u * dim).
 // u * 2^l is exact, so computing u once and scaling per level is bit-identical
 // to calling position_cell per level.
+// x / c, correctly rounded, for a constant divisor c with z = RN(1/c): the
+// estimate q0 = RN(x z) is corrected once with the exact remainder
+// r = fma(-q0, c, x), q = fma(r, z, q0) (Markstein's correction step;
+// Brisebarre, Muller & Raina, IEEE Trans. Comput. 53(8), 2004, for known
+// divisors).  For the two divisors used (1.6f and 0.70f - 0.30f) the result
+// equals IEEE x / c for every binary32 x with |x| >= 2^-100 (checked
+// exhaustively by tests/native/const_div_check.c); smaller |x|, where the
+// remainder is not exact, take the division, and non-finite estimates are
+// already the quotient.
+__device__ __forceinline__ float div_by_const(float x, float c, float z) {
+  if (fabsf(x) < 0x1p-100f) return x / c;
+  const float q0 = __fmul_rn(x, z);
+  if (!(fabsf(q0) < __int_as_float(0x7f800000))) return q0;
+  const float r = __fmaf_rn(-q0, c, x);
+  return __fmaf_rn(r, z, q0);
+}
+constexpr float kHalfRcp = 0.625f;  // RN(1 / 1.6f)
+
 __device__ __forceinline__ float unit_coord(float p) {
-  float n = clampf_d(p / kHalf, -0.99999f, 0.99999f);
+  float n = clampf_d(div_by_const(p, kHalf, kHalfRcp), -0.99999f, 0.99999f);
   return n * 0.5f + 0.5f;
 }
 
