@@ -185,6 +185,9 @@ int Engine::create(const std::vector<SceneSpec> &specs, Engine **out) {
   A((void **)&E->d_tmaps_, sizeof(CUtensorMap) * 8 * specs.size());
   A((void **)&E->sort_.hist, 4 * 256 * (size_t)sort_tiles(E->slots_));
   A((void **)&E->sort_.totals, 4 * 256);
+  for (const SceneDesc &d : E->scenes_) E->max_depth_ = std::max(E->max_depth_, d.max_depth);
+  A((void **)&E->d_starts_, 4 * C);
+  A((void **)&E->d_leaf_blocks_, 4 * (size_t)leaf_sort_blocks(E->max_depth_) * specs.size());
   E->sort_.capacity = E->slots_;
   if (st != RFMM_OK) {
     delete E;
@@ -205,7 +208,7 @@ int Engine::create(const std::vector<SceneSpec> &specs, Engine **out) {
     t.l2l_ctas_per_sm = 5;
     t.integrate_ctas_per_sm = E->body_limit_;
     t.integrate_dynamic = 0;
-    t.resort_interval = E->use_lists_ ? 0u : 64u;  // slots are sorted when they are filled
+    t.resort_interval = E->use_lists_ ? 0u : 16u;  // slots are sorted when they are filled
     t.graph_steps = 16;
     t.pdl = 1;
     if (e == cudaSuccess) e = E->set_tuning(t) == RFMM_OK ? cudaSuccess : cudaErrorInvalidValue;
@@ -348,12 +351,15 @@ int Engine::autotune(uint32_t steps_per_trial, rfmm_tuning *best) {
   cudaEvent_t a = nullptr, b = nullptr;
   RF_CK(cudaEventCreate(&a));
   RF_CK(cudaEventCreate(&b));
+  // Long enough for every candidate resort interval to refresh the order at
+  // least twice, so the trials see its amortised cost.
+  const uint32_t trial_steps = std::max(steps_per_trial, 64u);
   auto trial = [&](const rfmm_tuning &t, float *ms) -> int {
     int st = set_tuning(t);
     if (st == RFMM_OK) st = step(t.graph_steps);  // capture + warm
     if (st != RFMM_OK) return st;
     RF_CK(cudaEventRecord(a, stream_));
-    st = step(steps_per_trial);
+    st = step(trial_steps);
     if (st != RFMM_OK) return st;
     RF_CK(cudaEventRecord(b, stream_));
     RF_CK(cudaEventSynchronize(b));
@@ -365,7 +371,7 @@ int Engine::autotune(uint32_t steps_per_trial, rfmm_tuning *best) {
   int st = trial(cur, &cur_ms);
   // Coordinate descent, two sweeps over the knobs.
   for (int sweep = 0; sweep < 2 && st == RFMM_OK; sweep++) {
-    for (int knob = 0; knob < 7 && st == RFMM_OK; knob++) {
+    for (int knob = 0; knob < 8 && st == RFMM_OK; knob++) {
       std::vector<uint32_t> values;
       switch (knob) {
         case 0: values = {2, 4, 6, 8}; break;
@@ -375,12 +381,15 @@ int Engine::autotune(uint32_t steps_per_trial, rfmm_tuning *best) {
         case 4: values = {0, 1}; break;
         case 5: values = {0, 1}; break;
         case 6: values = {4, 8, 16, 32}; break;
+        case 7:
+          if (!use_lists_) values = {8, 16, 32, 64};  // serving slots are sorted on admission
+          break;
       }
       for (uint32_t v : values) {
         rfmm_tuning t = cur;
-        uint32_t *field[7] = {&t.upward_ctas_per_sm, &t.m2l_ctas_per_sm, &t.l2l_ctas_per_sm,
+        uint32_t *field[8] = {&t.upward_ctas_per_sm, &t.m2l_ctas_per_sm, &t.l2l_ctas_per_sm,
                               &t.integrate_ctas_per_sm, &t.integrate_dynamic, &t.pdl,
-                              &t.graph_steps};
+                              &t.graph_steps, &t.resort_interval};
         if (*field[knob] == v) continue;
         *field[knob] = v;
         float ms = 0.0f;
@@ -461,14 +470,14 @@ int Engine::seed_galaxy(uint32_t scene) {
   return RFMM_OK;
 }
 
-uint32_t Engine::resort_kernels() const { return 2u + 3u * ((key_bits_ + 7u) / 8u); }
+uint32_t Engine::radix_sort_kernels() const { return 2u + 3u * ((key_bits_ + 7u) / 8u); }
 
-void Engine::enqueue_resort(uint32_t ppar) {
+void Engine::enqueue_resort(uint32_t ppar, uint32_t count_par) {
+  // Leaf counting sort from the deposit of the current positions.
   LaunchCtx L = ctx(mcur_, lpar_, ppar);
-  launch_keys(L, sort_.keys[0], sort_.vals[0], nullptr, 0, tiles_, 0u);
-  const int r = radix_sort(stream_, sort_, slots_, key_bits_);
-  launch_gather(L, sort_.vals[r], d_part_[ppar], d_ids_[ppar], d_part_[ppar ^ 1u], d_ids_[ppar ^ 1u],
-                nullptr, tiles_, 0u);
+  leaf_counting_sort(L, (uint32_t)scenes_.size(), max_depth_, d_mom_[count_par], d_leaf_blocks_,
+                     d_starts_, d_part_[ppar], d_ids_[ppar], d_part_[ppar ^ 1u], d_ids_[ppar ^ 1u],
+                     tiles_);
 }
 
 int Engine::rebuild_lists() {
@@ -573,7 +582,7 @@ int Engine::commit() {
   RF_CK(cudaMemsetAsync(d_mom_[mcur_], 0, 16ull * cells_, stream_));
   launch_gather(L, sort_.vals[r], d_part_[pcur_], d_ids_[pcur_], d_part_[pcur_ ^ 1u],
                 d_ids_[pcur_ ^ 1u], d_mom_[mcur_], tiles_, 0u, d_pos4_);
-  launches_ += resort_kernels();
+  launches_ += radix_sort_kernels();
   if (near_mode_ == kNearP2P) {
     launch_leaf_starts(L, sort_.keys[r], (uint32_t)scenes_.size());
     launches_ += 1;
@@ -616,8 +625,7 @@ int Engine::set_near_mode(uint32_t mode) {
     if (d.key_level < d.depth) return RFMM_ERR_INVALID;
   if (mode == near_mode_) return RFMM_OK;
   if (mode == kNearP2P && d_pos4_ == nullptr) {
-    int st = alloc((void **)&d_pos4_, 16ull * slots_);
-    if (st == RFMM_OK) st = alloc((void **)&d_starts_, 4ull * cells_);
+    const int st = alloc((void **)&d_pos4_, 16ull * slots_);
     if (st != RFMM_OK) return st;
   }
   clear_graphs();
@@ -658,7 +666,7 @@ int Engine::launch_chunk(uint32_t len, bool sort_at_end) {
     cudaGraph_t g = nullptr;
     RF_CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
     for (uint32_t j = 0; j < len; j++) enqueue_step(mcur_ ^ (j & 1u), lpar_ ^ (j & 1u), pcur_);
-    if (sort_at_end) enqueue_resort(pcur_);
+    if (sort_at_end) enqueue_resort(pcur_, mcur_ ^ (len & 1u));
     cudaError_t e = cudaStreamEndCapture(stream_, &g);
     if (e != cudaSuccess) {
       if (g != nullptr) cudaGraphDestroy(g);
@@ -691,7 +699,7 @@ int Engine::step(uint32_t steps) {
   }
   while (steps > 0) {
     if (resort_interval_ > 0 && since_sort_ >= resort_interval_) {
-      enqueue_resort(pcur_);
+      enqueue_resort(pcur_, mcur_);
       RF_CK(cudaGetLastError());
       launches_ += resort_kernels();
       pcur_ ^= 1u;
@@ -862,7 +870,7 @@ int Engine::profile_steps(uint32_t steps, float ms[kKernelKinds], uint32_t launc
   };
   for (uint32_t s = 0; s < steps && st == RFMM_OK; s++) {
     if (near_mode_ == kNearReference && resort_interval_ > 0 && since_sort_ >= resort_interval_) {
-      timed(kKResort, [&] { enqueue_resort(pcur_); });
+      timed(kKResort, [&] { enqueue_resort(pcur_, mcur_); });
       launches_ += resort_kernels();
       pcur_ ^= 1u;
       since_sort_ = 0;

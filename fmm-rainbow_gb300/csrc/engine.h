@@ -101,14 +101,20 @@ class Engine {
   int build_tensor_maps();
   LaunchCtx ctx(uint32_t mpar, uint32_t lpar, uint32_t ppar) const;
   void enqueue_step(uint32_t mpar, uint32_t lpar, uint32_t ppar);
-  void enqueue_resort(uint32_t ppar);
+  // Refresh of the resident leaf order: bodies of particle buffer `ppar` are
+  // bucketed by leaf into the other buffer using the leaf counts of
+  // moments buffer `count_par` (the deposit of the current positions).
+  void enqueue_resort(uint32_t ppar, uint32_t count_par);
+  uint32_t radix_sort_kernels() const;  // keys + radix sort + gather (uploads)
+  uint32_t max_depth_ = 0;
+  uint32_t *d_leaf_blocks_ = nullptr;  // leaf counting sort: per-block sums
   // kNearP2P end of step: bodies back to caller order, leaf-key sort, gather
   // with the deposit into `mom_into`, position snapshot and leaf starts.
   void enqueue_p2p_sort(uint32_t mpar, uint32_t lpar, uint32_t ppar, uint4 *mom_into);
   uint32_t p2p_sort_kernels() const { return 4u + 3u * ((key_bits_ + 7u) / 8u); }
   uint32_t near_mode_ = kNearReference;
   float4 *d_pos4_ = nullptr;      // kNearP2P: leaf-sorted positions
-  uint32_t *d_starts_ = nullptr;  // kNearP2P: per-leaf start slots
+  uint32_t *d_starts_ = nullptr;  // per-leaf start slots (leaf sorts)
   int launch_chunk(uint32_t len, bool sort_at_end);
   int commit_scene(uint32_t scene);
   int rebuild_lists();
@@ -172,7 +178,7 @@ class Engine {
   };
   std::map<std::tuple<uint32_t, uint32_t, uint32_t, uint32_t, bool>, Graph> graphs_;
   uint64_t launches_ = 0;  // kernels this engine has launched (graph nodes included)
-  uint32_t resort_kernels() const;
+  uint32_t resort_kernels() const { return 4u; }
   cudaEvent_t ev_[8] = {};
 };
 

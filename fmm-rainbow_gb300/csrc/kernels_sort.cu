@@ -1,6 +1,8 @@
-// Stable LSD radix sort of (key, value) pairs with 8-bit digits.
+// Resident-order sorts: a stable LSD radix sort of (key, value) pairs with
+// 8-bit digits (uploads and the P2P mode's per-step sort), and the leaf
+// counting sort that refreshes the order of resident bodies.
 //
-// It orders bodies by (scene, Morton leaf key) so each leaf's bodies are
+// The radix sort orders bodies by (scene, Morton leaf key) so each leaf's bodies are
 // contiguous: leaf membership and occupancy then come from runs of equal
 // keys, and the deposit is a segmented reduction over those runs.  The sort
 // is stable, so the resident order is a deterministic function of the input.
@@ -14,6 +16,7 @@
 //                   shared memory), then scatter
 #include <cuda_runtime.h>
 
+#include "rfmm_device.cuh"
 #include "rfmm_kernels.h"
 
 namespace rfmm {
@@ -145,6 +148,242 @@ int radix_sort(cudaStream_t stream, SortScratch &s, uint32_t n, uint32_t bits) {
     cur ^= 1;
   }
   return cur;
+}
+
+// ------------------------------------------------ leaf counting-sort resort
+//
+// The periodic refresh of the resident leaf order.  The leaf counts of the
+// current positions are already known (integrate deposited them into the next
+// step's moments), so bodies are bucketed by leaf with one exclusive scan of
+// the counts in Morton order of the leaves and one scatter:
+//   k_leaf_block_sums  per 4096-leaf block of a scene, the sum of its counts
+//   k_leaf_block_scan  per scene, exclusive scan of its block sums (+ body_off)
+//   k_leaf_offsets     per block, exclusive scan of its counts -> first slot of
+//                      every leaf (starts, at the scene's cell offset)
+//   k_leaf_scatter     every body takes the next slot of its leaf (one atomic
+//                      per leaf group of a warp) and moves there with its id
+// Bodies of one leaf land in an arbitrary order, which no result depends on:
+// each body's update reads only its own state and the tree, and the moment
+// sums are exact integers.
+
+namespace {
+
+constexpr uint32_t kLeafBlock = 4096u;
+constexpr uint32_t kLeafThreads = 1024u;
+
+__device__ __forceinline__ uint32_t compact3(uint32_t v) {  // inverse of a 3-D bit spread
+  v &= 0x09249249u;
+  v = (v | (v >> 2)) & 0x030C30C3u;
+  v = (v | (v >> 4)) & 0x0300F00Fu;
+  v = (v | (v >> 8)) & 0x030000FFu;
+  v = (v | (v >> 16)) & 0x000003FFu;
+  return v;
+}
+
+__device__ __forceinline__ uint32_t spread3s(uint32_t v) {
+  v &= 0x3FFu;
+  v = (v | (v << 16)) & 0x030000FFu;
+  v = (v | (v << 8)) & 0x0300F00Fu;
+  v = (v | (v << 4)) & 0x030C30C3u;
+  v = (v | (v << 2)) & 0x09249249u;
+  return v;
+}
+
+// Count of the leaf with Morton index m (x in bit 0) of scene S.
+__device__ __forceinline__ uint32_t leaf_count(const SceneDesc &S, const uint4 *mom, uint32_t m) {
+  const uint32_t D = S.depth;
+  const uint32_t x = compact3(m), y = compact3(m >> 1), z = compact3(m >> 2);
+  return mom[S.cell_off + level_offset_d(D) + (x | (y << D) | (z << (2u * D)))].x;
+}
+
+// Sum over the 1024-thread block (every thread gets the total).
+__device__ __forceinline__ uint32_t block_sum_1024(uint32_t v, uint32_t *warp_buf) {
+  for (uint32_t off = 16u; off > 0u; off >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, off);
+  __syncthreads();
+  if ((threadIdx.x & 31u) == 0u) warp_buf[threadIdx.x >> 5] = v;
+  __syncthreads();
+  uint32_t t = warp_buf[threadIdx.x & 31u];
+  for (uint32_t off = 16u; off > 0u; off >>= 1) t += __shfl_xor_sync(0xFFFFFFFFu, t, off);
+  return t;
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(kLeafThreads) k_leaf_block_sums(const SceneDesc *__restrict__ scenes,
+                                                                  const uint4 *__restrict__ mom,
+                                                                  uint32_t *__restrict__ block_sums,
+                                                                  uint32_t max_blocks) {
+  __shared__ uint32_t warp_buf[32];
+  const SceneDesc &S = scenes[blockIdx.y];
+  const uint32_t leaves = 1u << (3u * S.depth);
+  const uint32_t base = blockIdx.x * kLeafBlock;
+  if (S.n == 0u || base >= leaves) return;  // block-uniform
+  uint32_t v = 0u;
+  for (uint32_t k = 0; k < kLeafBlock / kLeafThreads; k++) {
+    const uint32_t m = base + k * kLeafThreads + threadIdx.x;
+    if (m < leaves) v += leaf_count(S, mom, m);
+  }
+  v = block_sum_1024(v, warp_buf);
+  if (threadIdx.x == 0) block_sums[blockIdx.y * max_blocks + blockIdx.x] = v;
+}
+
+// One warp per scene: exclusive scan of the scene's block sums (at most 64
+// blocks: depth <= 6), offset by the scene's first slot.
+__global__ void __launch_bounds__(32) k_leaf_block_scan(const SceneDesc *__restrict__ scenes,
+                                                        uint32_t *__restrict__ block_sums,
+                                                        uint32_t max_blocks) {
+  const SceneDesc &S = scenes[blockIdx.x];
+  if (S.n == 0u) return;
+  const uint32_t lane = threadIdx.x;
+  const uint32_t nb = ((1u << (3u * S.depth)) + kLeafBlock - 1u) / kLeafBlock;
+  uint32_t *row = block_sums + blockIdx.x * max_blocks;
+  // Lane l holds blocks 2l and 2l + 1.
+  const uint32_t a = 2u * lane < nb ? row[2u * lane] : 0u;
+  const uint32_t b = 2u * lane + 1u < nb ? row[2u * lane + 1u] : 0u;
+  uint32_t x = a + b;
+  for (uint32_t off = 1u; off < 32u; off <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, off);
+    if (lane >= off) x += y;
+  }
+  const uint32_t before = S.body_off + x - (a + b);
+  if (2u * lane < nb) row[2u * lane] = before;
+  if (2u * lane + 1u < nb) row[2u * lane + 1u] = before + a;
+}
+
+__global__ void __launch_bounds__(kLeafThreads) k_leaf_offsets(const SceneDesc *__restrict__ scenes,
+                                                               const uint4 *__restrict__ mom,
+                                                               const uint32_t *__restrict__ block_offs,
+                                                               uint32_t max_blocks,
+                                                               uint32_t *__restrict__ starts) {
+  __shared__ uint32_t warp_sums[32];
+  const SceneDesc &S = scenes[blockIdx.y];
+  const uint32_t leaves = 1u << (3u * S.depth);
+  const uint32_t base = blockIdx.x * kLeafBlock;
+  if (S.n == 0u || base >= leaves) return;  // block-uniform
+  // Thread t owns leaves base + 4t .. 4t+3 (a contiguous run of the Morton order).
+  constexpr uint32_t kPer = kLeafBlock / kLeafThreads;
+  uint32_t c[kPer], total = 0u;
+  for (uint32_t k = 0; k < kPer; k++) {
+    const uint32_t m = base + threadIdx.x * kPer + k;
+    c[k] = m < leaves ? leaf_count(S, mom, m) : 0u;
+    total += c[k];
+  }
+  // Exclusive scan of the thread totals across the block.
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  uint32_t x = total;
+  for (uint32_t off = 1u; off < 32u; off <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, off);
+    if (lane >= off) x += y;
+  }
+  if (lane == 31u) warp_sums[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t s = warp_sums[lane];
+    for (uint32_t off = 1u; off < 32u; off <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, s, off);
+      if (lane >= off) s += y;
+    }
+    warp_sums[lane] = s;
+  }
+  __syncthreads();
+  uint32_t run = block_offs[blockIdx.y * max_blocks + blockIdx.x] + (warp ? warp_sums[warp - 1] : 0u) +
+                 x - total;
+  for (uint32_t k = 0; k < kPer; k++) {
+    const uint32_t m = base + threadIdx.x * kPer + k;
+    if (m < leaves) starts[S.cell_off + m] = run;
+    run += c[k];
+  }
+}
+
+// Each CTA moves the bodies of kScatterTiles tiles.  Slots are reserved in
+// two levels so a dense leaf (tens of thousands of bodies) sees one global
+// atomic per CTA instead of one per warp: warp groups of a leaf reserve their
+// offsets in a shared-memory table of the CTA's leaves, then one thread per
+// leaf reserves the CTA's whole block of that leaf from `starts`.
+constexpr uint32_t kScatterTiles = 4u;
+constexpr uint32_t kScatterSlots = 2048u;  // > bodies per CTA, so probing always ends
+
+__global__ void __launch_bounds__(256) k_leaf_scatter(const SceneDesc *__restrict__ scenes,
+                                                      const uint32_t *__restrict__ tile_scene,
+                                                      const float4 *__restrict__ part_in,
+                                                      const uint32_t *__restrict__ ids_in,
+                                                      float4 *__restrict__ part_out,
+                                                      uint32_t *__restrict__ ids_out,
+                                                      uint32_t *__restrict__ starts, uint32_t tiles) {
+  __shared__ uint32_t hkey[kScatterSlots], hcnt[kScatterSlots];
+  constexpr uint32_t kEmptyKey = 0xFFFFFFFFu;
+  for (uint32_t i = threadIdx.x; i < kScatterSlots; i += blockDim.x) {
+    hkey[i] = kEmptyKey;
+    hcnt[i] = 0u;
+  }
+  __syncthreads();
+  const uint32_t lane = threadIdx.x & 31u;
+  float4 p0[kScatterTiles], p1[kScatterTiles];
+  uint32_t off[kScatterTiles], hs[kScatterTiles], src[kScatterTiles];
+#pragma unroll
+  for (uint32_t r = 0; r < kScatterTiles; r++) {
+    const uint32_t tile = blockIdx.x * kScatterTiles + r;
+    uint32_t key = kEmptyKey;
+    src[r] = kEmptyKey;
+    if (tile < tiles) {
+      const SceneDesc &S = scenes[tile_scene[tile]];
+      const uint32_t slot = tile * 256u + threadIdx.x;
+      if (slot - S.body_off < S.n) {
+        p0[r] = part_in[2u * slot];
+        p1[r] = part_in[2u * slot + 1u];
+        src[r] = slot;
+        const uint32_t dim = 1u << S.depth;
+        key = S.cell_off + (spread3s(cell_of_unit(unit_coord(p0[r].x), dim)) |
+                            (spread3s(cell_of_unit(unit_coord(p0[r].y), dim)) << 1) |
+                            (spread3s(cell_of_unit(unit_coord(p0[r].z), dim)) << 2));
+      }
+    }
+    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
+    const uint32_t leader = __ffs(peers) - 1u;
+    uint32_t h = 0u, base = 0u;
+    if (key != kEmptyKey && lane == leader) {
+      h = (key * 2654435761u) >> 21;  // 11-bit multiplicative hash
+      for (uint32_t probe = 0; probe < kScatterSlots; probe++) {
+        const uint32_t prev = atomicCAS(&hkey[h], kEmptyKey, key);
+        if (prev == kEmptyKey || prev == key) break;
+        h = (h + 1u) & (kScatterSlots - 1u);
+      }
+      base = atomicAdd(&hcnt[h], __popc(peers));
+    }
+    hs[r] = __shfl_sync(0xFFFFFFFFu, h, leader);
+    off[r] = __shfl_sync(0xFFFFFFFFu, base, leader) + __popc(peers & ((1u << lane) - 1u));
+  }
+  __syncthreads();
+  // One global reservation per (CTA, leaf); hcnt becomes the CTA's first slot.
+  for (uint32_t i = threadIdx.x; i < kScatterSlots; i += blockDim.x)
+    if (hkey[i] != kEmptyKey) hcnt[i] = atomicAdd(&starts[hkey[i]], hcnt[i]);
+  __syncthreads();
+#pragma unroll
+  for (uint32_t r = 0; r < kScatterTiles; r++) {
+    if (src[r] == kEmptyKey) continue;
+    const uint32_t dst = hcnt[hs[r]] + off[r];
+    if (dst >= tiles * 256u) continue;  // defensive: counts and positions always agree
+    part_out[2u * dst] = p0[r];
+    part_out[2u * dst + 1u] = p1[r];
+    ids_out[dst] = ids_in[src[r]];
+  }
+}
+
+uint32_t leaf_sort_blocks(uint32_t max_depth) {
+  return ((1u << (3u * max_depth)) + kLeafBlock - 1u) / kLeafBlock;
+}
+
+void leaf_counting_sort(const LaunchCtx &L, uint32_t scenes, uint32_t max_depth, const uint4 *counts,
+                        uint32_t *block_scratch, uint32_t *starts, const float4 *part_in,
+                        const uint32_t *ids_in, float4 *part_out, uint32_t *ids_out,
+                        uint32_t tiles) {
+  const uint32_t nb = leaf_sort_blocks(max_depth);
+  k_leaf_block_sums<<<dim3(nb, scenes), kLeafThreads, 0, L.stream>>>(L.scenes, counts, block_scratch, nb);
+  k_leaf_block_scan<<<scenes, 32, 0, L.stream>>>(L.scenes, block_scratch, nb);
+  k_leaf_offsets<<<dim3(nb, scenes), kLeafThreads, 0, L.stream>>>(L.scenes, counts, block_scratch, nb,
+                                                                    starts);
+  k_leaf_scatter<<<(tiles + kScatterTiles - 1u) / kScatterTiles, 256, 0, L.stream>>>(
+      L.scenes, L.tile_scene, part_in, ids_in, part_out, ids_out, starts, tiles);
 }
 
 }  // namespace rfmm

@@ -123,5 +123,13 @@ struct SortScratch {
 uint32_t sort_tiles(uint32_t n);
 // Sorts keys[0]/vals[0] over `bits` low bits; returns which buffer holds the result.
 int radix_sort(cudaStream_t stream, SortScratch &s, uint32_t n, uint32_t bits);
+// Leaf counting sort of every scene's bodies (part_in/ids_in -> part_out/
+// ids_out) from the leaf counts in `counts` (moments of the current
+// positions).  block_scratch: leaf_sort_blocks(max_depth) words per scene;
+// starts: one word per tree cell (left holding each leaf's end slot).
+uint32_t leaf_sort_blocks(uint32_t max_depth);
+void leaf_counting_sort(const LaunchCtx &L, uint32_t scenes, uint32_t max_depth, const uint4 *counts,
+                        uint32_t *block_scratch, uint32_t *starts, const float4 *part_in,
+                        const uint32_t *ids_in, float4 *part_out, uint32_t *ids_out, uint32_t tiles);
 
 }  // namespace rfmm

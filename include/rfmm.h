@@ -145,7 +145,7 @@ int rfmm_phase_times(rfmm_handle *h, float ms[7]);
 int rfmm_check_finite(rfmm_handle *h, uint32_t probe, uint32_t *non_finite, float *max_abs);
 
 /* Steps between refreshes of the resident leaf order (0 = never; default
- * 64).  Results do not depend on it. */
+ * 16; the autotuner also tunes it).  Results do not depend on it. */
 int rfmm_set_resort_interval(rfmm_handle *h, uint32_t steps);
 
 /* Near-field mode.  RFMM_NEAR_REFERENCE (default) is the reference's: 26
