@@ -303,10 +303,11 @@ __device__ __forceinline__ void integrate_body(const SceneDesc &S, float4 &p0, f
     qz = f2i_rn_sat(pz * S.scale);
 }
 
-// Persistent integrate: each CTA walks a contiguous slice of body tiles
-// (leaf-sorted, so its bodies are spatially compact), integrates every body
-// and accumulates the next step's deposit in a shared-memory table flushed
-// once at the end.
+// Persistent integrate: CTA c of G walks body tiles c, c + G, c + 2G, ...
+// (each tile is 256 leaf-sorted, spatially compact bodies; interleaving the
+// tiles spreads dense and sparse regions, whose per-body costs differ, evenly
+// over the CTAs), integrates every body and accumulates the next step's
+// deposit in a shared-memory table flushed once at the end.
 //
 // kP2P: near field by exact pair sums over the leaf-sorted position snapshot;
 // no deposit (the end-of-step sort deposits the new positions).
@@ -330,18 +331,16 @@ __global__ void __launch_bounds__(256) k_integrate(const SceneDesc *__restrict__
   if (!kP2P) T.clear();
   grid_dependency_wait();  // fields of this step are complete
   const uint32_t ntiles = tile_list != nullptr ? min(ctr->tiles_active, tiles) : tiles;
-  // Static schedule: a contiguous slice per CTA.  Dynamic: tiles are taken
-  // one at a time from a counter (reset by this step's upward pass).
-  uint32_t t0, t1;
-  cta_tile_range(ntiles, t0, t1);
+  // Static schedule: interleaved tiles.  Dynamic: tiles are taken one at a
+  // time from a counter (reset by this step's upward pass).
   auto grab = [&]() -> uint32_t {
     __syncthreads();
     if (threadIdx.x == 0) s_next = atomicAdd(&ctr->tile_cursor, 1u);
     __syncthreads();
     return s_next;
   };
-  uint32_t i = dynamic ? grab() : t0;
-  const uint32_t end = dynamic ? ntiles : t1;
+  uint32_t i = dynamic ? grab() : blockIdx.x;
+  const uint32_t end = ntiles;
   uint32_t cur = 0xFFFFFFFFu;
   // The next tile's bodies are loaded one iteration ahead.
   float4 n0 = make_float4(0.f, 0.f, 0.f, 0.f), n1 = n0;
@@ -354,7 +353,7 @@ __global__ void __launch_bounds__(256) k_integrate(const SceneDesc *__restrict__
     const uint32_t tile = next_tile;
     const uint32_t slot = tile * kTile + threadIdx.x;
     float4 p0 = n0, p1 = n1;
-    const uint32_t ni = dynamic ? grab() : i + 1u;
+    const uint32_t ni = dynamic ? grab() : i + gridDim.x;
     if (ni < end) {
       next_tile = tile_list != nullptr ? tile_list[ni] : ni;
       n0 = part[2u * (next_tile * kTile + threadIdx.x)];
