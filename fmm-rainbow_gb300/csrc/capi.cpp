@@ -223,6 +223,29 @@ int rfmm_get_diagnostics(rfmm_handle *h, rfmm_diagnostics *out) {
   return RFMM_OK;
 }
 
+void rfmm_default_render_params(rfmm_render_params *out) {
+  if (out == nullptr) return;
+  out->width = 1280u;
+  out->height = 720u;
+  out->instances = 0u;
+  out->yaw = -0.18f;  // app.js:75-77
+  out->pitch = -0.14f;
+  out->zoom = 1.78f;
+  out->point_size = 5.0f;  // index.html "gradient radius" default
+  out->exposure = 1.0f;
+}
+
+int rfmm_render(rfmm_handle *h, const rfmm_render_params *params, void *host_rgba, size_t bytes) {
+  if (guard(h) || params == nullptr) return RFMM_ERR_INVALID;
+  return h->engine->render(0, *params, host_rgba, bytes, cudaMemcpyDeviceToHost);
+}
+
+int rfmm_render_device(rfmm_handle *h, const rfmm_render_params *params, void *device_rgba,
+                       size_t bytes) {
+  if (guard(h) || params == nullptr) return RFMM_ERR_INVALID;
+  return h->engine->render(0, *params, device_rgba, bytes, cudaMemcpyDeviceToDevice);
+}
+
 int rfmm_get_tuning(rfmm_handle *h, rfmm_tuning *out) {
   if (guard(h)) return RFMM_ERR_INVALID;
   return h->engine->get_tuning(out);

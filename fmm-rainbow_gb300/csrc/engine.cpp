@@ -1000,6 +1000,58 @@ int Engine::force_error(uint32_t scene, uint32_t targets, uint64_t seed, double 
   return RFMM_OK;
 }
 
+int Engine::render(uint32_t scene, const rfmm_render_params &p, void *dst, size_t bytes,
+                   cudaMemcpyKind kind) {
+  if (scene >= scenes_.size() || dst == nullptr) return RFMM_ERR_INVALID;
+  if (!committed_) return RFMM_ERR_STATE;
+  if (p.width == 0u || p.height == 0u || p.width > 16384u || p.height > 16384u) return RFMM_ERR_INVALID;
+  if (bytes != 4ull * p.width * p.height) return RFMM_ERR_INVALID;
+  const SceneDesc &d = scenes_[scene];
+  RenderCamera cam{};
+  cam.instances = p.instances ? p.instances : d.n;
+  cam.acc_w = (p.width + 1u) / 2u;  // accumulation at half the canvas size (app.js:219-220)
+  cam.acc_h = (p.height + 1u) / 2u;
+  cam.canvas_w = (float)p.width;
+  cam.canvas_h = (float)p.height;
+  cam.cos_yaw = (float)std::cos((double)p.yaw);
+  cam.sin_yaw = (float)std::sin((double)p.yaw);
+  cam.cos_pitch = (float)std::cos((double)p.pitch);
+  cam.sin_pitch = (float)std::sin((double)p.pitch);
+  cam.zoom = p.zoom;
+  cam.aspect = (float)((double)p.width / (double)std::max(1u, p.height));
+  cam.exposure = p.exposure;
+  cam.point_size = p.point_size;
+  cam.population_scale = 0.62f * std::pow(1048576.0f / std::max((float)cam.instances, 1.0f), 0.14f);
+  const size_t texels = (size_t)cam.acc_w * cam.acc_h, pixels = (size_t)p.width * p.height;
+  if (d_slot_of_ == nullptr) {
+    const int st = alloc((void **)&d_slot_of_, 4ull * slots_);
+    if (st != RFMM_OK) return st;
+  }
+  if (texels > render_texels_) {
+    int st = alloc((void **)&d_render_acc_, 32ull * texels);
+    if (st == RFMM_OK) st = alloc((void **)&d_render_tex_, 32ull * texels);
+    if (st != RFMM_OK) return st;
+    render_texels_ = texels;
+  }
+  uchar4 *out = reinterpret_cast<uchar4 *>(dst);
+  if (kind != cudaMemcpyDeviceToDevice) {
+    if (pixels > render_pixels_) {
+      const int st = alloc((void **)&d_render_out_, 4ull * pixels);
+      if (st != RFMM_OK) return st;
+      render_pixels_ = pixels;
+    }
+    out = d_render_out_;
+  }
+  LaunchCtx L = ctx(mcur_, lpar_, pcur_);
+  launch_slot_of(L, d_ids_[pcur_], d_slot_of_, d.tile_off, pad_tiles(d.n));
+  launch_render(L, scene, d_slot_of_, cam, d_render_acc_, d_render_tex_, d_render_tex_ + texels, out);
+  RF_CK(cudaGetLastError());
+  launches_ += 5;
+  if (kind != cudaMemcpyDeviceToDevice)
+    RF_CK(cudaMemcpyAsync(dst, out, bytes, cudaMemcpyDeviceToHost, stream_));
+  return sync();
+}
+
 int Engine::diagnostics(uint32_t scene, double out[9]) {
   if (out == nullptr) return RFMM_ERR_INVALID;
   const uint32_t blocks = 4u * (uint32_t)sms_;

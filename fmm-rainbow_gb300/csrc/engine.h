@@ -83,6 +83,8 @@ class Engine {
   int accelerations(uint32_t scene, float *host_out);  // n x (ax, ay, az, phi), caller order
   int force_error(uint32_t scene, uint32_t targets, uint64_t seed, double *rms_rel, double *max_rel);
   int diagnostics(uint32_t scene, double out[9]);
+  // Headless render of a scene's current bodies into an RGBA8 image.
+  int render(uint32_t scene, const rfmm_render_params &p, void *dst, size_t bytes, cudaMemcpyKind kind);
 
   uint32_t num_scenes() const { return (uint32_t)scenes_.size(); }
   const SceneDesc &scene(uint32_t s) const { return scenes_[s]; }
@@ -145,7 +147,11 @@ class Engine {
   float4 *d_accphi_ = nullptr;    // diagnostics: per-body acceleration + potential
   double *d_diag_ = nullptr;      // diagnostics: FP64 partial sums
   size_t diag_doubles_ = 0;
-  uint32_t *d_slot_of_ = nullptr;  // diagnostics: caller id -> resident slot
+  uint32_t *d_slot_of_ = nullptr;  // diagnostics / render: caller id -> resident slot
+  unsigned long long *d_render_acc_ = nullptr;  // render: fixed-point accumulation
+  float4 *d_render_tex_ = nullptr;              // render: two blur textures
+  uchar4 *d_render_out_ = nullptr;              // render: staging for host copies
+  size_t render_texels_ = 0, render_pixels_ = 0;
   int diag_prepare(uint32_t scene, size_t doubles, bool all_bodies);
   float4 *d_src_ = nullptr;
   float4 *d_aux_ = nullptr;

@@ -490,6 +490,11 @@ __global__ void __launch_bounds__(256) k_accel_targets(
   out[t] = make_float4(ax, ay, az, phi);
 }
 
+void launch_slot_of(const LaunchCtx &L, const uint32_t *ids, uint32_t *slot_of, uint32_t tile_base,
+                    uint32_t tiles) {
+  k_slot_of<<<tiles, kTile, 0, L.stream>>>(L.scenes, L.tile_scene, ids, slot_of, tile_base);
+}
+
 void launch_accel_targets(const LaunchCtx &L, uint32_t scene, uint32_t tile_base, uint32_t tiles,
                           const uint32_t *ids, uint32_t *slot_of, const uint32_t *targets,
                           uint32_t nt, float4 *out) {

@@ -105,6 +105,25 @@ void launch_accel_targets(const LaunchCtx &L, uint32_t scene, uint32_t tile_base
                           const uint32_t *ids, uint32_t *slot_of, const uint32_t *targets,
                           uint32_t nt, float4 *out);
 
+// Headless point-splat renderer (kernels_render.cu).  The camera terms the
+// reference's render plan stores in its parameter slots (app.js:141-185).
+struct RenderCamera {
+  uint32_t instances;        // points drawn (render count)
+  uint32_t acc_w, acc_h;     // accumulation texture (half the canvas, rounded up)
+  float canvas_w, canvas_h;  // canvas (viewport) size
+  float cos_yaw, sin_yaw, cos_pitch, sin_pitch;
+  float zoom;                // camera distance in half-extents (Params.speed)
+  float aspect;              // canvas width / height
+  float exposure;
+  float point_size;          // outer blur radius in canvas pixels
+  float population_scale;    // 0.62 * (2^20 / instances)^0.14
+};
+void launch_render(const LaunchCtx &L, uint32_t scene, const uint32_t *slot_of, const RenderCamera &cam,
+                   unsigned long long *acc, float4 *tex_a, float4 *tex_b, uchar4 *out);
+// slot_of[body_off + id] = resident slot, for the bodies of tiles [tile_base, +tiles).
+void launch_slot_of(const LaunchCtx &L, const uint32_t *ids, uint32_t *slot_of, uint32_t tile_base,
+                    uint32_t tiles);
+
 // FP64 diagnostics (kernels_diag.cu).
 void launch_direct_sum_f64(cudaStream_t stream, const float4 *part_caller, uint32_t n,
                            const uint32_t *targets, uint32_t nt, double gravity, double eps,

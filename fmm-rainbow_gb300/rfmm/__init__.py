@@ -84,6 +84,12 @@ class Diagnostics(C.Structure):
                 ("momentum", C.c_double * 3), ("angular_momentum", C.c_double * 3)]
 
 
+class RenderParams(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("instances", C.c_uint32),
+                ("yaw", C.c_float), ("pitch", C.c_float), ("zoom", C.c_float),
+                ("point_size", C.c_float), ("exposure", C.c_float)]
+
+
 class Plan(C.Structure):
     _fields_ = [("particles", C.c_uint32), ("depth", C.c_uint32), ("cells", C.c_uint32),
                 ("fixed_point_scale", C.c_float)]
@@ -156,6 +162,9 @@ SIGNATURES = {
     "rfmm_get_diagnostics": (_i, [_vp, C.POINTER(Diagnostics)]),
     "rfmm_batch_force_error": (_i, [_vp, _u32, _u32, C.c_uint64, C.POINTER(C.c_double),
                                     C.POINTER(C.c_double)]),
+    "rfmm_default_render_params": (None, [C.POINTER(RenderParams)]),
+    "rfmm_render": (_i, [_vp, C.POINTER(RenderParams), _vp, _sz]),
+    "rfmm_render_device": (_i, [_vp, C.POINTER(RenderParams), _vp, _sz]),
     "rfmm_get_tuning": (_i, [_vp, C.POINTER(Tuning)]),
     "rfmm_set_tuning": (_i, [_vp, C.POINTER(Tuning)]),
     "rfmm_autotune": (_i, [_vp, _u32, C.POINTER(Tuning)]),
@@ -209,6 +218,14 @@ def default_params(**kw) -> Params:
             getattr(p, k)[:] = v
         else:
             setattr(p, k, v)
+    return p
+
+
+def default_render_params(**kw) -> RenderParams:
+    p = RenderParams()
+    lib().rfmm_default_render_params(C.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
     return p
 
 
@@ -374,6 +391,17 @@ class Solver:
         _check(lib().rfmm_force_error(self._h, targets, seed, C.byref(rms), C.byref(mx)),
                "rfmm_force_error")
         return rms.value, mx.value
+
+    def render(self, **kw) -> np.ndarray:
+        """(height, width, 4) uint8 image of the current bodies (row 0 at the top)."""
+        p = default_render_params(**kw)
+        out = np.empty((p.height, p.width, 4), np.uint8)
+        _check(lib().rfmm_render(self._h, C.byref(p), out.ctypes.data, out.nbytes), "rfmm_render")
+        return out
+
+    def render_device(self, params, device_ptr, nbytes):
+        _check(lib().rfmm_render_device(self._h, C.byref(params), device_ptr, nbytes),
+               "rfmm_render_device")
 
     def diagnostics(self) -> dict:
         d = Diagnostics()

@@ -34,6 +34,7 @@ SOURCES = [
     "kernels_body.cu",
     "kernels_sort.cu",
     "kernels_diag.cu",
+    "kernels_render.cu",
     "noalloc.cu",
     "engine.cpp",
     "capi.cpp",

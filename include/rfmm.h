@@ -210,6 +210,32 @@ int rfmm_force_error(rfmm_handle *h, uint32_t targets, uint64_t seed, double *rm
 /* Energy and momentum with FP64 compensated (Neumaier) reductions. */
 int rfmm_get_diagnostics(rfmm_handle *h, rfmm_diagnostics *out);
 
+/* ---------------------------------------------------------------- render
+ *
+ * Headless restatement of the reference's display passes (wgsl:780-1009,
+ * app.js:650-710): every drawn point (instance i shows body (i * 747796405 +
+ * 2891336453) mod N in the caller's order) is splatted additively into an
+ * accumulation image of half the canvas size, blurred by the 5-tap separable
+ * filter and tone-mapped into an RGBA8 image of width x height (row 0 at the
+ * top).  No window or graphics API is involved.  The accumulation is a
+ * fixed-point sum (exact, order-independent) instead of an rgba16float blend.
+ * The control field highlight uses the handle's params. */
+typedef struct rfmm_render_params {
+  uint32_t width, height; /* canvas size in pixels */
+  uint32_t instances;     /* points drawn; 0 = N */
+  float yaw, pitch;       /* camera angles (radians) */
+  float zoom;             /* camera distance in world half-extents */
+  float point_size;       /* blur radius in canvas pixels (the "gradient radius") */
+  float exposure;
+} rfmm_render_params;
+
+/* Defaults of the reference app: yaw -0.18, pitch -0.14, zoom 1.78, point
+ * size 5, exposure 1, instances = N, 1280 x 720. */
+void rfmm_default_render_params(rfmm_render_params *out);
+int rfmm_render(rfmm_handle *h, const rfmm_render_params *params, void *host_rgba, size_t bytes);
+int rfmm_render_device(rfmm_handle *h, const rfmm_render_params *params, void *device_rgba,
+                       size_t bytes);
+
 /* ------------------------------------------------------------------- tuning
  *
  * Launch shapes and scheduling of the step kernels.  Results never depend on

@@ -43,6 +43,14 @@ class OParams(C.Structure):
     ]
 
 
+class ORenderParams(C.Structure):
+    """Camera and image parameters of the headless render (the solver's rfmm_render_params)."""
+
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("instances", C.c_uint32),
+                ("yaw", C.c_float), ("pitch", C.c_float), ("zoom", C.c_float),
+                ("point_size", C.c_float), ("exposure", C.c_float)]
+
+
 _lib = None
 
 
@@ -78,6 +86,7 @@ def lib():
             "oracle_direct_sum_f64": (None, [vp, u32, vp, u32, C.c_double, C.c_double, vp]),
             "oracle_accelerations": (None, [vp, vp, vp, P, vp]),
             "oracle_set_threads": (C.c_int, [C.c_int]),
+            "oracle_render": (None, [vp, P, C.POINTER(ORenderParams), vp, vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -180,6 +189,18 @@ def direct_sum_f64(particles: np.ndarray, targets: np.ndarray, gravity: float, e
     p = np.ascontiguousarray(particles)
     lib().oracle_direct_sum_f64(_ptr(p), len(p), _ptr(t), len(t), gravity, eps, _ptr(out))
     return out
+
+
+def render(particles: np.ndarray, params: OParams, width=1280, height=720, instances=0, yaw=-0.18,
+           pitch=-0.14, zoom=1.78, point_size=5.0, exposure=1.0):
+    """RGBA8 image (height, width, 4) and the fixed-point accumulation
+    ((height+1)//2, (width+1)//2, 4) of the display passes (wgsl:780-1009)."""
+    r = ORenderParams(width, height, instances, yaw, pitch, zoom, point_size, exposure)
+    img = np.zeros((height, width, 4), np.uint8)
+    acc = np.zeros(((height + 1) // 2, (width + 1) // 2, 4), np.uint64)
+    p = np.ascontiguousarray(particles)
+    lib().oracle_render(_ptr(p), C.byref(params), C.byref(r), _ptr(img), _ptr(acc))
+    return img, acc
 
 
 def set_threads(n: int) -> int:

@@ -943,3 +943,174 @@ int oracle_set_threads(int n) {
   return 1;
 #endif
 }
+
+/* ------------------------------------------------------------------ render */
+
+/* Headless restatement of the display passes (wgsl:780-1009, app.js:650-710)
+ * with the product's definitions: per-pixel fixed-point accumulation at 2^24
+ * units per 1.0 (order-independent), binary32 blur and resolve intermediates,
+ * exact bilinear weights, RGBA8 output with row 0 at the top.  Transcendentals
+ * are libm's, so the image matches the GPU's by tolerance. */
+typedef struct {
+  uint32_t width, height, instances;
+  float yaw, pitch, zoom, point_size, exposure;
+} ORenderParams;
+
+static float o_mix(float a, float b, float t) { return a * (1.0f - t) + b * t; }
+
+static void o_fetch_acc(const uint64_t *acc, uint32_t w, uint32_t h, int x, int y, float out[4]) {
+  if (x < 0) x = 0;
+  if (y < 0) y = 0;
+  if (x > (int)w - 1) x = (int)w - 1;
+  if (y > (int)h - 1) y = (int)h - 1;
+  const uint64_t *p = acc + 4u * ((size_t)y * w + (size_t)x);
+  for (int k = 0; k < 4; k++) out[k] = (float)p[k] * (1.0f / 16777216.0f);
+}
+
+static void o_fetch_tex(const float *tex, uint32_t w, uint32_t h, int x, int y, float out[4]) {
+  if (x < 0) x = 0;
+  if (y < 0) y = 0;
+  if (x > (int)w - 1) x = (int)w - 1;
+  if (y > (int)h - 1) y = (int)h - 1;
+  const float *p = tex + 4u * ((size_t)y * w + (size_t)x);
+  for (int k = 0; k < 4; k++) out[k] = p[k];
+}
+
+void oracle_render(const OParticle *particles, const OParams *P, const ORenderParams *R,
+                   uint8_t *rgba, uint64_t *acc_out) {
+  const uint32_t W = R->width, H = R->height, aw = (W + 1u) / 2u, ah = (H + 1u) / 2u;
+  const uint32_t instances = R->instances ? R->instances : P->n;
+  const float cyw = (float)cos((double)R->yaw), syw = (float)sin((double)R->yaw);
+  const float cpt = (float)cos((double)R->pitch), spt = (float)sin((double)R->pitch);
+  const float aspect = (float)((double)W / (double)(H > 1u ? H : 1u));
+  const float pop = 0.62f * powf(1048576.0f / fmaxf((float)instances, 1.0f), 0.14f);
+  uint64_t *acc = (uint64_t *)calloc((size_t)aw * ah * 4u, sizeof(uint64_t));
+  for (uint32_t i = 0; i < instances && P->n > 0u; i++) {
+    const OParticle *pt = &particles[(i * 747796405u + 2891336453u) % P->n];
+    const float yx = cyw * pt->px + syw * pt->pz, yy = pt->py, yz = -syw * pt->px + cyw * pt->pz;
+    const float rx = yx, ry = cpt * yy - spt * yz, rz = spt * yy + cpt * yz;
+    const float view_z = R->zoom * O_HALF - rz;
+    const float perspective = (1.92f * O_HALF) / view_z;
+    const float cx = rx * perspective / aspect, cy = ry * perspective;
+    const float depth = 0.46f + rz * 0.08f;
+    const float vel[3] = {pt->vx, pt->vy, pt->vz}, pos[3] = {pt->px, pt->py, pt->pz};
+    const float velocity = length3(vel);
+    const float speed = fmaxf(velocity, 0.0001f);
+    const float excitation = clampf(pt->exc, 0.0f, 1.0f);
+    const float signed_radial =
+        clampf(((pos[0] * vel[0] + pos[1] * vel[1]) + pos[2] * vel[2]) / (fmaxf(length3(pos), 0.0001f) * speed),
+               -1.0f, 1.0f);
+    const float infall = clampf(-signed_radial, 0.0f, 1.0f), outflow = clampf(signed_radial, 0.0f, 1.0f);
+    float sp[3] = {o_mix(0.50f, 0.24f, infall), o_mix(0.42f, 0.56f, infall), o_mix(0.58f, 1.00f, infall)};
+    sp[0] = o_mix(sp[0], 1.00f, outflow);
+    sp[1] = o_mix(sp[1], 0.50f, outflow);
+    sp[2] = o_mix(sp[2], 0.20f, outflow);
+    const float heat = smoothstepf(0.18f, 0.85f, excitation);
+    const float phase[3] = {0.00f, 0.67f, 0.33f};
+    const float luminosity = 0.30f + excitation * 0.90f;
+    const float speed_gain = 0.62f + fminf(velocity * 1.4f, 1.0f) * 0.30f;
+    float col[3];
+    for (int k = 0; k < 3; k++) {
+      const float rainbow = 0.5f + 0.5f * cosf(O_TAU * (pt->hue + phase[k]));
+      const float tint = powf(rainbow, 0.85f);
+      const float s = o_mix(sp[k] * tint, sp[k], heat);
+      col[k] = s * (speed_gain + excitation * 0.90f) + heat * heat * 0.55f;
+    }
+    float influence = 0.0f, cc[3] = {0.82f, 1.0f, 0.28f};
+    if (P->control_point[3] > 0.5f) {
+      const float dx = P->control_point[0] - pos[0], dy = P->control_point[1] - pos[1],
+                  dz = P->control_point[2] - pos[2];
+      const float radius = fmaxf(P->control_radius, 0.02f);
+      influence = expf(-2.0f * ((dx * dx + dy * dy) + dz * dz) / (radius * radius));
+      const float mode = P->control_axis_mode[3];
+      if (mode > 1.5f && mode < 2.5f) {
+        cc[0] = 1.0f; cc[1] = 0.38f; cc[2] = 0.18f;
+      } else if (mode >= 2.5f) {
+        cc[0] = 0.82f; cc[1] = 0.34f; cc[2] = 1.0f;
+      }
+    }
+    for (int k = 0; k < 3; k++) col[k] = o_mix(col[k], cc[k], influence * 0.68f);
+    const float depth_fade = clampf(0.62f + rz * 0.25f, 0.28f, 1.0f) * (0.76f + excitation * 0.48f) *
+                             luminosity * (1.0f + influence * 0.72f);
+    if (!(cx >= -1.0f && cx <= 1.0f && cy >= -1.0f && cy <= 1.0f && depth >= 0.0f && depth <= 1.0f)) continue;
+    const float fx = (cx + 1.0f) * 0.5f * (float)aw, fy = (1.0f - cy) * 0.5f * (float)ah;
+    int px = (int)floorf(fx), py = (int)floorf(fy);
+    if (px > (int)aw - 1) px = (int)aw - 1;
+    if (py > (int)ah - 1) py = (int)ah - 1;
+    const float weight = R->exposure * depth_fade * pop;
+    uint64_t *d = acc + 4u * ((size_t)py * aw + (size_t)px);
+    for (int k = 0; k < 3; k++) d[k] += (uint64_t)llrintf(col[k] * weight * 16777216.0f);
+    d[3] += (uint64_t)llrintf(weight * 16777216.0f);
+  }
+  if (acc_out) memcpy(acc_out, acc, sizeof(uint64_t) * 4u * (size_t)aw * ah);
+  /* Two separable passes (wgsl:914-970). */
+  float *ta = (float *)malloc(sizeof(float) * 4u * (size_t)aw * ah);
+  float *tb = (float *)malloc(sizeof(float) * 4u * (size_t)aw * ah);
+  for (int axis = 0; axis < 2; axis++) {
+    const float dim = axis == 0 ? (float)aw : (float)ah;
+    const float out_dim = axis == 0 ? (float)W : (float)H;
+    const float step = fmaxf(R->point_size, 1.0f) / (out_dim * 3.230769f);
+    const float offs[5] = {0.0f, step * 1.384615f, -(step * 1.384615f), step * 3.230769f, -(step * 3.230769f)};
+    const float wts[5] = {0.227027f, 0.316216f, 0.316216f, 0.070270f, 0.070270f};
+    float *dst = axis == 0 ? ta : tb;
+    for (uint32_t y = 0; y < ah; y++)
+      for (uint32_t x = 0; x < aw; x++) {
+        const float uv = ((axis == 0 ? (float)x : (float)y) + 0.5f) / dim;
+        float field[4] = {0, 0, 0, 0};
+        for (int t = 0; t < 5; t++) {
+          const float u = t == 0 ? uv : uv + offs[t];
+          const float tc = u * dim - 0.5f, f0 = floorf(tc), f = tc - f0;
+          const int i0 = (int)f0;
+          float a[4], b[4];
+          if (axis == 0) {
+            o_fetch_acc(acc, aw, ah, i0, (int)y, a);
+            o_fetch_acc(acc, aw, ah, i0 + 1, (int)y, b);
+          } else {
+            o_fetch_tex(ta, aw, ah, (int)x, i0, a);
+            o_fetch_tex(ta, aw, ah, (int)x, i0 + 1, b);
+          }
+          for (int k = 0; k < 4; k++) {
+            const float v = (a[k] * (1.0f - f) + b[k] * f) * wts[t];
+            field[k] = t == 0 ? v : field[k] + v;
+          }
+        }
+        memcpy(dst + 4u * ((size_t)y * aw + x), field, sizeof(field));
+      }
+  }
+  /* Resolve (wgsl:972-1009). */
+  const float bg[3] = {0.006f, 0.008f, 0.015f};
+  for (uint32_t y = 0; y < H; y++)
+    for (uint32_t x = 0; x < W; x++) {
+      const float u = ((float)x + 0.5f) / (float)W, v = ((float)y + 0.5f) / (float)H;
+      const float tx = u * (float)aw - 0.5f, ty = v * (float)ah - 0.5f;
+      const float fx0 = floorf(tx), fy0 = floorf(ty), fx = tx - fx0, fy = ty - fy0;
+      const int ix = (int)fx0, iy = (int)fy0;
+      float c00[4], c10[4], c01[4], c11[4], a[4];
+      o_fetch_tex(tb, aw, ah, ix, iy, c00);
+      o_fetch_tex(tb, aw, ah, ix + 1, iy, c10);
+      o_fetch_tex(tb, aw, ah, ix, iy + 1, c01);
+      o_fetch_tex(tb, aw, ah, ix + 1, iy + 1, c11);
+      for (int k = 0; k < 4; k++) {
+        const float top = c00[k] * (1.0f - fx) + c10[k] * fx;
+        const float bot = c01[k] * (1.0f - fx) + c11[k] * fx;
+        a[k] = top * (1.0f - fy) + bot * fy;
+      }
+      float rgb[3] = {bg[0], bg[1], bg[2]};
+      if (!(a[3] < 0.00001f)) {
+        const float avg[3] = {a[0] / a[3], a[1] / a[3], a[2] / a[3]};
+        const float luma = (avg[0] * 0.2126f + avg[1] * 0.7152f) + avg[2] * 0.0722f;
+        const float density = sqrtf(a[3] / (a[3] + 1.0f));
+        for (int k = 0; k < 3; k++) {
+          const float vivid = fmaxf(0.0f, o_mix(luma, avg[k], 1.16f));
+          const float mapped = 1.0f - expf(-vivid * density * 1.58f);
+          rgb[k] = powf(clampf(mapped + bg[k], 0.0f, 1.0f), 0.82f);
+        }
+      }
+      uint8_t *o = rgba + 4u * ((size_t)y * W + x);
+      for (int k = 0; k < 3; k++) o[k] = (uint8_t)lrintf(rgb[k] * 255.0f);
+      o[3] = 255;
+    }
+  free(ta);
+  free(tb);
+  free(acc);
+}
