@@ -311,8 +311,10 @@ __device__ __forceinline__ void integrate_body(const SceneDesc &S, float4 &p0, f
 //
 // kP2P: near field by exact pair sums over the leaf-sorted position snapshot;
 // no deposit (the end-of-step sort deposits the new positions).
+// Six resident CTAs per SM (40 registers): more warps to cover the latency of
+// the per-body dependent chain (measured: 6 CTAs beat 4 and 8).
 template <bool kP2P>
-__global__ void __launch_bounds__(256) k_integrate(const SceneDesc *__restrict__ scenes,
+__global__ void __launch_bounds__(256, 6) k_integrate(const SceneDesc *__restrict__ scenes,
                                                    const uint32_t *__restrict__ tile_scene,
                                                    float4 *__restrict__ part,
                                                    const uint4 *__restrict__ mom,
