@@ -1,5 +1,6 @@
 // Host engine implementation (see engine.h).
 #include "engine.h"
+#include "rfmm_math.h"
 
 #include <algorithm>
 #include <cmath>
@@ -1021,7 +1022,7 @@ int Engine::render(uint32_t scene, const rfmm_render_params &p, void *dst, size_
   cam.aspect = (float)((double)p.width / (double)std::max(1u, p.height));
   cam.exposure = p.exposure;
   cam.point_size = p.point_size;
-  cam.population_scale = 0.62f * std::pow(1048576.0f / std::max((float)cam.instances, 1.0f), 0.14f);
+  cam.population_scale = 0.62f * rf_powf(1048576.0f / std::max((float)cam.instances, 1.0f), 0.14f);
   const size_t texels = (size_t)cam.acc_w * cam.acc_h, pixels = (size_t)p.width * p.height;
   if (d_slot_of_ == nullptr) {
     const int st = alloc((void **)&d_slot_of_, 4ull * slots_);

@@ -17,6 +17,7 @@
 
 #include "rfmm_device.cuh"
 #include "rfmm_kernels.h"
+#include "rfmm_math.h"
 
 namespace rfmm {
 
@@ -230,7 +231,7 @@ __device__ __forceinline__ void integrate_body(const SceneDesc &S, float4 &p0, f
                   cdz = S.control_point[2] - pz;
       const float d2 = (cdx * cdx + cdy * cdy) + cdz * cdz;
       const float cr = fmaxf(S.control_radius, 0.02f);
-      control_influence = expf(-2.0f * d2 / (cr * cr));
+      control_influence = rf_expf(-2.0f * d2 / (cr * cr));
       const float strength = S.control_strength;
       const float inv = 1.0f / sqrtf(d2 + cr * cr * 0.018f);
       const float dirx = cdx * inv, diry = cdy * inv, dirz = cdz * inv;
@@ -632,10 +633,10 @@ __device__ __forceinline__ float random01(uint32_t seed) {
 }
 
 __device__ float seeded_enclosed_mass(float radius) {  // wgsl:216-230
-  const float bulge = 0.05f * powf(clampf_d(radius / 0.11f, 0.0f, 1.0f), 3.0f);
-  const float halo = 0.70f * powf(clampf_d(radius / 0.70f, 0.0f, 1.0f), 3.0f);
-  const float disc = 0.18f * powf(clampf_d((radius - 0.055f) / 0.60f, 0.0f, 1.0f), 1.0f / 0.72f);
-  const float polar = 0.07f * powf(clampf_d((radius - 0.22f) / 0.31f, 0.0f, 1.0f), 1.0f / 0.86f);
+  const float bulge = 0.05f * rf_powf(clampf_d(radius / 0.11f, 0.0f, 1.0f), 3.0f);
+  const float halo = 0.70f * rf_powf(clampf_d(radius / 0.70f, 0.0f, 1.0f), 3.0f);
+  const float disc = 0.18f * rf_powf(clampf_d((radius - 0.055f) / 0.60f, 0.0f, 1.0f), 1.0f / 0.72f);
+  const float polar = 0.07f * rf_powf(clampf_d((radius - 0.22f) / 0.31f, 0.0f, 1.0f), 1.0f / 0.86f);
   return fmaxf(bulge + halo + disc + polar, 0.0001f);
 }
 
@@ -660,13 +661,13 @@ __global__ void __launch_bounds__(256) k_initialize(const SceneDesc *__restrict_
   if (u5 < 0.75f) {
     const float z = u0 * 2.0f - 1.0f, phi = kTau * u1;
     const float outer = u5 < 0.05f ? 0.11f : 0.70f;
-    const float radius = outer * powf(u2, 0.3333333f);
+    const float radius = outer * rf_powf(u2, 0.3333333f);
     const float ring = sqrtf(fmaxf(0.0f, 1.0f - z * z));
-    const float rd[3] = {ring * cosf(phi), z, ring * sinf(phi)};
+    const float rd[3] = {ring * rf_cosf(phi), z, ring * rf_sinf(phi)};
     for (int k = 0; k < 3; k++) pos[k] = radius * rd[k];
     const float tz = u3 * 2.0f - 1.0f, tphi = kTau * u4;
     const float tring = sqrtf(fmaxf(0.0f, 1.0f - tz * tz));
-    const float rnd[3] = {tring * cosf(tphi), tz, tring * sinf(tphi)};
+    const float rnd[3] = {tring * rf_cosf(tphi), tz, tring * rf_sinf(tphi)};
     float tangent[3];
     cross3(rd, rnd, tangent);
     if (length3(tangent[0], tangent[1], tangent[2]) < 0.001f) {
@@ -682,34 +683,34 @@ __global__ void __launch_bounds__(256) k_initialize(const SceneDesc *__restrict_
     for (int k = 0; k < 3; k++) vel[k] = orbital * (tangent[k] / tl);
     excitation = u5 < 0.05f ? 0.09f : 0.025f + u4 * 0.025f;
   } else if (u5 < 0.93f) {
-    const float radius = 0.055f + 0.60f * powf(u0, 0.72f);
+    const float radius = 0.055f + 0.60f * rf_powf(u0, 0.72f);
     const float arm = (float)(i & 3u) * (kTau / 4.0f);
     const float angle = arm + radius * 7.8f + (u1 - 0.5f) * (0.045f + radius * 0.055f);
     const float thickness = (u2 + u3 + u4 - 1.5f) * (0.0035f + radius * 0.010f);
-    const float flat[3] = {radius * cosf(angle), radius * sinf(angle) * 0.72f, thickness};
+    const float flat[3] = {radius * rf_cosf(angle), radius * rf_sinf(angle) * 0.72f, thickness};
     const float tilt = 0.20f;
     pos[0] = flat[0];
-    pos[1] = flat[1] * cosf(tilt) - flat[2] * sinf(tilt);
-    pos[2] = flat[1] * sinf(tilt) + flat[2] * cosf(tilt);
+    pos[1] = flat[1] * rf_cosf(tilt) - flat[2] * rf_sinf(tilt);
+    pos[2] = flat[1] * rf_sinf(tilt) + flat[2] * rf_cosf(tilt);
     const float orbital = 0.99f * sqrtf(S.gravity * seeded_enclosed_mass(radius) / (radius + 0.018f));
-    const float tangent[3] = {-sinf(angle), cosf(angle) * 0.72f * cosf(tilt),
-                              cosf(angle) * 0.72f * sinf(tilt)};
+    const float tangent[3] = {-rf_sinf(angle), rf_cosf(angle) * 0.72f * rf_cosf(tilt),
+                              rf_cosf(angle) * 0.72f * rf_sinf(tilt)};
     const float pl = length3(pos[0], pos[1], pos[2]);
     const float tl = length3(tangent[0], tangent[1], tangent[2]);
-    const float sw = sinf(angle * 3.0f - radius * 13.0f);
+    const float sw = rf_sinf(angle * 3.0f - radius * 13.0f);
     for (int k = 0; k < 3; k++) vel[k] = orbital * (tangent[k] / tl) + (pos[k] / pl) * orbital * 0.035f * sw;
     excitation = 0.08f + u3 * 0.05f;
   } else {
     const float lineage = (float)(i & 3u);
-    const float radius = 0.22f + 0.31f * powf(u0, 0.86f) + (lineage - 1.5f) * 0.007f;
+    const float radius = 0.22f + 0.31f * rf_powf(u0, 0.86f) + (lineage - 1.5f) * 0.007f;
     const float angle = kTau * u1 + radius * 3.5f;
     const float thickness = (u2 + u3 + u4 - 1.5f) * (0.004f + radius * 0.009f);
-    const float flat[3] = {radius * cosf(angle), thickness, radius * sinf(angle)};
+    const float flat[3] = {radius * rf_cosf(angle), thickness, radius * rf_sinf(angle)};
     const float tilt = -0.54f + lineage * 0.36f;
-    pos[0] = flat[0] * cosf(tilt) - flat[1] * sinf(tilt);
-    pos[1] = flat[0] * sinf(tilt) + flat[1] * cosf(tilt);
+    pos[0] = flat[0] * rf_cosf(tilt) - flat[1] * rf_sinf(tilt);
+    pos[1] = flat[0] * rf_sinf(tilt) + flat[1] * rf_cosf(tilt);
     pos[2] = flat[2];
-    const float tangent[3] = {-sinf(angle) * cosf(tilt), -sinf(angle) * sinf(tilt), cosf(angle)};
+    const float tangent[3] = {-rf_sinf(angle) * rf_cosf(tilt), -rf_sinf(angle) * rf_sinf(tilt), rf_cosf(angle)};
     const float orbital = 0.99f * sqrtf(S.gravity * seeded_enclosed_mass(radius) / (radius + 0.018f));
     const float tl = length3(tangent[0], tangent[1], tangent[2]);
     for (int k = 0; k < 3; k++) vel[k] = -orbital * (tangent[k] / tl);
@@ -724,7 +725,7 @@ __global__ void __launch_bounds__(256) k_initialize(const SceneDesc *__restrict_
     float am[3];
     cross3(pos, vel, am);
     const float spin = am[1] / fmaxf(length3(am[0], am[1], am[2]), 0.0001f);
-    const float h = atan2f(vel[1], vel[0]) / kTau + (vel[2] / speed) * 0.14f + spin * 0.075f +
+    const float h = rf_atan2f(vel[1], vel[0]) / kTau + (vel[2] / speed) * 0.14f + spin * 0.075f +
                     radial_motion * 0.065f + excitation * 0.085f + (float)(i & 3u) * 0.018f;
     hue = h - floorf(h);
   }

@@ -18,6 +18,7 @@
 
 #include "rfmm_device.cuh"
 #include "rfmm_kernels.h"
+#include "rfmm_math.h"
 
 namespace rfmm {
 
@@ -111,8 +112,8 @@ __global__ void __launch_bounds__(256) k_splat(const SceneDesc *__restrict__ sce
   const float luminosity = 0.30f + excitation * 0.90f;
   const float speed_gain = 0.62f + fminf(velocity * 1.4f, 1.0f) * 0.30f;
   for (int k = 0; k < 3; k++) {
-    const float rainbow = 0.5f + 0.5f * cosf(kTau * (pl.w + phase[k]));
-    const float tint = powf(rainbow, 0.85f);
+    const float rainbow = 0.5f + 0.5f * rf_cosf(kTau * (pl.w + phase[k]));
+    const float tint = rf_powf(rainbow, 0.85f);
     const float s = mixf(sp[k] * tint, sp[k], heat);
     col[k] = s * (speed_gain + excitation * 0.90f) + heat * heat * 0.55f;
   }
@@ -122,7 +123,7 @@ __global__ void __launch_bounds__(256) k_splat(const SceneDesc *__restrict__ sce
     const float dx = S.control_point[0] - pl.x, dy = S.control_point[1] - pl.y,
                 dz = S.control_point[2] - pl.z;
     const float radius = fmaxf(S.control_radius, 0.02f);
-    influence = expf(-2.0f * ((dx * dx + dy * dy) + dz * dz) / (radius * radius));
+    influence = rf_expf(-2.0f * ((dx * dx + dy * dy) + dz * dz) / (radius * radius));
     const float mode = S.control_axis_mode[3];
     if (mode > 1.5f && mode < 2.5f) {
       cc[0] = 1.0f; cc[1] = 0.38f; cc[2] = 0.18f;
@@ -211,8 +212,8 @@ __global__ void __launch_bounds__(256) k_resolve(const float4 *__restrict__ tex,
     const float density = sqrtf(a.w / (a.w + 1.0f));
     for (int k = 0; k < 3; k++) {
       const float vivid = fmaxf(0.0f, mixf(luma, avg[k], 1.16f));
-      const float mapped = 1.0f - expf(-vivid * density * 1.58f);
-      rgb[k] = powf(clampf_d(mapped + bg[k], 0.0f, 1.0f), 0.82f);
+      const float mapped = 1.0f - rf_expf(-vivid * density * 1.58f);
+      rgb[k] = rf_powf(clampf_d(mapped + bg[k], 0.0f, 1.0f), 0.82f);
     }
   }
   out[(size_t)y * W + x] = make_uchar4((unsigned char)__float2int_rn(rgb[0] * 255.0f),

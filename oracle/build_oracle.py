@@ -12,6 +12,9 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "rfmm_oracle.c")
+# The contract's transcendental functions, shared with the kernels.
+MATH_DIR = os.path.join(os.path.dirname(HERE), "fmm-rainbow_gb300", "csrc")
+MATH_H = os.path.join(MATH_DIR, "rfmm_math.h")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "librfmm_oracle.so")
 
@@ -35,10 +38,11 @@ def build(force: bool = False, quiet: bool = True) -> str:
     os.makedirs(OUT_DIR, exist_ok=True)
     if (not force and os.path.exists(LIB)
             and os.path.getmtime(LIB) >= os.path.getmtime(SRC)
+            and os.path.getmtime(LIB) >= os.path.getmtime(MATH_H)
             and os.path.getmtime(LIB) >= os.path.getmtime(__file__)):
         return LIB
     tmp = LIB + ".tmp%d" % os.getpid()
-    cmd = ["gcc", *CFLAGS, SRC, "-o", tmp, "-lm"]
+    cmd = ["gcc", *CFLAGS, "-I", MATH_DIR, SRC, "-o", tmp, "-lm"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError("oracle build failed:\n%s\n%s" % (" ".join(cmd), res.stderr))

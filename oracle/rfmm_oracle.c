@@ -33,8 +33,11 @@
  *     a*(1-t) + b*t; smoothstep(l, h, x) with t = clamp((x-l)/(h-l), 0, 1)
  *     and t*t*(3-2t); fract(x) = x - floor(x);
  *   - integer moment sums wrap modulo 2^32 (i32 atomics in the reference).
- * Transcendentals of `initialize` (and of the optional control field) use
- * libm and are therefore matched by tolerance, not bit for bit.
+ * The transcendentals of `initialize`, of the control field and of the display
+ * passes are not the reference's (WGSL leaves them implementation-defined) but
+ * the contract's own binary32 functions (fmm-rainbow_gb300/csrc/rfmm_math.h,
+ * shared with the kernels; their accuracy against libm is tested separately),
+ * so those paths match the GPU bit for bit too.
  *
  * Pinning: the planner is pinned to the reference's own unit tests
  * (src/lib.rs:163-217).  The reference keeps no golden outputs for the
@@ -47,6 +50,8 @@
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
+
+#include "rfmm_math.h" /* the contract's sin/cos/exp/pow/atan2, shared with the kernels */
 
 #ifdef _OPENMP
 #include <omp.h>
@@ -638,7 +643,7 @@ void oracle_integrate(OParticle *particles, const OMoment *moments, const OField
       for (int k = 0; k < 3; k++) cd[k] = P->control_point[k] - pos[k];
       const float d2 = (cd[0] * cd[0] + cd[1] * cd[1]) + cd[2] * cd[2];
       const float cr = fmaxf(P->control_radius, 0.02f);
-      control_influence = expf(-2.0f * d2 / (cr * cr));
+      control_influence = rf_expf(-2.0f * d2 / (cr * cr));
       const float strength = P->control_strength;
       const float inv = 1.0f / sqrtf(d2 + cr * cr * 0.018f);
       float dir[3] = {cd[0] * inv, cd[1] * inv, cd[2] * inv};
@@ -724,10 +729,10 @@ static uint32_t hash32(uint32_t x) { /* wgsl:205-210 */
 static float random01(uint32_t seed) { return (float)hash32(seed) * (1.0f / 4294967296.0f); }
 
 static float seeded_enclosed_mass(float radius) { /* wgsl:216-230 */
-  float bulge = 0.05f * powf(clampf(radius / 0.11f, 0.0f, 1.0f), 3.0f);
-  float halo = 0.70f * powf(clampf(radius / 0.70f, 0.0f, 1.0f), 3.0f);
-  float disc = 0.18f * powf(clampf((radius - 0.055f) / 0.60f, 0.0f, 1.0f), 1.0f / 0.72f);
-  float polar = 0.07f * powf(clampf((radius - 0.22f) / 0.31f, 0.0f, 1.0f), 1.0f / 0.86f);
+  float bulge = 0.05f * rf_powf(clampf(radius / 0.11f, 0.0f, 1.0f), 3.0f);
+  float halo = 0.70f * rf_powf(clampf(radius / 0.70f, 0.0f, 1.0f), 3.0f);
+  float disc = 0.18f * rf_powf(clampf((radius - 0.055f) / 0.60f, 0.0f, 1.0f), 1.0f / 0.72f);
+  float polar = 0.07f * rf_powf(clampf((radius - 0.22f) / 0.31f, 0.0f, 1.0f), 1.0f / 0.86f);
   return fmaxf(bulge + halo + disc + polar, 0.0001f);
 }
 
@@ -748,13 +753,13 @@ void oracle_initialize(OParticle *particles, const OParams *P) { /* wgsl:232-374
     if (u5 < 0.75f) {
       float z = u0 * 2.0f - 1.0f, phi = O_TAU * u1;
       float outer = u5 < 0.05f ? 0.11f : 0.70f;
-      float radius = outer * powf(u2, 0.3333333f);
+      float radius = outer * rf_powf(u2, 0.3333333f);
       float ring = sqrtf(fmaxf(0.0f, 1.0f - z * z));
-      float rd[3] = {ring * cosf(phi), z, ring * sinf(phi)};
+      float rd[3] = {ring * rf_cosf(phi), z, ring * rf_sinf(phi)};
       for (int k = 0; k < 3; k++) pos[k] = radius * rd[k];
       float tz = u3 * 2.0f - 1.0f, tphi = O_TAU * u4;
       float tring = sqrtf(fmaxf(0.0f, 1.0f - tz * tz));
-      float rnd[3] = {tring * cosf(tphi), tz, tring * sinf(tphi)};
+      float rnd[3] = {tring * rf_cosf(tphi), tz, tring * rf_sinf(tphi)};
       float tangent[3];
       cross3(rd, rnd, tangent);
       if (length3(tangent) < 0.001f) {
@@ -770,34 +775,34 @@ void oracle_initialize(OParticle *particles, const OParams *P) { /* wgsl:232-374
       for (int k = 0; k < 3; k++) vel[k] = orbital * (tangent[k] / tl);
       excitation = u5 < 0.05f ? 0.09f : 0.025f + u4 * 0.025f;
     } else if (u5 < 0.93f) {
-      float radius = 0.055f + 0.60f * powf(u0, 0.72f);
+      float radius = 0.055f + 0.60f * rf_powf(u0, 0.72f);
       float arm = (float)(i & 3u) * (O_TAU / 4.0f);
       float angle = arm + radius * 7.8f + (u1 - 0.5f) * (0.045f + radius * 0.055f);
       float thickness = (u2 + u3 + u4 - 1.5f) * (0.0035f + radius * 0.010f);
-      float flat[3] = {radius * cosf(angle), radius * sinf(angle) * 0.72f, thickness};
+      float flat[3] = {radius * rf_cosf(angle), radius * rf_sinf(angle) * 0.72f, thickness};
       float tilt = 0.20f;
       pos[0] = flat[0];
-      pos[1] = flat[1] * cosf(tilt) - flat[2] * sinf(tilt);
-      pos[2] = flat[1] * sinf(tilt) + flat[2] * cosf(tilt);
+      pos[1] = flat[1] * rf_cosf(tilt) - flat[2] * rf_sinf(tilt);
+      pos[2] = flat[1] * rf_sinf(tilt) + flat[2] * rf_cosf(tilt);
       float orbital = 0.99f * sqrtf(P->gravity * seeded_enclosed_mass(radius) / (radius + 0.018f));
-      float tangent[3] = {-sinf(angle), cosf(angle) * 0.72f * cosf(tilt),
-                          cosf(angle) * 0.72f * sinf(tilt)};
+      float tangent[3] = {-rf_sinf(angle), rf_cosf(angle) * 0.72f * rf_cosf(tilt),
+                          rf_cosf(angle) * 0.72f * rf_sinf(tilt)};
       float pl = length3(pos), tl = length3(tangent);
-      float sw = sinf(angle * 3.0f - radius * 13.0f);
+      float sw = rf_sinf(angle * 3.0f - radius * 13.0f);
       for (int k = 0; k < 3; k++)
         vel[k] = orbital * (tangent[k] / tl) + (pos[k] / pl) * orbital * 0.035f * sw;
       excitation = 0.08f + u3 * 0.05f;
     } else {
       float lineage = (float)(i & 3u);
-      float radius = 0.22f + 0.31f * powf(u0, 0.86f) + (lineage - 1.5f) * 0.007f;
+      float radius = 0.22f + 0.31f * rf_powf(u0, 0.86f) + (lineage - 1.5f) * 0.007f;
       float angle = O_TAU * u1 + radius * 3.5f;
       float thickness = (u2 + u3 + u4 - 1.5f) * (0.004f + radius * 0.009f);
-      float flat[3] = {radius * cosf(angle), thickness, radius * sinf(angle)};
+      float flat[3] = {radius * rf_cosf(angle), thickness, radius * rf_sinf(angle)};
       float tilt = -0.54f + lineage * 0.36f;
-      pos[0] = flat[0] * cosf(tilt) - flat[1] * sinf(tilt);
-      pos[1] = flat[0] * sinf(tilt) + flat[1] * cosf(tilt);
+      pos[0] = flat[0] * rf_cosf(tilt) - flat[1] * rf_sinf(tilt);
+      pos[1] = flat[0] * rf_sinf(tilt) + flat[1] * rf_cosf(tilt);
       pos[2] = flat[2];
-      float tangent[3] = {-sinf(angle) * cosf(tilt), -sinf(angle) * sinf(tilt), cosf(angle)};
+      float tangent[3] = {-rf_sinf(angle) * rf_cosf(tilt), -rf_sinf(angle) * rf_sinf(tilt), rf_cosf(angle)};
       float orbital = 0.99f * sqrtf(P->gravity * seeded_enclosed_mass(radius) / (radius + 0.018f));
       float tl = length3(tangent);
       for (int k = 0; k < 3; k++) vel[k] = -orbital * (tangent[k] / tl);
@@ -812,7 +817,7 @@ void oracle_initialize(OParticle *particles, const OParams *P) { /* wgsl:232-374
       float am[3];
       cross3(pos, vel, am);
       float spin = am[1] / fmaxf(length3(am), 0.0001f);
-      hue = fractf(atan2f(vel[1], vel[0]) / O_TAU + (vel[2] / speed) * 0.14f + spin * 0.075f +
+      hue = fractf(rf_atan2f(vel[1], vel[0]) / O_TAU + (vel[2] / speed) * 0.14f + spin * 0.075f +
                    radial_motion * 0.065f + excitation * 0.085f + (float)(i & 3u) * 0.018f);
     }
     OParticle *p = &particles[ii];
@@ -949,8 +954,7 @@ int oracle_set_threads(int n) {
 /* Headless restatement of the display passes (wgsl:780-1009, app.js:650-710)
  * with the product's definitions: per-pixel fixed-point accumulation at 2^24
  * units per 1.0 (order-independent), binary32 blur and resolve intermediates,
- * exact bilinear weights, RGBA8 output with row 0 at the top.  Transcendentals
- * are libm's, so the image matches the GPU's by tolerance. */
+ * exact bilinear weights, RGBA8 output with row 0 at the top. */
 typedef struct {
   uint32_t width, height, instances;
   float yaw, pitch, zoom, point_size, exposure;
@@ -983,7 +987,7 @@ void oracle_render(const OParticle *particles, const OParams *P, const ORenderPa
   const float cyw = (float)cos((double)R->yaw), syw = (float)sin((double)R->yaw);
   const float cpt = (float)cos((double)R->pitch), spt = (float)sin((double)R->pitch);
   const float aspect = (float)((double)W / (double)(H > 1u ? H : 1u));
-  const float pop = 0.62f * powf(1048576.0f / fmaxf((float)instances, 1.0f), 0.14f);
+  const float pop = 0.62f * rf_powf(1048576.0f / fmaxf((float)instances, 1.0f), 0.14f);
   uint64_t *acc = (uint64_t *)calloc((size_t)aw * ah * 4u, sizeof(uint64_t));
   for (uint32_t i = 0; i < instances && P->n > 0u; i++) {
     const OParticle *pt = &particles[(i * 747796405u + 2891336453u) % P->n];
@@ -1011,8 +1015,8 @@ void oracle_render(const OParticle *particles, const OParams *P, const ORenderPa
     const float speed_gain = 0.62f + fminf(velocity * 1.4f, 1.0f) * 0.30f;
     float col[3];
     for (int k = 0; k < 3; k++) {
-      const float rainbow = 0.5f + 0.5f * cosf(O_TAU * (pt->hue + phase[k]));
-      const float tint = powf(rainbow, 0.85f);
+      const float rainbow = 0.5f + 0.5f * rf_cosf(O_TAU * (pt->hue + phase[k]));
+      const float tint = rf_powf(rainbow, 0.85f);
       const float s = o_mix(sp[k] * tint, sp[k], heat);
       col[k] = s * (speed_gain + excitation * 0.90f) + heat * heat * 0.55f;
     }
@@ -1021,7 +1025,7 @@ void oracle_render(const OParticle *particles, const OParams *P, const ORenderPa
       const float dx = P->control_point[0] - pos[0], dy = P->control_point[1] - pos[1],
                   dz = P->control_point[2] - pos[2];
       const float radius = fmaxf(P->control_radius, 0.02f);
-      influence = expf(-2.0f * ((dx * dx + dy * dy) + dz * dz) / (radius * radius));
+      influence = rf_expf(-2.0f * ((dx * dx + dy * dy) + dz * dz) / (radius * radius));
       const float mode = P->control_axis_mode[3];
       if (mode > 1.5f && mode < 2.5f) {
         cc[0] = 1.0f; cc[1] = 0.38f; cc[2] = 0.18f;
@@ -1102,8 +1106,8 @@ void oracle_render(const OParticle *particles, const OParams *P, const ORenderPa
         const float density = sqrtf(a[3] / (a[3] + 1.0f));
         for (int k = 0; k < 3; k++) {
           const float vivid = fmaxf(0.0f, o_mix(luma, avg[k], 1.16f));
-          const float mapped = 1.0f - expf(-vivid * density * 1.58f);
-          rgb[k] = powf(clampf(mapped + bg[k], 0.0f, 1.0f), 0.82f);
+          const float mapped = 1.0f - rf_expf(-vivid * density * 1.58f);
+          rgb[k] = rf_powf(clampf(mapped + bg[k], 0.0f, 1.0f), 0.82f);
         }
       }
       uint8_t *o = rgba + 4u * ((size_t)y * W + x);

@@ -3,9 +3,9 @@
 The solver is called through its C ABI (include/rfmm.h, via ctypes).  The
 bar is bit-exact for the integer tree (moments, occupancy) and, because the
 kernels follow the oracle's floating-point contract (binary32,
-round-to-nearest, no contraction, IEEE div/sqrt, reference loop order), also
-bit-exact for fields and particles on the default path.  Transcendental
-paths (galaxy seed, control field) are checked against a tolerance.
+round-to-nearest, no contraction, IEEE div/sqrt, reference loop order, the
+contract's own sin/cos/exp/pow/atan2), also bit-exact for fields and
+particles, the galaxy seed and the control field.
 """
 import numpy as np
 import pytest
@@ -78,24 +78,27 @@ def test_steps_bit_exact(rfmm_mod, oracle_mod, kind, n):
 
 
 def test_galaxy_seed_digest_solve(rfmm_mod, oracle_mod):
-    """The reference harness's own scene (native/main.rs:423-454)."""
+    """The reference harness's own scene (native/main.rs:423-454): the seed,
+    the field solve and two steps, bit for bit (the seed's sin/cos/pow/atan2
+    are the contract's own functions on both sides)."""
     O, R = oracle_mod, rfmm_mod
     n = 65536
     with R.Solver(n) as s:  # harness defaults: dt 0.0009, G 0.34, eps 0.012
         s.seed_galaxy()
         gp = s.particles()
         ref = O.initialize(n)
-        # libm vs CUDA transcendentals: positions agree to a few ulp.
-        d = np.abs(gp["pos"] - ref["pos"]).max()
-        assert d < 1e-5, d
-        dv = np.abs(gp["vel"] - ref["vel"]).max()
-        assert dv < 1e-4, dv
-        # From the GPU's own seed, the solve is bit-exact.
-        st = O.OracleState(gp, O.make_params(n))
+        _assert_same(gp, ref, "seeded particles")
+        st = O.OracleState(ref, O.make_params(n))
         st.solve_fields()
         s.solve_fields()
         _assert_same(s.moments(), st.moments, "moments")
         _assert_same(s.fields(), st.fields, "fields")
+        assert s.digest(R.BUF_FIELDS) == O.fnv1a(st.fields)
+        st = O.OracleState(ref, O.make_params(n))
+        st.step(2)
+        s.seed_galaxy()
+        s.step(2)
+        _assert_same(s.particles(), st.particles, "particles after 2 steps")
 
 
 def _edge_scene(name):
@@ -159,26 +162,23 @@ def test_params_speed_depth_override_bit_exact(rfmm_mod, oracle_mod):
 
 
 @pytest.mark.parametrize("mode", [1.0, 2.0, 3.0])
-def test_control_field_within_tolerance(rfmm_mod, oracle_mod, mode):
-    """The shepherd field uses expf: matched within 1e-5 relative rms."""
+def test_control_field_bit_exact(rfmm_mod, oracle_mod, mode):
+    """Pull, push and vortex shepherd fields (wgsl:659-689), bit for bit."""
     O, R = oracle_mod, rfmm_mod
     from rfmm import scenes
     n = 20000
-    p = scenes.plummer(n, seed=13)
+    p = scenes.make("plummer", n, 13)
     cp, ax = (0.5, 0.55, 0.5, 1.0), (0.0, 1.0, 0.3, mode)
     st = O.OracleState(p, O.make_params(n, gravity=1.0, softening=1e-3, dt=5e-4, control_point=cp,
                                         control_axis_mode=ax, control_strength=2.0, control_radius=0.2))
-    st.step(1)
+    st.step(2)
     prm = R.default_params(gravity=1.0, softening=1e-3, dt=5e-4, control_point=cp,
                            control_axis_mode=ax, control_strength=2.0, control_radius=0.2)
     with R.Solver(n, prm) as s:
         s.upload(p)
-        s.step(1)
-        g = s.particles()
-    dv = g["vel"].astype(np.float64) - st.particles["vel"]
-    rel = np.sqrt((dv ** 2).sum() / (st.particles["vel"].astype(np.float64) ** 2).sum())
-    assert rel < 1e-5, rel
-    assert np.abs(g["pos"] - st.particles["pos"]).max() < 1e-6
+        s.step(2)
+        _assert_same(s.particles(), st.particles, "particles")
+        _assert_same(s.fields(), st.fields, "fields")
 
 
 def test_golden_digests_on_gpu(rfmm_mod, oracle_mod):
@@ -191,14 +191,18 @@ def test_golden_digests_on_gpu(rfmm_mod, oracle_mod):
     gold = json.load(open(os.path.join(here, "golden", "oracle_digests.json")))
     checked = 0
     for name, g in sorted(gold.items()):
-        if g["kind"] == "galaxy":
-            continue  # libm-seeded scene; covered by test_galaxy_seed_digest_solve
-        p = make_golden.scene(g["kind"], g["n"], g["seed"])
-        if O.fnv1a(p) != g["input_particles"]:
-            continue  # this platform's scene generator differs in the last bits
+        galaxy = g["kind"] == "galaxy"
+        p = None if galaxy else make_golden.scene(g["kind"], g["n"], g["seed"])
+        if not galaxy and O.fnv1a(p) != g["input_particles"]:
+            continue  # this platform's numpy scene generator differs in the last bits
         prm = R.default_params(gravity=g["gravity"], softening=g["softening"], dt=g["dt"])
         with R.Solver(g["n"], prm) as s:
-            s.upload(p)
+            if galaxy:  # seeded on the GPU
+                s.seed_galaxy()
+                assert s.digest(R.BUF_PARTICLES) == g["input_particles"], name
+                p = s.particles()
+            else:
+                s.upload(p)
             s.solve_fields()
             assert s.digest(R.BUF_MOMENTS) == g["solve_moments"], name
             assert s.digest(R.BUF_FIELDS) == g["solve_fields"], name
