@@ -212,6 +212,9 @@ int Engine::create(const std::vector<SceneSpec> &specs, Engine **out) {
     t.resort_interval = E->use_lists_ ? 0u : 16u;  // slots are sorted when they are filled
     t.graph_steps = 16;
     t.pdl = 1;
+    // Many scenes per engine make M2L throughput-bound, where the compacting
+    // variant is faster; one scene is latency-bound, where it is not.
+    t.m2l_compact = specs.size() > 1u ? 1u : 0u;
     if (e == cudaSuccess) e = E->set_tuning(t) == RFMM_OK ? cudaSuccess : cudaErrorInvalidValue;
   }
   if (e == cudaSuccess)
@@ -333,7 +336,7 @@ int Engine::set_tuning(const rfmm_tuning &t) {
   if (t.upward_ctas_per_sm < 1u || t.upward_ctas_per_sm > 16u || t.m2l_ctas_per_sm < 1u ||
       t.m2l_ctas_per_sm > 6u || t.l2l_ctas_per_sm < 1u || t.l2l_ctas_per_sm > 8u ||
       t.integrate_ctas_per_sm < 1u || t.integrate_ctas_per_sm > body_limit_ || t.graph_steps < 1u ||
-      t.graph_steps > 64u || t.integrate_dynamic > 1u || t.pdl > 1u)
+      t.graph_steps > 64u || t.integrate_dynamic > 1u || t.pdl > 1u || t.m2l_compact > 1u)
     return RFMM_ERR_INVALID;
   clear_graphs();  // captured launch shapes change
   tuning_ = t;
@@ -372,7 +375,7 @@ int Engine::autotune(uint32_t steps_per_trial, rfmm_tuning *best) {
   int st = trial(cur, &cur_ms);
   // Coordinate descent, two sweeps over the knobs.
   for (int sweep = 0; sweep < 2 && st == RFMM_OK; sweep++) {
-    for (int knob = 0; knob < 8 && st == RFMM_OK; knob++) {
+    for (int knob = 0; knob < 9 && st == RFMM_OK; knob++) {
       std::vector<uint32_t> values;
       switch (knob) {
         case 0: values = {2, 4, 6, 8}; break;
@@ -385,12 +388,13 @@ int Engine::autotune(uint32_t steps_per_trial, rfmm_tuning *best) {
         case 7:
           if (!use_lists_) values = {8, 16, 32, 64};  // serving slots are sorted on admission
           break;
+        case 8: values = {0, 1}; break;
       }
       for (uint32_t v : values) {
         rfmm_tuning t = cur;
-        uint32_t *field[8] = {&t.upward_ctas_per_sm, &t.m2l_ctas_per_sm, &t.l2l_ctas_per_sm,
+        uint32_t *field[9] = {&t.upward_ctas_per_sm, &t.m2l_ctas_per_sm, &t.l2l_ctas_per_sm,
                               &t.integrate_ctas_per_sm, &t.integrate_dynamic, &t.pdl,
-                              &t.graph_steps, &t.resort_interval};
+                              &t.graph_steps, &t.resort_interval, &t.m2l_compact};
         if (*field[knob] == v) continue;
         *field[knob] = v;
         float ms = 0.0f;
@@ -436,6 +440,7 @@ LaunchCtx Engine::ctx(uint32_t mpar, uint32_t lpar, uint32_t ppar) const {
   L.m2l_ctas = (uint32_t)sms_ * tuning_.m2l_ctas_per_sm;
   L.l2l_ctas = (uint32_t)sms_ * tuning_.l2l_ctas_per_sm;
   L.integrate_dynamic = tuning_.integrate_dynamic != 0u;
+  L.m2l_compact = tuning_.m2l_compact != 0u;
   L.tile_list = use_lists_ ? d_tile_list_ : nullptr;
   L.task_list = use_lists_ ? d_task_list_ : nullptr;
   L.pdl = pdl_;

@@ -28,6 +28,8 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "rfmm_device.cuh"
 #include "rfmm_kernels.h"
 
@@ -277,6 +279,21 @@ struct M2LShared {
   float vals[8][10][kSlotStride];
 };
 
+// The compacting variant: each child's contributing slots are listed first and
+// evaluated 32 at a time (fewer evaluation rounds and additions when many
+// slots are empty, one more pass over the stencil to build the lists).
+constexpr uint32_t kRound = 32u;
+constexpr uint32_t kRoundStride = 33u;
+struct M2LCompactShared {
+  float4 tile[kTileCells];
+  unsigned long long mbar;
+  uint32_t stop;
+  uint32_t live[8];
+  uint32_t nvalid[8];            // contributing stencil slots of each child
+  uint8_t slots[8][kTileCells];  // those slots, in the reference's loop order
+  float vals[8][10][kRoundStride];
+};
+
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
@@ -317,6 +334,7 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, i
       : "memory");
 }
 
+template <bool kCompact>
 __global__ void __launch_bounds__(256) k_m2l(const SceneDesc *__restrict__ scenes,
                                              const WorkItem *__restrict__ plist, uint32_t plist_cap,
                                              Counters *__restrict__ ctr, uint32_t list_par,
@@ -328,7 +346,8 @@ __global__ void __launch_bounds__(256) k_m2l(const SceneDesc *__restrict__ scene
   // The TMA destination must be 128-byte aligned: align the carve-out by hand
   // (the launch reserves 128 spare bytes).
   const uint32_t pad = (128u - (smem_u32(smem_raw) & 127u)) & 127u;
-  M2LShared &sh = *reinterpret_cast<M2LShared *>(smem_raw + pad);
+  using Shared = typename std::conditional<kCompact, M2LCompactShared, M2LShared>::type;
+  Shared &sh = *reinterpret_cast<Shared *>(smem_raw + pad);
   const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
   if (tid == 0) {
     mbar_init(&sh.mbar, 1u);
@@ -375,6 +394,70 @@ __global__ void __launch_bounds__(256) k_m2l(const SceneDesc *__restrict__ scene
     __syncthreads();
     if (sh.stop) return;
 
+    float acc = 0.0f;  // running sum of (child tid/10, component tid%10)
+    if constexpr (kCompact) {
+    // Warp w handles child w of the parent.  It first lists the stencil
+    // slots that contribute (not adjacent to the child, non-empty source), in
+    // the reference's loop order; then rounds of 32 listed slots are
+    // evaluated, one per lane, and 80 threads (8 children x 10 components)
+    // add each round to their running sums in list order.  Skipped slots
+    // would add +0, which cannot change a sum that starts at +0.
+    const int cx = (int)(warp & 1u), cy = (int)((warp >> 1) & 1u), cz = (int)(warp >> 2);
+    const uint32_t tx = (uint32_t)(2 * pcx + cx), ty = (uint32_t)(2 * pcy + cy), tz = (uint32_t)(2 * pcz + cz);
+    const uint32_t target = lvl_base + lin3(tx, ty, tz, dim);
+    const bool live = mom[target].x != 0u;  // empty children are not targets
+    const float ctx = cell_center_lv(tx, l), cty = cell_center_lv(ty, l), ctz = cell_center_lv(tz, l);
+    const float eps = (0.06f * kHalf) * pow2_neg(l);  // wgsl:507, / 2^l as an exact scaling
+    uint32_t nv = 0u;
+    if (live) {
+      for (uint32_t k0 = 0; k0 < kTileCells; k0 += 32u) {
+        const uint32_t k = k0 + lane;
+        bool use = false;
+        uint32_t cell = 0u;
+        if (k < kTileCells) {
+          // Reference loop order: source parent (pz, py, px) then child (cz, cy, cx).
+          const uint32_t pidx = k >> 3, ch = k & 7u;
+          const int ux = 2 * (int)(pidx % 3u) + (int)(ch & 1u);
+          const int uy = 2 * (int)((pidx / 3u) % 3u) + (int)((ch >> 1) & 1u);
+          const int uz = 2 * (int)(pidx / 9u) + (int)(ch >> 2);
+          // Source child coordinate minus target coordinate = u - 2 - child.
+          const int sx = ux - 2 - cx, sy = uy - 2 - cy, sz = uz - 2 - cz;
+          const bool near = sx >= -1 && sx <= 1 && sy >= -1 && sy <= 1 && sz >= -1 && sz <= 1;
+          cell = (uint32_t)(ux + 6 * (uy + 6 * uz));
+          use = !near && sh.tile[cell].w != 0.0f;
+        }
+        const uint32_t mask = __ballot_sync(0xFFFFFFFFu, use);
+        if (use) sh.slots[warp][nv + __popc(mask & ((1u << lane) - 1u))] = (uint8_t)cell;
+        nv += __popc(mask);
+      }
+    }
+    if (lane == 0) {
+      sh.live[warp] = live ? target : 0xFFFFFFFFu;
+      sh.nvalid[warp] = nv;
+    }
+    __syncthreads();
+    uint32_t rounds = 0u;
+#pragma unroll
+    for (uint32_t w = 0; w < 8u; w++) rounds = max(rounds, (sh.nvalid[w] + kRound - 1u) / kRound);
+    const uint32_t my_n = tid < 80u ? sh.nvalid[tid / 10u] : 0u;
+    for (uint32_t r = 0; r < rounds; r++) {
+      const uint32_t j = r * kRound + lane;
+      if (j < nv) {
+        const uint32_t cell = sh.slots[warp][j];
+        float out[10];
+        pair_field_d(sh.tile[cell], ctx, cty, ctz, eps, out);
+#pragma unroll
+        for (int c = 0; c < 10; c++) sh.vals[warp][c][lane] = out[c];
+      }
+      __syncthreads();
+      if (tid < 80u && r * kRound < my_n) {
+        const float *row = sh.vals[tid / 10u][tid % 10u];
+        const uint32_t m = min(kRound, my_n - r * kRound);
+        for (uint32_t kk = 0; kk < m; kk++) acc = acc + row[kk];
+      }
+      __syncthreads();
+    }
+    } else {
     // Warp w evaluates the stencil of child w of the parent, a chunk of slots
     // at a time; 80 threads (8 children x 10 components) then add the chunk to
     // their running sums, strictly in slot order.
@@ -385,7 +468,6 @@ __global__ void __launch_bounds__(256) k_m2l(const SceneDesc *__restrict__ scene
     if (lane == 0) sh.live[warp] = live ? target : 0xFFFFFFFFu;
     const float ctx = cell_center_lv(tx, l), cty = cell_center_lv(ty, l), ctz = cell_center_lv(tz, l);
     const float eps = (0.06f * kHalf) * pow2_neg(l);  // wgsl:507, / 2^l as an exact scaling
-    float acc = 0.0f;                                 // running sum of (child tid/10, comp tid%10)
     for (uint32_t c0 = 0; c0 < kTileCells; c0 += kChunk) {
       if (live) {
         for (uint32_t kk = lane; kk < kChunk; kk += 32u) {
@@ -417,6 +499,7 @@ __global__ void __launch_bounds__(256) k_m2l(const SceneDesc *__restrict__ scene
         for (uint32_t kk = 0; kk < kChunk; kk++) acc = acc + row[kk];
       }
       __syncthreads();
+    }
     }
     if (tid < 96u) {
       const uint32_t t = tid < 80u ? tid / 10u : (tid - 80u) >> 1;
@@ -543,10 +626,13 @@ void launch_upward(const LaunchCtx &L, uint32_t list_par, uint32_t tasks) {
                      L.plist_cap, L.plist_prev, L.ctr, list_par, L.tickets);
 }
 
-size_t m2l_smem_bytes() { return sizeof(M2LShared) + 128; }
+size_t m2l_smem_bytes(bool compact) {
+  return (compact ? sizeof(M2LCompactShared) : sizeof(M2LShared)) + 128;
+}
 
 void launch_m2l(const LaunchCtx &L, uint32_t list_par) {
-  launch_step_kernel(L, k_m2l, dim3(L.m2l_ctas), dim3(256), m2l_smem_bytes(), L.scenes,
+  launch_step_kernel(L, L.m2l_compact ? k_m2l<true> : k_m2l<false>, dim3(L.m2l_ctas), dim3(256),
+                     m2l_smem_bytes(L.m2l_compact), L.scenes,
                      (const WorkItem *)L.plist, L.plist_cap, L.ctr, list_par, (const uint4 *)L.mom,
                      (const float4 *)L.src, L.lfield, L.tmaps);
 }
@@ -558,8 +644,12 @@ void launch_l2l_near(const LaunchCtx &L, uint32_t list_par) {
 }
 
 cudaError_t configure_tree_kernels() {
-  return cudaFuncSetAttribute(k_m2l, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)m2l_smem_bytes());
+  cudaError_t e = cudaFuncSetAttribute(k_m2l<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)m2l_smem_bytes(false));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_m2l<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)m2l_smem_bytes(true));
+  return e;
 }
 
 }  // namespace rfmm

@@ -36,6 +36,7 @@ struct LaunchCtx {
   uint32_t m2l_ctas;           // persistent grid of the M2L pass
   uint32_t l2l_ctas;           // persistent grid of the L2L + near pass
   bool integrate_dynamic;      // integrate CTAs grab tiles from a counter
+  bool m2l_compact;            // M2L variant that lists contributing slots first
   const uint32_t *tile_list;   // active body tiles (null: every tile)
   const uint32_t *task_list;   // active upward tasks (null: every task)
   bool pdl;                    // launch step kernels with programmatic stream serialization

@@ -73,7 +73,7 @@ class Tuning(C.Structure):
     _fields_ = [("upward_ctas_per_sm", C.c_uint32), ("m2l_ctas_per_sm", C.c_uint32),
                 ("l2l_ctas_per_sm", C.c_uint32), ("integrate_ctas_per_sm", C.c_uint32),
                 ("integrate_dynamic", C.c_uint32), ("resort_interval", C.c_uint32),
-                ("graph_steps", C.c_uint32), ("pdl", C.c_uint32)]
+                ("graph_steps", C.c_uint32), ("pdl", C.c_uint32), ("m2l_compact", C.c_uint32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -223,7 +223,7 @@ def test_tuning_never_changes_results(rfmm_mod, oracle_mod):
     p = scenes.plummer(n, seed=21)
     st = O.OracleState(p, _oracle_params(O, n))
     st.step(6)
-    variants = [dict(), dict(integrate_dynamic=1, graph_steps=4, pdl=0),
+    variants = [dict(), dict(integrate_dynamic=1, graph_steps=4, pdl=0, m2l_compact=1),
                 dict(upward_ctas_per_sm=2, m2l_ctas_per_sm=1, l2l_ctas_per_sm=1,
                      integrate_ctas_per_sm=1, resort_interval=3, graph_steps=1)]
     for v in variants:
