@@ -512,7 +512,12 @@ int Engine::commit_scene(uint32_t scene) {
   LaunchCtx L = ctx(mcur_, lpar_, pcur_);
   launch_keys(L, sort_.keys[0], sort_.vals[0], nullptr, 0, tiles, d.tile_off);
   const int r = radix_sort(stream_, sort_, tiles * kTile, 3u * d.key_level);
+  // A rebuilt scene starts from cleared moment, source and record buffers (the
+  // upward pass skips subtrees that are empty in both moment buffers).
   RF_CK(cudaMemsetAsync(d_mom_[mcur_] + d.cell_off, 0, 16ull * d.cells, stream_));
+  RF_CK(cudaMemsetAsync(d_mom_[mcur_ ^ 1u] + d.cell_off, 0, 16ull * d.cells, stream_));
+  RF_CK(cudaMemsetAsync(d_src_ + d.cell_off, 0, 16ull * d.cells, stream_));
+  RF_CK(cudaMemsetAsync(d_aux_ + d.cell_off, 0, 16ull * d.cells, stream_));
   launch_gather(L, sort_.vals[r], d_part_[pcur_], d_ids_[pcur_], d_part_[pcur_ ^ 1u],
                 d_ids_[pcur_ ^ 1u], d_mom_[mcur_], tiles, d.tile_off);
   RF_CK(cudaGetLastError());
@@ -585,7 +590,12 @@ int Engine::commit() {
   LaunchCtx L = ctx(mcur_, lpar_, pcur_);
   launch_keys(L, sort_.keys[0], sort_.vals[0], nullptr, 0, tiles_, 0u);
   const int r = radix_sort(stream_, sort_, slots_, key_bits_);
+  // The rebuilt tree starts from cleared moment, source and record buffers
+  // (the upward pass skips subtrees that are empty in both moment buffers).
   RF_CK(cudaMemsetAsync(d_mom_[mcur_], 0, 16ull * cells_, stream_));
+  RF_CK(cudaMemsetAsync(d_mom_[mcur_ ^ 1u], 0, 16ull * cells_, stream_));
+  RF_CK(cudaMemsetAsync(d_src_, 0, 16ull * cells_, stream_));
+  RF_CK(cudaMemsetAsync(d_aux_, 0, 16ull * cells_, stream_));
   launch_gather(L, sort_.vals[r], d_part_[pcur_], d_ids_[pcur_], d_part_[pcur_ ^ 1u],
                 d_ids_[pcur_ ^ 1u], d_mom_[mcur_], tiles_, 0u, d_pos4_);
   launches_ += radix_sort_kernels();

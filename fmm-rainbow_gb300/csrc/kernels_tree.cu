@@ -63,17 +63,41 @@ __device__ __forceinline__ void upward_task(
   const uint32_t sx = sub % rdim, sy = (sub / rdim) % rdim, sz = sub / (rdim * rdim);
   if (tid == 0) s_nitems = 0;
 
-  // Leaves of this subtree: 8x8x8 block, x fastest (rows of 128 B); two per thread.
+  // Leaves of this subtree: 8x8x8 block, x fastest (rows of 128 B); two per
+  // thread.  Also read: the leaves of the previous deposit (mom_next) and
+  // this subtree's upper cells in the current buffer.
+  const uint32_t dim = 1u << D;
+  uint32_t seen = 0u;
+  uint4 m[2];
 #pragma unroll
   for (uint32_t h = 0; h < 2u; h++) {
     const uint32_t t = tid + h * 256u;
     const uint32_t lx = t & 7u, ly = (t >> 3) & 7u, lz = t >> 6;
-    const uint32_t dim = 1u << D;
     const uint32_t leaf = level_offset_d(D) + lin3(sx * 8u + lx, sy * 8u + ly, sz * 8u + lz, dim);
-    const uint4 m = mom[S.cell_off + leaf];
-    s0[t] = m;
-    src[S.cell_off + leaf] = make_source(m, S.scale, S.gravity, S.n_f);
-    aux[S.cell_off + leaf] = make_aux(m.x, S.gravity, S.n_f);
+    m[h] = mom[S.cell_off + leaf];
+    seen |= m[h].x | mom_next[S.cell_off + leaf].x;
+  }
+  if (tid < 73u) {  // 64 cells of level D-1, 8 of D-2, the subtree root at level r
+    const uint32_t l = tid < 64u ? D - 1u : (tid < 72u ? D - 2u : r);
+    const uint32_t w = tid < 64u ? 4u : (tid < 72u ? 2u : 1u);
+    const uint32_t i = tid < 64u ? tid : (tid < 72u ? tid - 64u : 0u);
+    const uint32_t ix = i % w, iy = (i / w) % w, iz = i / (w * w);
+    seen |= mom[S.cell_off + level_offset_d(l) + lin3(sx * w + ix, sy * w + iy, sz * w + iz, 1u << l)].x;
+  }
+  // Empty now, empty in the previous deposit and cleared upper cells: the
+  // subtree's moments, sources and next-deposit leaves are all zero already
+  // (induction over steps; every rebuild of the moments clears the buffers),
+  // so it only takes part in the ticket count.  Bodies never sit in its
+  // leaves, so their sample cells are never read.
+  if (__syncthreads_or(seen != 0u)) {
+#pragma unroll
+  for (uint32_t h = 0; h < 2u; h++) {
+    const uint32_t t = tid + h * 256u;
+    const uint32_t lx = t & 7u, ly = (t >> 3) & 7u, lz = t >> 6;
+    const uint32_t leaf = level_offset_d(D) + lin3(sx * 8u + lx, sy * 8u + ly, sz * 8u + lz, dim);
+    s0[t] = m[h];
+    src[S.cell_off + leaf] = make_source(m[h], S.scale, S.gravity, S.n_f);
+    aux[S.cell_off + leaf] = make_aux(m[h].x, S.gravity, S.n_f);
     mom_next[S.cell_off + leaf] = make_uint4(0u, 0u, 0u, 0u);
   }
   __syncthreads();
@@ -145,8 +169,10 @@ __device__ __forceinline__ void upward_task(
     }
     choice[S.cell_off + level_offset_d(D) + lin3_lv(sx * 8u + lx, sy * 8u + ly, sz * 8u + lz, D)] = v;
   }
+  }  // not empty
+  __syncthreads();
   // Publish this subtree's parents.
-  if (tid == 0) {
+  if (tid == 0 && s_nitems != 0u) {
     uint32_t base = atomicAdd(&ctr->parents[list_par], s_nitems);
     if (base + s_nitems > plist_cap) {
       atomicCAS(&ctr->error, 0u, (uint32_t)kDevErrListOverflow);

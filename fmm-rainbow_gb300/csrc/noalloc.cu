@@ -197,6 +197,11 @@ extern "C" int rfmm_solve_fields_noalloc(const void *device_particles, uint32_t 
   if (e == cudaSuccess) e = cudaMemsetAsync(S->task_scene, 0, sizeof(S->task_scene), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(device_moments, 0, 16ull * d.cells, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(device_fields, 0, 48ull * d.cells, s);
+  // The upward pass trusts that subtrees empty in both moment buffers have
+  // cleared sources: start every call from cleared scratch.
+  if (e == cudaSuccess) e = cudaMemsetAsync(S->mom_next, 0, sizeof(S->mom_next), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(S->src, 0, sizeof(S->src), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(S->aux, 0, sizeof(S->aux), s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(S->part, device_particles, 32ull * n, cudaMemcpyDeviceToDevice, s);
   if (e != cudaSuccess) return cuda_rc(e);
 
