@@ -182,7 +182,7 @@ int Engine::create(const std::vector<SceneSpec> &specs, Engine **out) {
   A((void **)&E->d_lfield_, 48 * C);
   A((void **)&E->d_fields_, 48 * C);
   A((void **)&E->d_ctr_, sizeof(Counters));
-  A((void **)&E->d_tickets_, 4 * specs.size());
+  A((void **)&E->d_tickets_, 4 * kTicketStride * specs.size());
   A((void **)&E->d_tmaps_, sizeof(CUtensorMap) * 8 * specs.size());
   A((void **)&E->sort_.hist, 4 * 256 * (size_t)sort_tiles(E->slots_));
   A((void **)&E->sort_.totals, 4 * 256);
@@ -237,7 +237,8 @@ int Engine::create(const std::vector<SceneSpec> &specs, Engine **out) {
   if (e == cudaSuccess) e = cudaMemsetAsync(E->d_lfield_, 0, 48 * C, E->stream_);
   if (e == cudaSuccess) e = cudaMemsetAsync(E->d_fields_, 0, 48 * C, E->stream_);
   if (e == cudaSuccess) e = cudaMemsetAsync(E->d_ctr_, 0, sizeof(Counters), E->stream_);
-  if (e == cudaSuccess) e = cudaMemsetAsync(E->d_tickets_, 0, 4 * specs.size(), E->stream_);
+  if (e == cudaSuccess)
+    e = cudaMemsetAsync(E->d_tickets_, 0, 4 * kTicketStride * specs.size(), E->stream_);
   if (e != cudaSuccess) {
     delete E;
     return cuda_status(e);

@@ -189,9 +189,20 @@ __device__ __forceinline__ void upward_task(
   if (tid == 0) {
     __threadfence();
     const uint32_t ntasks = 1u << (3u * r);
-    const uint32_t done = atomicAdd(&tickets[scene], 1u);
-    s_last = (done == ntasks - 1u) ? 1u : 0u;
-    if (s_last) tickets[scene] = 0u;
+    const uint32_t ngroups = (ntasks + kTicketGroup - 1u) / kTicketGroup;
+    const uint32_t group = sub / kTicketGroup;
+    const uint32_t gsize = min(kTicketGroup, ntasks - group * kTicketGroup);
+    uint32_t *t = tickets + scene * kTicketStride;
+    uint32_t last = 0u;
+    if (atomicAdd(&t[1u + group], 1u) == gsize - 1u) {  // last subtree of its group
+      t[1u + group] = 0u;
+      __threadfence();
+      if (atomicAdd(&t[0], 1u) == ngroups - 1u) {  // last group of the scene
+        t[0] = 0u;
+        last = 1u;
+      }
+    }
+    s_last = last;
   }
   __syncthreads();
   if (s_last) {

@@ -49,7 +49,7 @@ struct Scratch {
   CUtensorMap tmaps[8];                      // 64-byte aligned TMA descriptors
   alignas(16) SceneDesc scene;
   alignas(16) Counters ctr;
-  alignas(16) uint32_t tickets[4];
+  alignas(16) uint32_t tickets[kTicketStride];
   alignas(16) uint32_t tile_scene[kMaxTiles];  // one scene: all zero
   alignas(16) uint32_t task_scene[kMaxTasks];  // one scene: all zero
   alignas(16) float4 part[2 * kMaxBodies];     // padded copy of the caller's bodies

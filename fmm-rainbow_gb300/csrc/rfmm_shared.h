@@ -14,6 +14,12 @@ constexpr uint32_t kTile = 256u;
 // neither; instead every body sums the exact softened pair forces of the
 // bodies in the 3x3x3 block of cells around its sample cell (an accuracy
 // mode without a reference counterpart).
+// Completion tickets of the upward pass, per scene: word 0 counts finished
+// groups of kTicketGroup subtrees, words 1.. count each group's finished
+// subtrees (two levels, so no single word takes an atomic from every CTA).
+constexpr uint32_t kTicketGroup = 64u;
+constexpr uint32_t kTicketStride = 16u;  // 1 + up to 8 groups (512 subtrees at depth 6)
+
 constexpr uint32_t kNearReference = 0u;
 constexpr uint32_t kNearP2P = 1u;
 
