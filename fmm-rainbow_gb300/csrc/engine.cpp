@@ -92,6 +92,15 @@ int Engine::create(const std::vector<SceneSpec> &specs, Engine **out) {
     if (s.params.depth != 0u && (s.params.depth < 4u || s.params.depth > 6u)) return RFMM_ERR_INVALID;
     if (!(s.params.fixed_point_scale >= 0.0f)) return RFMM_ERR_INVALID;
   }
+  {
+    // Kernels index bodies (2 float4 each) and cells with 32-bit arithmetic.
+    uint64_t slots = 0, cells = 0;
+    for (const SceneSpec &s : specs) {
+      slots += (uint64_t)pad_tiles(s.n) * kTile;
+      cells += total_cells(s.params.depth ? s.params.depth : depth_for_particles(s.n));
+    }
+    if (slots > (1ull << 30) || cells > (1ull << 28)) return RFMM_ERR_BUDGET;
+  }
   int dev = 0;
   RF_CK(cudaGetDevice(&dev));
   cudaDeviceProp prop;

@@ -174,7 +174,7 @@ class Engine {
   int tree_buf_ = -1;    // moment buffer holding the last complete tree
   bool committed_ = false;
   bool solved_ = false;  // fields hold a solution
-  uint32_t resort_interval_ = 64, since_sort_ = 0;
+  uint32_t resort_interval_ = 16, since_sort_ = 0;
   bool pdl_ = true;  // programmatic dependent launch between step kernels
   std::vector<bool> uploaded_;
 

@@ -162,10 +162,10 @@ __device__ __forceinline__ float4 make_source(uint4 m, float scale, float gravit
 }
 
 // Per-CTA deposit accumulator: an open-addressing hash table in shared
-// memory keyed by global leaf cell.  A CTA reduces a contiguous slice of the
-// leaf-sorted bodies into it and flushes each touched leaf with one set of
-// 32-bit reductions, so a leaf holding tens of thousands of bodies receives a
-// few global reductions instead of one per warp.  All sums are integers
+// memory keyed by global leaf cell.  A CTA reduces the leaf-sorted tiles it
+// walks into it and flushes each touched leaf with one set of 32-bit
+// reductions, so a leaf holding tens of thousands of bodies receives a few
+// global reductions instead of one per warp.  All sums are integers
 // modulo 2^32, so the result is independent of order and equals the
 // reference's per-body atomics (wgsl:418-421) bit for bit.
 struct DepositTable {

@@ -43,7 +43,7 @@ struct alignas(16) SceneDesc {
   uint32_t key_base;   // scene rank shifted above the 3*key_level Morton bits (sort key)
   float control_point[4];      // wgsl:45
   float control_axis_mode[4];  // wgsl:47
-  uint32_t key_level;  // level of the fine Morton cells the resident order sorts by (>= depth)
+  uint32_t key_level;  // level of the fine Morton cells uploads sort by (>= depth)
   uint32_t max_depth;  // deepest tree this scene's buffers hold (serving slots)
   uint32_t tile_cap;   // body tiles reserved for this scene
   uint32_t near_mode;  // kNearReference or kNearP2P

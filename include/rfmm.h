@@ -248,7 +248,7 @@ typedef struct rfmm_tuning {
   uint32_t m2l_ctas_per_sm;       /* persistent M2L grid, 1..6 */
   uint32_t l2l_ctas_per_sm;       /* persistent L2L + near grid, 1..8 */
   uint32_t integrate_ctas_per_sm; /* persistent integrate grid, 1..resident limit */
-  uint32_t integrate_dynamic;     /* 0: contiguous tile slices, 1: tiles from a counter */
+  uint32_t integrate_dynamic;     /* 0: interleaved tiles per CTA, 1: tiles from a counter */
   uint32_t resort_interval;       /* steps between resident-order refreshes, 0 = never */
   uint32_t graph_steps;           /* steps per captured CUDA graph, 1..64 */
   uint32_t pdl;                   /* programmatic dependent launch between step kernels */
