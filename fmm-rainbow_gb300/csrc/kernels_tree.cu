@@ -217,7 +217,8 @@ __device__ __forceinline__ void upward_task(
       const uint32_t dim = 1u << l, cdim = dim << 1, nl = 1u << (3u * l);
       uint4 acc = make_uint4(0u, 0u, 0u, 0u);
       if (tid < nl) {
-        const uint32_t x = tid % dim, y = (tid / dim) % dim, z = tid / (dim * dim);
+        uint32_t x, y, z;
+        cell_coords_lv(tid, (uint32_t)l, x, y, z);
         for (uint32_t dz = 0; dz < 2u; dz++)
           for (uint32_t dy = 0; dy < 2u; dy++)
             for (uint32_t dx = 0; dx < 2u; dx++)
@@ -279,7 +280,8 @@ __global__ void __launch_bounds__(256) k_upward(const SceneDesc *__restrict__ sc
       const uint32_t lp = w.cell == 0u ? 0u : level_of_d(w.cell);
       const uint32_t pdim = 1u << lp, dim = pdim << 1;
       const uint32_t pl = w.cell - level_offset_d(lp);
-      const uint32_t px = pl % pdim, py = (pl / pdim) % pdim, pz = pl / (pdim * pdim);
+      uint32_t px, py, pz;
+      cell_coords_lv(pl, lp, px, py, pz);
       for (uint32_t e = lane; e < 96u; e += 32u) {
         const uint32_t ch = e / 12u, comp = e % 12u;
         const uint32_t c = P.cell_off + level_offset_d(lp + 1u) +
@@ -304,15 +306,33 @@ __global__ void __launch_bounds__(256) k_upward(const SceneDesc *__restrict__ sc
 // -------------------------------------------------------------------- M2L
 
 constexpr uint32_t kTileCells = 216u;   // 6x6x6 children of a 3x3x3 parent block
-constexpr uint32_t kChunk = 54u;        // stencil slots evaluated per pass (216 = 4 x 54)
-constexpr uint32_t kSlotStride = 55u;   // padded so the 80 summing threads hit distinct banks
+constexpr uint32_t kChunk = 64u;        // stencil slots evaluated per pass (216 = 3 x 64 + 24)
+constexpr uint32_t kSlotStride = 65u;   // padded so the 80 summing threads hit distinct banks
 constexpr uint32_t kTmaBytes = kTileCells * 16u;
+
+// Stencil slot k in the reference's loop order (source parent (pz, py, px),
+// then child (cz, cy, cx)): bits 0-7 the slot's cell in the 6x6x6 tile, bit
+// 8 + c set when the cell is adjacent to (or is) child c of the target parent.
+__device__ __forceinline__ uint16_t m2l_slot_info(uint32_t k) {
+  const uint32_t pidx = k >> 3, ch = k & 7u;
+  const int ux = 2 * (int)(pidx % 3u) + (int)(ch & 1u);
+  const int uy = 2 * (int)((pidx / 3u) % 3u) + (int)((ch >> 1) & 1u);
+  const int uz = 2 * (int)(pidx / 9u) + (int)(ch >> 2);
+  uint32_t near = 0u;
+  for (uint32_t c = 0; c < 8u; c++) {
+    // Source child coordinate minus target coordinate = u - 2 - child.
+    const int sx = ux - 2 - (int)(c & 1u), sy = uy - 2 - (int)((c >> 1) & 1u), sz = uz - 2 - (int)(c >> 2);
+    if (sx >= -1 && sx <= 1 && sy >= -1 && sy <= 1 && sz >= -1 && sz <= 1) near |= 1u << c;
+  }
+  return (uint16_t)((uint32_t)(ux + 6 * (uy + 6 * uz)) | (near << 8));
+}
 
 struct M2LShared {
   float4 tile[kTileCells];  // first member: 128-byte aligned by the launch
   unsigned long long mbar;
   uint32_t stop;
   uint32_t live[8];         // target cell of each child, or ~0 if the child is empty
+  uint16_t slot_info[kTileCells];
   float vals[8][10][kSlotStride];
 };
 
@@ -327,6 +347,7 @@ struct M2LCompactShared {
   uint32_t stop;
   uint32_t live[8];
   uint32_t nvalid[8];            // contributing stencil slots of each child
+  uint16_t slot_info[kTileCells];
   uint8_t slots[8][kTileCells];  // those slots, in the reference's loop order
   float vals[8][10][kRoundStride];
 };
@@ -391,6 +412,7 @@ __global__ void __launch_bounds__(256) k_m2l(const SceneDesc *__restrict__ scene
     sh.stop = 0u;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
+  for (uint32_t k = tid; k < kTileCells; k += blockDim.x) sh.slot_info[k] = m2l_slot_info(k);
   grid_dependency_wait();  // the upward pass built the tree and the parent list
   const uint32_t count = min(ctr->parents[list_par], plist_cap);
   if (blockIdx.x == 0 && tid == 0) ctr->parents[list_par ^ 1u] = 0u;  // reset for the next step
@@ -403,7 +425,9 @@ __global__ void __launch_bounds__(256) k_m2l(const SceneDesc *__restrict__ scene
     const uint32_t lp = w.cell == 0u ? 0u : level_of_d(w.cell);
     const uint32_t l = lp + 1u, pdim = 1u << lp, dim = pdim << 1;
     const uint32_t pl = w.cell - level_offset_d(lp);
-    const int pcx = (int)(pl % pdim), pcy = (int)((pl / pdim) % pdim), pcz = (int)(pl / (pdim * pdim));
+    uint32_t upx, upy, upz;
+    cell_coords_lv(pl, lp, upx, upy, upz);
+    const int pcx = (int)upx, pcy = (int)upy, pcz = (int)upz;
     const int bx = 2 * pcx - 2, by = 2 * pcy - 2, bz = 2 * pcz - 2;
     const uint32_t lvl_base = S.cell_off + level_offset_d(l);
 
@@ -452,16 +476,9 @@ __global__ void __launch_bounds__(256) k_m2l(const SceneDesc *__restrict__ scene
         bool use = false;
         uint32_t cell = 0u;
         if (k < kTileCells) {
-          // Reference loop order: source parent (pz, py, px) then child (cz, cy, cx).
-          const uint32_t pidx = k >> 3, ch = k & 7u;
-          const int ux = 2 * (int)(pidx % 3u) + (int)(ch & 1u);
-          const int uy = 2 * (int)((pidx / 3u) % 3u) + (int)((ch >> 1) & 1u);
-          const int uz = 2 * (int)(pidx / 9u) + (int)(ch >> 2);
-          // Source child coordinate minus target coordinate = u - 2 - child.
-          const int sx = ux - 2 - cx, sy = uy - 2 - cy, sz = uz - 2 - cz;
-          const bool near = sx >= -1 && sx <= 1 && sy >= -1 && sy <= 1 && sz >= -1 && sz <= 1;
-          cell = (uint32_t)(ux + 6 * (uy + 6 * uz));
-          use = !near && sh.tile[cell].w != 0.0f;
+          const uint32_t info = sh.slot_info[k];
+          cell = info & 0xFFu;
+          use = !((info >> (8u + warp)) & 1u) && sh.tile[cell].w != 0.0f;
         }
         const uint32_t mask = __ballot_sync(0xFFFFFFFFu, use);
         if (use) sh.slots[warp][nv + __popc(mask & ((1u << lane) - 1u))] = (uint8_t)cell;
@@ -506,18 +523,12 @@ __global__ void __launch_bounds__(256) k_m2l(const SceneDesc *__restrict__ scene
     const float ctx = cell_center_lv(tx, l), cty = cell_center_lv(ty, l), ctz = cell_center_lv(tz, l);
     const float eps = (0.06f * kHalf) * pow2_neg(l);  // wgsl:507, / 2^l as an exact scaling
     for (uint32_t c0 = 0; c0 < kTileCells; c0 += kChunk) {
+      const uint32_t m = min(kChunk, kTileCells - c0);
       if (live) {
-        for (uint32_t kk = lane; kk < kChunk; kk += 32u) {
-          const uint32_t k = c0 + kk;
-          // Reference loop order: source parent (pz, py, px) then child (cz, cy, cx).
-          const uint32_t pidx = k >> 3, ch = k & 7u;
-          const int ux = 2 * (int)(pidx % 3u) + (int)(ch & 1u);
-          const int uy = 2 * (int)((pidx / 3u) % 3u) + (int)((ch >> 1) & 1u);
-          const int uz = 2 * (int)(pidx / 9u) + (int)(ch >> 2);
-          // Source child coordinate minus target coordinate = u - 2 - child.
-          const int sx = ux - 2 - cx, sy = uy - 2 - cy, sz = uz - 2 - cz;
-          const bool near = sx >= -1 && sx <= 1 && sy >= -1 && sy <= 1 && sz >= -1 && sz <= 1;
-          const float4 src4 = sh.tile[ux + 6 * (uy + 6 * uz)];
+        for (uint32_t kk = lane; kk < m; kk += 32u) {
+          const uint32_t info = sh.slot_info[c0 + kk];
+          const bool near = (info >> (8u + warp)) & 1u;
+          const float4 src4 = sh.tile[info & 0xFFu];
           float out[10];
           if (!near && src4.w != 0.0f) {
             pair_field_d(src4, ctx, cty, ctz, eps, out);
@@ -532,8 +543,8 @@ __global__ void __launch_bounds__(256) k_m2l(const SceneDesc *__restrict__ scene
       __syncthreads();
       if (tid < 80u && sh.live[tid / 10u] != 0xFFFFFFFFu) {
         const float *row = sh.vals[tid / 10u][tid % 10u];
-#pragma unroll 6
-        for (uint32_t kk = 0; kk < kChunk; kk++) acc = acc + row[kk];
+#pragma unroll 8
+        for (uint32_t kk = 0; kk < m; kk++) acc = acc + row[kk];
       }
       __syncthreads();
     }
@@ -580,9 +591,11 @@ __global__ void __launch_bounds__(256) k_l2l_near(const SceneDesc *__restrict__ 
     const uint32_t lp = w.cell == 0u ? 0u : level_of_d(w.cell);
     const uint32_t l = lp + 1u, pdim = 1u << lp, dim = pdim << 1;
     const uint32_t pl = w.cell - level_offset_d(lp);
-    const uint32_t tx = 2u * (pl % pdim) + (warp & 1u);
-    const uint32_t ty = 2u * ((pl / pdim) % pdim) + ((warp >> 1) & 1u);
-    const uint32_t tz = 2u * (pl / (pdim * pdim)) + (warp >> 2);
+    uint32_t upx, upy, upz;
+    cell_coords_lv(pl, lp, upx, upy, upz);
+    const uint32_t tx = 2u * upx + (warp & 1u);
+    const uint32_t ty = 2u * upy + ((warp >> 1) & 1u);
+    const uint32_t tz = 2u * upz + (warp >> 2);
     const uint32_t lvl_base = S.cell_off + level_offset_d(l);
     const uint32_t target = lvl_base + lin3(tx, ty, tz, dim);
     const uint32_t tcount = mom[target].x;

@@ -86,13 +86,19 @@ __device__ __forceinline__ uint32_t lin3(uint32_t x, uint32_t y, uint32_t z, uin
 }
 
 // Level containing local tree cell g (g >= 1), as level_of (wgsl:380-392).
+// Level l holds the cells g with (8^l - 1) / 7 <= g < (8^(l+1) - 1) / 7, i.e.
+// 8^l <= 7g + 1 < 8^(l+1): l = floor(log2(7g + 1) / 3) (g < 2^28).
 __device__ __forceinline__ uint32_t level_of_d(uint32_t g) {
-  uint32_t level = 1u, start = 1u;
-  while (g >= start + (1u << (3u * level))) {
-    start += 1u << (3u * level);
-    ++level;
-  }
-  return level;
+  return (31u - (uint32_t)__clz((int)(7u * g + 1u))) / 3u;
+}
+
+// Coordinates of local cell index `i` at level l (x | y << l | z << 2l).
+__device__ __forceinline__ void cell_coords_lv(uint32_t i, uint32_t l, uint32_t &x, uint32_t &y,
+                                               uint32_t &z) {
+  const uint32_t mask = (1u << l) - 1u;
+  x = i & mask;
+  y = (i >> l) & mask;
+  z = i >> (2u * l);
 }
 
 // Programmatic dependent launch: a kernel launched with the programmatic
