@@ -246,7 +246,9 @@ __device__ __forceinline__ void upward_task(
 }
 
 // Persistent upward pass over the active subtree tasks (task_list, or every
-// task when null).
+// task when null).  The first `clear_ctas` CTAs only clear the fields of the
+// previous step's targets (children of its listed parents; fields are zero
+// off the M2L path), so the subtree CTAs start their reductions at once.
 __global__ void __launch_bounds__(256) k_upward(const SceneDesc *__restrict__ scenes,
                                                 const uint32_t *__restrict__ task_scene,
                                                 const uint32_t *__restrict__ task_list,
@@ -258,7 +260,7 @@ __global__ void __launch_bounds__(256) k_upward(const SceneDesc *__restrict__ sc
                                                 WorkItem *__restrict__ plist, uint32_t plist_cap,
                                                 const WorkItem *__restrict__ plist_prev,
                                                 Counters *__restrict__ ctr, uint32_t list_par,
-                                                uint32_t *__restrict__ tickets) {
+                                                uint32_t *__restrict__ tickets, uint32_t clear_ctas) {
   __shared__ uint4 s0[512];
   __shared__ uint4 s1[64];
   __shared__ uint4 s2[8];
@@ -266,37 +268,56 @@ __global__ void __launch_bounds__(256) k_upward(const SceneDesc *__restrict__ sc
   __shared__ uint32_t s_nitems, s_base, s_last, s_root;
   __shared__ SceneDesc sS;
   const uint32_t tid = threadIdx.x;
-  grid_dependency_wait();  // the previous integrate deposited and read the fields
-  if (blockIdx.x == 0 && tid == 0) ctr->tile_cursor = 0u;  // for this step's integrate
-
-  // Clear the fields of the previous step's targets (children of listed parents).
-  {
+  if (blockIdx.x < clear_ctas) {
+    grid_dependency_wait();  // the previous integrate read the fields
+    if (blockIdx.x == 0 && tid == 0) ctr->tile_cursor = 0u;  // for this step's integrate
+    // Each warp takes 32 listed parents at a time (one per lane), then clears
+    // their 8 children's 48-byte fields with one 16-byte store per lane.
     const uint32_t prev_n = min(ctr->parents[list_par ^ 1u], plist_cap);
-    const uint32_t wpb = blockDim.x >> 5;
-    const uint32_t warp = blockIdx.x * wpb + (tid >> 5), lane = tid & 31u;
-    for (uint32_t i = warp; i < prev_n; i += gridDim.x * wpb) {
-      const WorkItem w = plist_prev[i];
-      const SceneDesc &P = scenes[w.scene];
-      const uint32_t lp = w.cell == 0u ? 0u : level_of_d(w.cell);
-      const uint32_t pdim = 1u << lp, dim = pdim << 1;
-      const uint32_t pl = w.cell - level_offset_d(lp);
-      uint32_t px, py, pz;
-      cell_coords_lv(pl, lp, px, py, pz);
-      for (uint32_t e = lane; e < 96u; e += 32u) {
-        const uint32_t ch = e / 12u, comp = e % 12u;
-        const uint32_t c = P.cell_off + level_offset_d(lp + 1u) +
-                           lin3(2u * px + (ch & 1u), 2u * py + ((ch >> 1) & 1u),
-                                2u * pz + (ch >> 2), dim);
-        fields[(size_t)c * 12u + comp] = 0.0f;
+    const uint32_t wpb = blockDim.x >> 5, lane = tid & 31u;
+    const uint32_t ch = lane / 3u, part = lane % 3u;  // lanes 0..23: child, float4 of its field
+    const uint32_t choff_x = ch & 1u, choff_y = (ch >> 1) & 1u, choff_z = ch >> 2;
+    for (uint32_t i0 = (blockIdx.x * wpb + (tid >> 5)) * 32u; i0 < prev_n; i0 += clear_ctas * wpb * 32u) {
+      uint32_t base = 0u, dim = 0u;
+      if (i0 + lane < prev_n) {
+        const WorkItem w = plist_prev[i0 + lane];
+        const uint32_t lp = w.cell == 0u ? 0u : level_of_d(w.cell);
+        uint32_t px, py, pz;
+        cell_coords_lv(w.cell - level_offset_d(lp), lp, px, py, pz);
+        dim = 2u << lp;
+        base = scenes[w.scene].cell_off + level_offset_d(lp + 1u) + lin3(2u * px, 2u * py, 2u * pz, dim);
+      }
+      const uint32_t nb = min(32u, prev_n - i0);
+      for (uint32_t j = 0; j < nb; j++) {
+        const uint32_t b = __shfl_sync(0xFFFFFFFFu, base, j), d = __shfl_sync(0xFFFFFFFFu, dim, j);
+        if (lane < 24u) {
+          const uint32_t c = b + choff_x + d * (choff_y + d * choff_z);
+          reinterpret_cast<float4 *>(fields)[(size_t)c * 3u + part] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
       }
     }
+    grid_dependents_may_launch();
+    return;
   }
 
+  // Scene descriptors and task lists change only by host copies, never by
+  // the kernel this launch may overlap, so the first task's scene is staged
+  // before waiting for that kernel.
+  const uint32_t cta = blockIdx.x - clear_ctas, ncta = gridDim.x - clear_ctas;
   const uint32_t ntasks = task_list != nullptr ? min(ctr->tasks_active, ntasks_all) : ntasks_all;
-  for (uint32_t it = blockIdx.x; it < ntasks; it += gridDim.x) {
-    const uint32_t task = task_list != nullptr ? task_list[it] : it;
-    const uint32_t scene = task_scene[task];
+  uint32_t task = 0u, scene = 0u;
+  if (cta < ntasks) {
+    task = task_list != nullptr ? task_list[cta] : cta;
+    scene = task_scene[task];
     load_scene(sS, scenes, scene);
+  }
+  grid_dependency_wait();  // the previous integrate deposited into mom_next
+  for (uint32_t it = cta; it < ntasks; it += ncta) {
+    if (it != cta) {
+      task = task_list != nullptr ? task_list[it] : it;
+      scene = task_scene[task];
+      load_scene(sS, scenes, scene);
+    }
     upward_task(sS, scene, task - sS.task_off, mom, mom_next, src, aux, choice, plist, plist_cap,
                 ctr, list_par, tickets, s0, s1, s2, s_items, s_nitems, s_base, s_last, s_root);
   }
@@ -569,6 +590,7 @@ __global__ void __launch_bounds__(256) k_m2l(const SceneDesc *__restrict__ scene
 
 struct L2LShared {
   float vals[8][10][27];
+  float centre[127];  // cell_center_lv(c, l) at [2^l - 1 + c], levels 0..6
 };
 
 __global__ void __launch_bounds__(256) k_l2l_near(const SceneDesc *__restrict__ scenes,
@@ -581,10 +603,21 @@ __global__ void __launch_bounds__(256) k_l2l_near(const SceneDesc *__restrict__ 
                                                   float *__restrict__ fields) {
   __shared__ L2LShared sh;
   const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
+  if (tid < 127u) {
+    const uint32_t l = 31u - (uint32_t)__clz((int)(tid + 1u));
+    sh.centre[tid] = cell_center_lv(tid + 1u - (1u << l), l);
+  }
   grid_dependency_wait();  // M2L results of every target are complete
   const uint32_t count = min(ctr->parents[list_par], plist_cap);
   // Lane c < 12 owns field component c (ax ay az phi Jxx Jxy Jxz Jyy Jyz Jzz 0 0).
   const uint32_t c = lane < 12u ? lane : 11u;
+  // The translation of component c < 4 is f_c +/- ((f_b dx + f_c' dy) + f_d dz):
+  // the source lanes of its three terms and its sign.
+  constexpr uint32_t kSrcB = 0x0654u, kSrcC = 0x1875u, kSrcD = 0x2986u;  // 4 bits per lane 0..3
+  const uint32_t sb = lane < 4u ? (kSrcB >> (4u * lane)) & 15u : lane;
+  const uint32_t sc = lane < 4u ? (kSrcC >> (4u * lane)) & 15u : lane;
+  const uint32_t sd = lane < 4u ? (kSrcD >> (4u * lane)) & 15u : lane;
+  __syncthreads();
   for (uint32_t item = blockIdx.x; item < count; item += gridDim.x) {
     const WorkItem w = plist[item];
     const SceneDesc &S = scenes[w.scene];
@@ -620,18 +653,19 @@ __global__ void __launch_bounds__(256) k_l2l_near(const SceneDesc *__restrict__ 
       if (a <= l) {
         const uint32_t sh_ = l - a;
         const uint32_t ax = tx >> sh_, ay = ty >> sh_, az = tz >> sh_;
-        const float dx = cell_center_lv(ax, a) - cell_center_lv(ax >> 1, a - 1u);
-        const float dy = cell_center_lv(ay, a) - cell_center_lv(ay >> 1, a - 1u);
-        const float dz = cell_center_lv(az, a) - cell_center_lv(az >> 1, a - 1u);
-        float v[10];
-#pragma unroll
-        for (int k = 0; k < 10; k++) v[k] = __shfl_sync(0xFFFFFFFFu, f, k);
-        // inherited (wgsl:603-609): a += J . delta, phi -= a . delta, J unchanged.
-        float inh = f;
-        if (c == 0u) inh = v[0] + (v[4] * dx + v[5] * dy + v[6] * dz);
-        if (c == 1u) inh = v[1] + (v[5] * dx + v[7] * dy + v[8] * dz);
-        if (c == 2u) inh = v[2] + (v[6] * dx + v[8] * dy + v[9] * dz);
-        if (c == 3u) inh = v[3] - ((v[0] * dx + v[1] * dy) + v[2] * dz);
+        const float *cen = sh.centre + (1u << a) - 1u, *pcen = sh.centre + (1u << (a - 1u)) - 1u;
+        const float dx = cen[ax] - pcen[ax >> 1];
+        const float dy = cen[ay] - pcen[ay >> 1];
+        const float dz = cen[az] - pcen[az >> 1];
+        // inherited (wgsl:603-609): a += J . delta, phi -= a . delta, J unchanged:
+        //   ax + ((Jxx dx + Jxy dy) + Jxz dz), ay + ((Jxy dx + Jyy dy) + Jyz dz),
+        //   az + ((Jxz dx + Jyz dy) + Jzz dz), phi - ((ax dx + ay dy) + az dz)
+        // (x - t == x + (-t) exactly).
+        const float vb = __shfl_sync(0xFFFFFFFFu, f, sb);
+        const float vc = __shfl_sync(0xFFFFFFFFu, f, sc);
+        const float vd = __shfl_sync(0xFFFFFFFFu, f, sd);
+        const float t = (vb * dx + vc * dy) + vd * dz;
+        const float inh = lane < 4u ? f + (lane == 3u ? -t : t) : f;
         f = g[a - 1] + inh;
       }
     }
@@ -671,9 +705,13 @@ __global__ void __launch_bounds__(256) k_l2l_near(const SceneDesc *__restrict__ 
 
 void launch_upward(const LaunchCtx &L, uint32_t list_par, uint32_t tasks) {
   const uint32_t grid = tasks < L.tree_ctas ? tasks : L.tree_ctas;
-  launch_step_kernel(L, k_upward, dim3(grid), dim3(256), 0, L.scenes, L.task_scene, L.task_list,
-                     tasks, L.mom, L.mom_next, L.src, L.aux, L.choice, L.fields, L.plist,
-                     L.plist_cap, L.plist_prev, L.ctr, list_par, L.tickets);
+  // Clearing CTAs: one pass of 32 parents per warp covers 8 * 32 * clear_ctas
+  // listed parents.
+  uint32_t clear = (L.plist_cap + 2047u) / 2048u;
+  clear = clear < 8u ? 8u : (clear > 64u ? 64u : clear);
+  launch_step_kernel(L, k_upward, dim3(grid + clear), dim3(256), 0, L.scenes, L.task_scene,
+                     L.task_list, tasks, L.mom, L.mom_next, L.src, L.aux, L.choice, L.fields,
+                     L.plist, L.plist_cap, L.plist_prev, L.ctr, list_par, L.tickets, clear);
 }
 
 size_t m2l_smem_bytes(bool compact) {
