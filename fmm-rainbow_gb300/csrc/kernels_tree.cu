@@ -49,6 +49,15 @@ __device__ __forceinline__ void store_cell(const SceneDesc &S, uint32_t local_ce
   aux[g] = make_aux(m.x, S.gravity, S.n_f);
 }
 
+// atomicAdd with acquire-release semantics at GPU scope: this thread's earlier
+// writes are visible to whoever observes the new value, and writes released
+// by earlier adders are visible to this thread afterwards.
+__device__ __forceinline__ uint32_t atomic_add_acq_rel(uint32_t *p, uint32_t v) {
+  uint32_t old;
+  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+
 // Body of one upward task: the 8x8x8-leaf subtree `sub` of scene `scene`.
 __device__ __forceinline__ void upward_task(
     const SceneDesc &S, uint32_t scene, uint32_t sub, uint4 *__restrict__ mom,
@@ -170,34 +179,20 @@ __device__ __forceinline__ void upward_task(
     choice[S.cell_off + level_offset_d(D) + lin3_lv(sx * 8u + lx, sy * 8u + ly, sz * 8u + lz, D)] = v;
   }
   }  // not empty
-  __syncthreads();
-  // Publish this subtree's parents.
-  if (tid == 0 && s_nitems != 0u) {
-    uint32_t base = atomicAdd(&ctr->parents[list_par], s_nitems);
-    if (base + s_nitems > plist_cap) {
-      atomicCAS(&ctr->error, 0u, (uint32_t)kDevErrListOverflow);
-      s_nitems = base < plist_cap ? plist_cap - base : 0u;
-    }
-    s_base = base;
-  }
-  __syncthreads();
-  for (uint32_t i = tid; i < s_nitems; i += blockDim.x) plist[s_base + i] = s_items[i];
 
   // The scene's last finished subtree reduces levels r-1 .. 0.  Only thread 0
-  // wrote the level-r cell that reduction reads, so only it fences.
-  __syncthreads();
+  // wrote the level-r cell that reduction reads; its tickets release that
+  // write (and acquire the earlier subtrees' ones) on the way to the last CTA.
   if (tid == 0) {
-    __threadfence();
     const uint32_t ntasks = 1u << (3u * r);
     const uint32_t ngroups = (ntasks + kTicketGroup - 1u) / kTicketGroup;
     const uint32_t group = sub / kTicketGroup;
     const uint32_t gsize = min(kTicketGroup, ntasks - group * kTicketGroup);
     uint32_t *t = tickets + scene * kTicketStride;
     uint32_t last = 0u;
-    if (atomicAdd(&t[1u + group], 1u) == gsize - 1u) {  // last subtree of its group
+    if (atomic_add_acq_rel(&t[1u + group], 1u) == gsize - 1u) {  // last subtree of its group
       t[1u + group] = 0u;
-      __threadfence();
-      if (atomicAdd(&t[0], 1u) == ngroups - 1u) {  // last group of the scene
+      if (atomic_add_acq_rel(&t[0], 1u) == ngroups - 1u) {  // last group of the scene
         t[0] = 0u;
         last = 1u;
       }
@@ -207,7 +202,6 @@ __device__ __forceinline__ void upward_task(
   __syncthreads();
   if (s_last) {
     __threadfence();
-    if (tid == 0) s_nitems = 0;
     // Level r has at most 512 cells: stage it (written by other CTAs) via L2.
     const uint32_t nr = 1u << (3u * r);
     for (uint32_t i = tid; i < nr; i += blockDim.x)
@@ -231,17 +225,19 @@ __device__ __forceinline__ void upward_task(
       if (tid < nl) s0[tid] = acc;
       __syncthreads();
     }
-    if (tid == 0) {
-      uint32_t base = atomicAdd(&ctr->parents[list_par], s_nitems);
-      if (base + s_nitems > plist_cap) {
-        atomicCAS(&ctr->error, 0u, (uint32_t)kDevErrListOverflow);
-        s_nitems = base < plist_cap ? plist_cap - base : 0u;
-      }
-      s_base = base;
-    }
-    __syncthreads();
-    for (uint32_t i = tid; i < s_nitems; i += blockDim.x) plist[s_base + i] = s_items[i];
   }
+  // Publish the parents listed by this subtree (and, in the scene's last
+  // CTA, by the top levels): after the tickets, off the path to the last CTA.
+  if (tid == 0 && s_nitems != 0u) {
+    uint32_t base = atomicAdd(&ctr->parents[list_par], s_nitems);
+    if (base + s_nitems > plist_cap) {
+      atomicCAS(&ctr->error, 0u, (uint32_t)kDevErrListOverflow);
+      s_nitems = base < plist_cap ? plist_cap - base : 0u;
+    }
+    s_base = base;
+  }
+  __syncthreads();
+  for (uint32_t i = tid; i < s_nitems; i += blockDim.x) plist[s_base + i] = s_items[i];
   __syncthreads();
 }
 
@@ -264,7 +260,7 @@ __global__ void __launch_bounds__(256) k_upward(const SceneDesc *__restrict__ sc
   __shared__ uint4 s0[512];
   __shared__ uint4 s1[64];
   __shared__ uint4 s2[8];
-  __shared__ WorkItem s_items[80];
+  __shared__ WorkItem s_items[160];  // a subtree's 73 cells + the top levels' 73
   __shared__ uint32_t s_nitems, s_base, s_last, s_root;
   __shared__ SceneDesc sS;
   const uint32_t tid = threadIdx.x;
@@ -631,12 +627,10 @@ __global__ void __launch_bounds__(256) k_l2l_near(const SceneDesc *__restrict__ 
     const uint32_t tz = 2u * upz + (warp >> 2);
     const uint32_t lvl_base = S.cell_off + level_offset_d(l);
     const uint32_t target = lvl_base + lin3(tx, ty, tz, dim);
+    // The target's count, its ancestors' M2L components (lane c reads
+    // component c) and its 26 neighbours' sources (lane j < 26) do not depend
+    // on one another: all are requested before the count is tested.
     const uint32_t tcount = mom[target].x;
-    if (tcount == 0u) continue;  // warp-uniform
-
-    // Top-down chain f_a = m2l(a) + translate(f_{a-1}) from the root field 0
-    // (the reference never writes cell 0's field, wgsl:459).  The ancestors'
-    // M2L components are loaded up front (lane c reads component c).
     float g[6];
 #pragma unroll
     for (uint32_t a = 1u; a <= 6u; a++) {
@@ -647,6 +641,18 @@ __global__ void __launch_bounds__(256) k_l2l_near(const SceneDesc *__restrict__ 
         g[a - 1] = __ldg(lfield + (size_t)anc * 12u + c);
       }
     }
+    float4 nsrc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // w = 0: no term
+    if (lane < 26u && S.near_mode == kNearReference) {
+      const uint32_t j = lane < 13u ? lane : lane + 1u;  // skip the centre (13)
+      const int dx = (int)(j % 3u) - 1, dy = (int)((j / 3u) % 3u) - 1, dz = (int)(j / 9u) - 1;
+      const int sx = (int)tx + dx, sy = (int)ty + dy, sz = (int)tz + dz;
+      if (sx >= 0 && sy >= 0 && sz >= 0 && sx < (int)dim && sy < (int)dim && sz < (int)dim)
+        nsrc = __ldg(&src[lvl_base + lin3((uint32_t)sx, (uint32_t)sy, (uint32_t)sz, dim)]);
+    }
+    if (tcount == 0u) continue;  // warp-uniform
+
+    // Top-down chain f_a = m2l(a) + translate(f_{a-1}) from the root field 0
+    // (the reference never writes cell 0's field, wgsl:459).
     float f = 0.0f;
 #pragma unroll
     for (uint32_t a = 1u; a <= 6u; a++) {
@@ -676,16 +682,10 @@ __global__ void __launch_bounds__(256) k_l2l_near(const SceneDesc *__restrict__ 
                   ctz = cell_center_lv(tz, l);
       const float near_eps = fmaxf(S.softening, (0.72f * kHalf) * pow2_neg(l));
       if (lane < 26u) {
-        const uint32_t j = lane < 13u ? lane : lane + 1u;  // skip the centre (13)
-        const int dx = (int)(j % 3u) - 1, dy = (int)((j / 3u) % 3u) - 1, dz = (int)(j / 9u) - 1;
-        const int sx = (int)tx + dx, sy = (int)ty + dy, sz = (int)tz + dz;
         float out[10];
 #pragma unroll
         for (int k = 0; k < 10; k++) out[k] = 0.0f;
-        if (sx >= 0 && sy >= 0 && sz >= 0 && sx < (int)dim && sy < (int)dim && sz < (int)dim) {
-          const float4 s = __ldg(&src[lvl_base + lin3((uint32_t)sx, (uint32_t)sy, (uint32_t)sz, dim)]);
-          if (s.w != 0.0f) pair_field_d(s, ctx, cty, ctz, near_eps, out);
-        }
+        if (nsrc.w != 0.0f) pair_field_d(nsrc, ctx, cty, ctz, near_eps, out);
 #pragma unroll
         for (int k = 0; k < 10; k++) sh.vals[warp][k][lane] = out[k];
       }
