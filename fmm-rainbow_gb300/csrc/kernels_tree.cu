@@ -455,11 +455,6 @@ __global__ void __launch_bounds__(256) k_m2l(const SceneDesc *__restrict__ scene
         mbar_expect_tx(&sh.mbar, kTmaBytes);
         tma_load_3d(sh.tile, &tmaps[w.scene * 8u + l], 4 * bx, by, bz, &sh.mbar);
       }
-      if (!mbar_wait(&sh.mbar, phase)) {
-        if (atomicCAS(&ctr->error, 0u, (uint32_t)kDevErrTmaTimeout) == 0u) ctr->error_info = item;
-        sh.stop = 1u;
-      }
-      phase ^= 1u;
     } else {
       for (uint32_t t = tid; t < kTileCells; t += blockDim.x) {
         const int x = bx + (int)(t % 6u), y = by + (int)((t / 6u) % 6u), z = bz + (int)(t / 36u);
@@ -468,6 +463,22 @@ __global__ void __launch_bounds__(256) k_m2l(const SceneDesc *__restrict__ scene
           v = src[lvl_base + lin3((uint32_t)x, (uint32_t)y, (uint32_t)z, dim)];
         sh.tile[t] = v;
       }
+    }
+    // Warp w handles child w of the parent: its target cell, occupancy and
+    // centre are read while the tile is in flight; then warp 0 alone waits
+    // for the copy (the other warps wait at the barrier without issuing).
+    const int cx = (int)(warp & 1u), cy = (int)((warp >> 1) & 1u), cz = (int)(warp >> 2);
+    const uint32_t tx = (uint32_t)(2 * pcx + cx), ty = (uint32_t)(2 * pcy + cy), tz = (uint32_t)(2 * pcz + cz);
+    const uint32_t target = lvl_base + lin3(tx, ty, tz, dim);
+    const bool live = mom[target].x != 0u;  // empty children are not targets
+    const float ctx = cell_center_lv(tx, l), cty = cell_center_lv(ty, l), ctz = cell_center_lv(tz, l);
+    const float eps = (0.06f * kHalf) * pow2_neg(l);  // wgsl:507, / 2^l as an exact scaling
+    if (l >= 3u) {
+      if (warp == 0u && !mbar_wait(&sh.mbar, phase) && lane == 0u) {
+        if (atomicCAS(&ctr->error, 0u, (uint32_t)kDevErrTmaTimeout) == 0u) ctr->error_info = item;
+        sh.stop = 1u;
+      }
+      phase ^= 1u;
     }
     __syncthreads();
     if (sh.stop) return;
@@ -480,12 +491,6 @@ __global__ void __launch_bounds__(256) k_m2l(const SceneDesc *__restrict__ scene
     // evaluated, one per lane, and 80 threads (8 children x 10 components)
     // add each round to their running sums in list order.  Skipped slots
     // would add +0, which cannot change a sum that starts at +0.
-    const int cx = (int)(warp & 1u), cy = (int)((warp >> 1) & 1u), cz = (int)(warp >> 2);
-    const uint32_t tx = (uint32_t)(2 * pcx + cx), ty = (uint32_t)(2 * pcy + cy), tz = (uint32_t)(2 * pcz + cz);
-    const uint32_t target = lvl_base + lin3(tx, ty, tz, dim);
-    const bool live = mom[target].x != 0u;  // empty children are not targets
-    const float ctx = cell_center_lv(tx, l), cty = cell_center_lv(ty, l), ctz = cell_center_lv(tz, l);
-    const float eps = (0.06f * kHalf) * pow2_neg(l);  // wgsl:507, / 2^l as an exact scaling
     uint32_t nv = 0u;
     if (live) {
       for (uint32_t k0 = 0; k0 < kTileCells; k0 += 32u) {
@@ -524,7 +529,12 @@ __global__ void __launch_bounds__(256) k_m2l(const SceneDesc *__restrict__ scene
       if (tid < 80u && r * kRound < my_n) {
         const float *row = sh.vals[tid / 10u][tid % 10u];
         const uint32_t m = min(kRound, my_n - r * kRound);
-        for (uint32_t kk = 0; kk < m; kk++) acc = acc + row[kk];
+        if (m == kRound) {
+#pragma unroll
+          for (uint32_t kk = 0; kk < kRound; kk++) acc = acc + row[kk];
+        } else {
+          for (uint32_t kk = 0; kk < m; kk++) acc = acc + row[kk];
+        }
       }
       __syncthreads();
     }
@@ -532,13 +542,7 @@ __global__ void __launch_bounds__(256) k_m2l(const SceneDesc *__restrict__ scene
     // Warp w evaluates the stencil of child w of the parent, a chunk of slots
     // at a time; 80 threads (8 children x 10 components) then add the chunk to
     // their running sums, strictly in slot order.
-    const int cx = (int)(warp & 1u), cy = (int)((warp >> 1) & 1u), cz = (int)(warp >> 2);
-    const uint32_t tx = (uint32_t)(2 * pcx + cx), ty = (uint32_t)(2 * pcy + cy), tz = (uint32_t)(2 * pcz + cz);
-    const uint32_t target = lvl_base + lin3(tx, ty, tz, dim);
-    const bool live = mom[target].x != 0u;  // empty children are not targets
     if (lane == 0) sh.live[warp] = live ? target : 0xFFFFFFFFu;
-    const float ctx = cell_center_lv(tx, l), cty = cell_center_lv(ty, l), ctz = cell_center_lv(tz, l);
-    const float eps = (0.06f * kHalf) * pow2_neg(l);  // wgsl:507, / 2^l as an exact scaling
     for (uint32_t c0 = 0; c0 < kTileCells; c0 += kChunk) {
       const uint32_t m = min(kChunk, kTileCells - c0);
       if (live) {
