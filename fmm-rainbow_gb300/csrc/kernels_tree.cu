@@ -8,19 +8,22 @@
 //   near_all 521-572   26 neighbour cell monopoles per adaptive leaf
 //
 // GB300 structure:
-//   k_upward     one 512-thread CTA per 8x8x8-leaf subtree reduces four levels
-//                in shared memory; the last CTA of a scene (ticket counter)
-//                finishes the top levels.  It also writes each cell's source
-//                record (centre of mass, G*m), appends every parent with more
-//                than 16 bodies to the work list, zeroes the leaf level the
-//                next integrate deposits into, and clears the fields of the
-//                previous step's targets (fields are zero off the M2L path).
+//   k_upward     one 256-thread CTA per 8x8x8-leaf subtree reduces four levels
+//                in shared memory and takes a completion ticket as soon as
+//                its root is known; the last CTA of a scene finishes the top
+//                levels.  It also writes each cell's source record (centre
+//                of mass, G*m), appends every parent with more than 16 bodies
+//                to the work list, zeroes the leaf level the next integrate
+//                deposits into, and resolves each leaf's sample cell; a few
+//                extra CTAs clear the fields of the previous step's targets
+//                (fields are zero off the M2L path).
 //   k_m2l        one CTA per listed parent: the 6x6x6 source tile of the
 //                parent's 3x3x3 neighbourhood is staged in shared memory by a
-//                TMA tensor copy; warp w evaluates child w's 216 stencil slots
-//                in parallel and 10 lanes then sum them in the reference's
-//                loop order (excluded and empty slots contribute +0, which
-//                leaves an accumulation that starts at +0 unchanged).
+//                TMA tensor copy; warp w evaluates child w's contributing
+//                stencil slots in parallel and 80 threads (8 children x 10
+//                components) sum them in the reference's loop order (excluded
+//                and empty slots contribute +0, which leaves an accumulation
+//                that starts at +0 unchanged).
 //   k_l2l_near   one warp per target: the top-down L2L chain is recomputed
 //                from the M2L results of the target's ancestors (so levels
 //                need no ordering), then adaptive leaves add their 26 near
@@ -58,18 +61,38 @@ __device__ __forceinline__ uint32_t atomic_add_acq_rel(uint32_t *p, uint32_t v) 
   return old;
 }
 
+// Sum of the 8 children (2x, 2y, 2z) + {0,1}^3 of cell (x, y, z) in a
+// child level of side cdim held in shared memory.
+__device__ __forceinline__ uint4 sum_children(const uint4 *c, uint32_t x, uint32_t y, uint32_t z,
+                                              uint32_t cdim) {
+  uint4 acc = make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+  for (uint32_t dz = 0; dz < 2u; dz++)
+#pragma unroll
+    for (uint32_t dy = 0; dy < 2u; dy++)
+#pragma unroll
+      for (uint32_t dx = 0; dx < 2u; dx++)
+        acc = add_moment(acc, c[(2u * x + dx) + cdim * ((2u * y + dy) + cdim * (2u * z + dz))]);
+  return acc;
+}
+
 // Body of one upward task: the 8x8x8-leaf subtree `sub` of scene `scene`.
+// The completion ticket needs only the subtree root's moment, so the
+// reduction runs first in shared memory, thread 0 writes the root and takes
+// the ticket, and the other writes of the subtree (sources and records of its
+// cells, the cleared next-deposit leaves, the listed parents, the leaves'
+// sample cells) follow the ticket, off the path to the scene's last CTA.
 __device__ __forceinline__ void upward_task(
     const SceneDesc &S, uint32_t scene, uint32_t sub, uint4 *__restrict__ mom,
     uint4 *__restrict__ mom_next, float4 *__restrict__ src, float4 *__restrict__ aux,
     uint32_t *__restrict__ choice, WorkItem *__restrict__ plist, uint32_t plist_cap,
     Counters *__restrict__ ctr, uint32_t list_par, uint32_t *__restrict__ tickets, uint4 *s0,
-    uint4 *s1, uint4 *s2, WorkItem *s_items, uint32_t &s_nitems, uint32_t &s_base,
-    uint32_t &s_last, uint32_t &s_root) {
+    uint4 *s1, uint4 *s2, uint4 *s_top, WorkItem *s_items, uint32_t &s_nitems, uint32_t &s_base,
+    uint32_t &s_last) {
   const uint32_t tid = threadIdx.x;
-  const uint32_t D = S.depth, r = S.sub_level;
-  const uint32_t rdim = 1u << r;
-  const uint32_t sx = sub % rdim, sy = (sub / rdim) % rdim, sz = sub / (rdim * rdim);
+  const uint32_t D = S.depth, r = S.sub_level;  // r = D - 3
+  uint32_t sx, sy, sz;
+  cell_coords_lv(sub, r, sx, sy, sz);
   if (tid == 0) s_nitems = 0;
 
   // Leaves of this subtree: 8x8x8 block, x fastest (rows of 128 B); two per
@@ -86,103 +109,40 @@ __device__ __forceinline__ void upward_task(
     m[h] = mom[S.cell_off + leaf];
     seen |= m[h].x | mom_next[S.cell_off + leaf].x;
   }
-  if (tid < 73u) {  // 64 cells of level D-1, 8 of D-2, the subtree root at level r
-    const uint32_t l = tid < 64u ? D - 1u : (tid < 72u ? D - 2u : r);
-    const uint32_t w = tid < 64u ? 4u : (tid < 72u ? 2u : 1u);
-    const uint32_t i = tid < 64u ? tid : (tid < 72u ? tid - 64u : 0u);
-    const uint32_t ix = i % w, iy = (i / w) % w, iz = i / (w * w);
-    seen |= mom[S.cell_off + level_offset_d(l) + lin3(sx * w + ix, sy * w + iy, sz * w + iz, 1u << l)].x;
-  }
+  // Upper cell `tid` < 73 of the subtree: 64 of level D-1, 8 of D-2, the root.
+  const uint32_t ul = tid < 64u ? D - 1u : (tid < 72u ? D - 2u : r);
+  const uint32_t uw = tid < 64u ? 4u : (tid < 72u ? 2u : 1u);
+  const uint32_t ui = tid < 64u ? tid : (tid < 72u ? tid - 64u : 0u);
+  const uint32_t ucell = level_offset_d(ul) + lin3(sx * uw + ui % uw, sy * uw + (ui / uw) % uw,
+                                                   sz * uw + ui / (uw * uw), 1u << ul);
+  if (tid < 73u) seen |= mom[S.cell_off + ucell].x;
   // Empty now, empty in the previous deposit and cleared upper cells: the
   // subtree's moments, sources and next-deposit leaves are all zero already
   // (induction over steps; every rebuild of the moments clears the buffers),
   // so it only takes part in the ticket count.  Bodies never sit in its
   // leaves, so their sample cells are never read.
-  if (__syncthreads_or(seen != 0u)) {
-#pragma unroll
-  for (uint32_t h = 0; h < 2u; h++) {
-    const uint32_t t = tid + h * 256u;
-    const uint32_t lx = t & 7u, ly = (t >> 3) & 7u, lz = t >> 6;
-    const uint32_t leaf = level_offset_d(D) + lin3(sx * 8u + lx, sy * 8u + ly, sz * 8u + lz, dim);
-    s0[t] = m[h];
-    src[S.cell_off + leaf] = make_source(m[h], S.scale, S.gravity, S.n_f);
-    aux[S.cell_off + leaf] = make_aux(m[h].x, S.gravity, S.n_f);
-    mom_next[S.cell_off + leaf] = make_uint4(0u, 0u, 0u, 0u);
-  }
-  __syncthreads();
-  // Level D-1 (4x4x4 per subtree).
-  if (tid < 64u) {
-    const uint32_t x = tid & 3u, y = (tid >> 2) & 3u, z = tid >> 4;
-    uint4 acc = make_uint4(0u, 0u, 0u, 0u);
-#pragma unroll
-    for (uint32_t dz = 0; dz < 2u; dz++)
-#pragma unroll
-      for (uint32_t dy = 0; dy < 2u; dy++)
-#pragma unroll
-        for (uint32_t dx = 0; dx < 2u; dx++)
-          acc = add_moment(acc, s0[(2u * x + dx) + 8u * ((2u * y + dy) + 8u * (2u * z + dz))]);
-    s1[tid] = acc;
-    const uint32_t dim = 1u << (D - 1u);
-    const uint32_t cell = level_offset_d(D - 1u) + lin3(sx * 4u + x, sy * 4u + y, sz * 4u + z, dim);
-    store_cell(S, cell, acc, mom, src, aux);
-    if ((int32_t)acc.x > (int32_t)kAdaptive) s_items[atomicAdd(&s_nitems, 1u)] = {scene, cell};
-  }
-  __syncthreads();
-  if (tid < 8u) {
-    const uint32_t x = tid & 1u, y = (tid >> 1) & 1u, z = tid >> 2;
-    uint4 acc = make_uint4(0u, 0u, 0u, 0u);
-#pragma unroll
-    for (uint32_t dz = 0; dz < 2u; dz++)
-#pragma unroll
-      for (uint32_t dy = 0; dy < 2u; dy++)
-#pragma unroll
-        for (uint32_t dx = 0; dx < 2u; dx++)
-          acc = add_moment(acc, s1[(2u * x + dx) + 4u * ((2u * y + dy) + 4u * (2u * z + dz))]);
-    s2[tid] = acc;
-    const uint32_t dim = 1u << (D - 2u);
-    const uint32_t cell = level_offset_d(D - 2u) + lin3(sx * 2u + x, sy * 2u + y, sz * 2u + z, dim);
-    store_cell(S, cell, acc, mom, src, aux);
-    if ((int32_t)acc.x > (int32_t)kAdaptive) s_items[atomicAdd(&s_nitems, 1u)] = {scene, cell};
-  }
-  __syncthreads();
-  if (tid == 0) {
-    uint4 acc = make_uint4(0u, 0u, 0u, 0u);
-    for (uint32_t k = 0; k < 8u; k++) acc = add_moment(acc, s2[k]);
-    const uint32_t cell = level_offset_d(r) + lin3(sx, sy, sz, rdim);
-    store_cell(S, cell, acc, mom, src, aux);
-    if ((int32_t)acc.x > (int32_t)kAdaptive) s_items[atomicAdd(&s_nitems, 1u)] = {scene, cell};
-    s_root = acc.x;
-  }
-  __syncthreads();
-  // Sample cell of each leaf.  Counts never shrink towards the root, so when
-  // this subtree's root holds more than 16 bodies every level <= r is skipped
-  // by the descent and the choice lies within the subtree: the first of
-  // levels D-2, D-1 with count <= 16, else the leaf.
-#pragma unroll
-  for (uint32_t h = 0; h < 2u; h++) {
-    const uint32_t t = tid + h * 256u;
-    const uint32_t lx = t & 7u, ly = (t >> 3) & 7u, lz = t >> 6;
-    uint32_t v = kChoiceUnresolved;
-    if ((int32_t)s_root > (int32_t)kAdaptive) {
-      const uint32_t c2 = s2[(lx >> 2) + 2u * ((ly >> 2) + 2u * (lz >> 2))].x;
-      const uint32_t c1 = s1[(lx >> 1) + 4u * ((ly >> 1) + 4u * (lz >> 1))].x;
-      if ((int32_t)c2 <= (int32_t)kAdaptive) {
-        v = ((D - 2u) << 28) | (level_offset_d(D - 2u) +
-                                lin3_lv(sx * 2u + (lx >> 2), sy * 2u + (ly >> 2), sz * 2u + (lz >> 2), D - 2u));
-      } else if ((int32_t)c1 <= (int32_t)kAdaptive) {
-        v = ((D - 1u) << 28) | (level_offset_d(D - 1u) +
-                                lin3_lv(sx * 4u + (lx >> 1), sy * 4u + (ly >> 1), sz * 4u + (lz >> 1), D - 1u));
-      } else {
-        v = (D << 28) | (level_offset_d(D) + lin3_lv(sx * 8u + lx, sy * 8u + ly, sz * 8u + lz, D));
-      }
+  const bool live = __syncthreads_or(seen != 0u);
+  if (live) {
+    s0[tid] = m[0];
+    s0[tid + 256u] = m[1];
+    __syncthreads();
+    if (tid < 64u) s1[tid] = sum_children(s0, tid & 3u, (tid >> 2) & 3u, tid >> 4, 8u);
+    __syncthreads();
+    if (tid < 8u) s2[tid] = sum_children(s1, tid & 1u, (tid >> 1) & 1u, tid >> 2, 4u);
+    __syncthreads();
+    if (tid == 0) {
+      uint4 acc = make_uint4(0u, 0u, 0u, 0u);
+      for (uint32_t k = 0; k < 8u; k++) acc = add_moment(acc, s2[k]);
+      s2[8] = acc;
+      // The level-r cell the last CTA reads.
+      mom[S.cell_off + level_offset_d(r) + lin3(sx, sy, sz, 1u << r)] = acc;
     }
-    choice[S.cell_off + level_offset_d(D) + lin3_lv(sx * 8u + lx, sy * 8u + ly, sz * 8u + lz, D)] = v;
   }
-  }  // not empty
 
   // The scene's last finished subtree reduces levels r-1 .. 0.  Only thread 0
   // wrote the level-r cell that reduction reads; its tickets release that
-  // write (and acquire the earlier subtrees' ones) on the way to the last CTA.
+  // write (and acquire the earlier subtrees' ones) on the way to the last CTA,
+  // whose other threads are ordered after thread 0 by the barrier below.
   if (tid == 0) {
     const uint32_t ntasks = 1u << (3u * r);
     const uint32_t ngroups = (ntasks + kTicketGroup - 1u) / kTicketGroup;
@@ -200,34 +160,78 @@ __device__ __forceinline__ void upward_task(
     s_last = last;
   }
   __syncthreads();
+
+  if (live) {
+    // Leaves: source records and the cleared next-deposit leaf.
+#pragma unroll
+    for (uint32_t h = 0; h < 2u; h++) {
+      const uint32_t t = tid + h * 256u;
+      const uint32_t lx = t & 7u, ly = (t >> 3) & 7u, lz = t >> 6;
+      const uint32_t leaf = S.cell_off + level_offset_d(D) + lin3(sx * 8u + lx, sy * 8u + ly, sz * 8u + lz, dim);
+      src[leaf] = make_source(m[h], S.scale, S.gravity, S.n_f);
+      aux[leaf] = make_aux(m[h].x, S.gravity, S.n_f);
+      mom_next[leaf] = make_uint4(0u, 0u, 0u, 0u);
+    }
+    // Upper cells.
+    if (tid < 73u) {
+      const uint4 acc = tid < 64u ? s1[tid] : (tid < 72u ? s2[tid - 64u] : s2[8]);
+      store_cell(S, ucell, acc, mom, src, aux);
+      if ((int32_t)acc.x > (int32_t)kAdaptive) s_items[atomicAdd(&s_nitems, 1u)] = {scene, ucell};
+    }
+    // Sample cell of each leaf.  Counts never shrink towards the root, so
+    // when this subtree's root holds more than 16 bodies every level <= r is
+    // skipped by the descent and the choice lies within the subtree: the
+    // first of levels D-2, D-1 with count <= 16, else the leaf.
+    const uint32_t root_count = s2[8].x;
+#pragma unroll
+    for (uint32_t h = 0; h < 2u; h++) {
+      const uint32_t t = tid + h * 256u;
+      const uint32_t lx = t & 7u, ly = (t >> 3) & 7u, lz = t >> 6;
+      uint32_t v = kChoiceUnresolved;
+      if ((int32_t)root_count > (int32_t)kAdaptive) {
+        const uint32_t c2 = s2[(lx >> 2) + 2u * ((ly >> 2) + 2u * (lz >> 2))].x;
+        const uint32_t c1 = s1[(lx >> 1) + 4u * ((ly >> 1) + 4u * (lz >> 1))].x;
+        if ((int32_t)c2 <= (int32_t)kAdaptive) {
+          v = ((D - 2u) << 28) | (level_offset_d(D - 2u) +
+                                  lin3_lv(sx * 2u + (lx >> 2), sy * 2u + (ly >> 2), sz * 2u + (lz >> 2), D - 2u));
+        } else if ((int32_t)c1 <= (int32_t)kAdaptive) {
+          v = ((D - 1u) << 28) | (level_offset_d(D - 1u) +
+                                  lin3_lv(sx * 4u + (lx >> 1), sy * 4u + (ly >> 1), sz * 4u + (lz >> 1), D - 1u));
+        } else {
+          v = (D << 28) | (level_offset_d(D) + lin3_lv(sx * 8u + lx, sy * 8u + ly, sz * 8u + lz, D));
+        }
+      }
+      choice[S.cell_off + level_offset_d(D) + lin3_lv(sx * 8u + lx, sy * 8u + ly, sz * 8u + lz, D)] = v;
+    }
+  }
+
   if (s_last) {
-    __threadfence();
     // Level r has at most 512 cells: stage it (written by other CTAs) via L2.
     const uint32_t nr = 1u << (3u * r);
     for (uint32_t i = tid; i < nr; i += blockDim.x)
       s0[i] = __ldcg(&mom[S.cell_off + level_offset_d(r) + i]);
     __syncthreads();
+    // Sums of levels r-1 .. 0 into s_top (level l at level_offset(l)), then
+    // their records in one pass.
     for (int l = (int)r - 1; l >= 0; l--) {
-      const uint32_t dim = 1u << l, cdim = dim << 1, nl = 1u << (3u * l);
-      uint4 acc = make_uint4(0u, 0u, 0u, 0u);
+      const uint32_t nl = 1u << (3u * l);
       if (tid < nl) {
         uint32_t x, y, z;
         cell_coords_lv(tid, (uint32_t)l, x, y, z);
-        for (uint32_t dz = 0; dz < 2u; dz++)
-          for (uint32_t dy = 0; dy < 2u; dy++)
-            for (uint32_t dx = 0; dx < 2u; dx++)
-              acc = add_moment(acc, s0[lin3(2u * x + dx, 2u * y + dy, 2u * z + dz, cdim)]);
-        const uint32_t cell = level_offset_d((uint32_t)l) + tid;
-        store_cell(S, cell, acc, mom, src, aux);
-        if ((int32_t)acc.x > (int32_t)kAdaptive) s_items[atomicAdd(&s_nitems, 1u)] = {scene, cell};
+        const uint4 *child = l + 1 == (int)r ? s0 : s_top + level_offset_d((uint32_t)l + 1u);
+        s_top[level_offset_d((uint32_t)l) + tid] = sum_children(child, x, y, z, 2u << l);
       }
       __syncthreads();
-      if (tid < nl) s0[tid] = acc;
-      __syncthreads();
+    }
+    if (tid < level_offset_d(r)) {  // every cell of levels 0 .. r-1
+      const uint4 acc = s_top[tid];
+      store_cell(S, tid, acc, mom, src, aux);
+      if ((int32_t)acc.x > (int32_t)kAdaptive) s_items[atomicAdd(&s_nitems, 1u)] = {scene, tid};
     }
   }
+  __syncthreads();
   // Publish the parents listed by this subtree (and, in the scene's last
-  // CTA, by the top levels): after the tickets, off the path to the last CTA.
+  // CTA, by the top levels).
   if (tid == 0 && s_nitems != 0u) {
     uint32_t base = atomicAdd(&ctr->parents[list_par], s_nitems);
     if (base + s_nitems > plist_cap) {
@@ -259,9 +263,10 @@ __global__ void __launch_bounds__(256) k_upward(const SceneDesc *__restrict__ sc
                                                 uint32_t *__restrict__ tickets, uint32_t clear_ctas) {
   __shared__ uint4 s0[512];
   __shared__ uint4 s1[64];
-  __shared__ uint4 s2[8];
+  __shared__ uint4 s2[9];     // level D-2, then the subtree root
+  __shared__ uint4 s_top[73];  // levels 0 .. r-1 of the last CTA (r <= 3)
   __shared__ WorkItem s_items[160];  // a subtree's 73 cells + the top levels' 73
-  __shared__ uint32_t s_nitems, s_base, s_last, s_root;
+  __shared__ uint32_t s_nitems, s_base, s_last;
   __shared__ SceneDesc sS;
   const uint32_t tid = threadIdx.x;
   if (blockIdx.x < clear_ctas) {
@@ -315,7 +320,7 @@ __global__ void __launch_bounds__(256) k_upward(const SceneDesc *__restrict__ sc
       load_scene(sS, scenes, scene);
     }
     upward_task(sS, scene, task - sS.task_off, mom, mom_next, src, aux, choice, plist, plist_cap,
-                ctr, list_par, tickets, s0, s1, s2, s_items, s_nitems, s_base, s_last, s_root);
+                ctr, list_par, tickets, s0, s1, s2, s_top, s_items, s_nitems, s_base, s_last);
   }
   grid_dependents_may_launch();
 }
