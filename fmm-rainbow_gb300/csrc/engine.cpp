@@ -153,12 +153,13 @@ int Engine::create(const std::vector<SceneSpec> &specs, Engine **out) {
   E->tiles_ = body_off / kTile;
   E->cells_ = cell_off;
   E->tasks_ = task_off;
-  // Sort key = scene rank above a Morton code of fine cells (level F >= depth):
-  // bodies of one leaf stay contiguous and a warp's bodies stay spatially
-  // compact, so a few steps of drift still leave few leaf runs per warp.
+  // Sort key = scene rank above a Morton code of fine cells (level F >= depth,
+  // at most 8: one scene sorts in three 8-bit radix passes): bodies of one
+  // leaf stay contiguous and a warp's bodies stay spatially compact, so a few
+  // steps of drift still leave few leaf runs per warp.
   {
     const uint32_t scene_bits = log2_ceil((uint32_t)specs.size());
-    const uint32_t fine = std::min(10u, (32u - scene_bits) / 3u);
+    const uint32_t fine = std::min(8u, (32u - scene_bits) / 3u);
     for (uint32_t i = 0; i < E->scenes_.size(); i++) {
       E->scenes_[i].key_level = fine;
       E->scenes_[i].key_base = scene_bits ? (i << (3u * fine)) : 0u;

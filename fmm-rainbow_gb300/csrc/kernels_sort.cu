@@ -8,7 +8,7 @@
 // is stable, so the resident order is a deterministic function of the input.
 //
 // Per 8-bit pass:
-//   k_sort_hist     per 4096-key tile, digit histogram in shared memory
+//   k_sort_hist     per 2048-key tile, digit histogram in shared memory
 //   k_sort_scan     one CTA per digit: exclusive scan of that digit's tile
 //                   counts (digit-major layout), plus the digit total
 //   k_sort_scatter  per tile: digit base + tile offset + stable rank inside
@@ -22,8 +22,8 @@
 namespace rfmm {
 
 constexpr uint32_t kSortThreads = 256u;
-constexpr uint32_t kSortItems = 16u;
-constexpr uint32_t kSortTile = kSortThreads * kSortItems;  // 4096 keys
+constexpr uint32_t kSortItems = 8u;
+constexpr uint32_t kSortTile = kSortThreads * kSortItems;  // 2048 keys
 
 uint32_t sort_tiles(uint32_t n) { return (n + kSortTile - 1u) / kSortTile; }
 
