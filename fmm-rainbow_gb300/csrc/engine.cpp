@@ -13,7 +13,7 @@ namespace rfmm {
 
 namespace {
 
-constexpr uint32_t kMaxScenes = 1u << 14; // scene rank must fit above the 18 Morton bits
+constexpr uint32_t kMaxScenes = kMaxSceneCount;
 
 uint32_t pad_tiles(uint32_t n) { return (n + kTile - 1u) / kTile; }
 
@@ -466,9 +466,7 @@ int Engine::upload(uint32_t scene, const void *src, size_t bytes, cudaMemcpyKind
   const SceneDesc &d = scenes_[scene];
   if (bytes != 32ull * d.n) return RFMM_ERR_INVALID;
   RF_CK(cudaMemcpyAsync(d_part_[pcur_] + 2ull * d.body_off, src, bytes, kind, stream_));
-  launch_iota(stream_, d_ids_[pcur_] + d.body_off, pad_tiles(d.n) * kTile);
-  RF_CK(cudaGetLastError());
-  launches_ += 1;
+  mark_fresh(scene);  // ids are numbered by the commit's key pass
   uploaded_[scene] = true;
   committed_ = false;
   return RFMM_OK;
@@ -479,9 +477,9 @@ int Engine::seed_galaxy(uint32_t scene) {
   const SceneDesc &d = scenes_[scene];
   LaunchCtx L = ctx(mcur_, lpar_, pcur_);
   launch_initialize(L, d_part_[pcur_], d.tile_off, pad_tiles(d.n));
-  launch_iota(stream_, d_ids_[pcur_] + d.body_off, pad_tiles(d.n) * kTile);
   RF_CK(cudaGetLastError());
-  launches_ += 2;
+  launches_ += 1;
+  mark_fresh(scene);
   uploaded_[scene] = true;
   committed_ = false;
   return RFMM_OK;
@@ -599,7 +597,12 @@ int Engine::commit() {
   for (bool u : uploaded_)
     if (!u) return RFMM_ERR_STATE;
   LaunchCtx L = ctx(mcur_, lpar_, pcur_);
-  launch_keys(L, sort_.keys[0], sort_.vals[0], nullptr, 0, tiles_, 0u);
+  // The key pass also numbers the bodies of scenes uploaded since the last
+  // commit in caller order.
+  launch_keys(L, sort_.keys[0], sort_.vals[0], d_ids_[pcur_], any_fresh_ ? 2 : 0, tiles_, 0u,
+              &fresh_);
+  fresh_ = SceneMask{};
+  any_fresh_ = false;
   const int r = radix_sort(stream_, sort_, slots_, key_bits_);
   // The rebuilt tree starts from cleared moment, source and record buffers
   // (the upward pass skips subtrees that are empty in both moment buffers).
@@ -665,10 +668,10 @@ int Engine::set_near_mode(uint32_t mode) {
   LaunchCtx L = ctx(mcur_, lpar_, pcur_);
   launch_unpermute(L, d_ids_[pcur_], d_part_[pcur_ ^ 1u], 0u, tiles_);
   pcur_ ^= 1u;
-  for (const SceneDesc &d : scenes_)
-    if (d.n != 0u) launch_iota(stream_, d_ids_[pcur_] + d.body_off, pad_tiles(d.n) * kTile);
+  for (uint32_t i = 0; i < scenes_.size(); i++)
+    if (scenes_[i].n != 0u) mark_fresh(i);  // back in caller order
   RF_CK(cudaGetLastError());
-  launches_ += 1u + (uint64_t)scenes_.size();
+  launches_ += 1u;
   return commit();
 }
 

@@ -142,6 +142,12 @@ class Engine {
   uint32_t *d_tile_scene_ = nullptr, *d_task_scene_ = nullptr;
   float4 *d_part_[2] = {nullptr, nullptr};
   uint32_t *d_ids_[2] = {nullptr, nullptr};
+  SceneMask fresh_{};       // scenes uploaded since the last commit (ids still to number)
+  bool any_fresh_ = false;
+  void mark_fresh(uint32_t scene) {
+    fresh_.bits[scene >> 5] |= 1u << (scene & 31u);
+    any_fresh_ = true;
+  }
   uint4 *d_mom_[2] = {nullptr, nullptr};
   uint4 *d_mom_scratch_ = nullptr;
   float4 *d_accphi_ = nullptr;    // diagnostics: per-body acceleration + potential

@@ -518,9 +518,11 @@ __global__ void __launch_bounds__(256) k_keys(const SceneDesc *__restrict__ scen
                                               const float4 *__restrict__ part,
                                               uint32_t *__restrict__ keys, uint32_t *__restrict__ vals,
                                               uint32_t *__restrict__ ids, int fresh_ids,
-                                              uint32_t tile_base) {
+                                              uint32_t tile_base,
+                                              const __grid_constant__ SceneMask fresh) {
   const uint32_t tile = tile_base + blockIdx.x;
-  const SceneDesc &S = scenes[tile_scene[tile]];
+  const uint32_t sc = tile_scene[tile];
+  const SceneDesc &S = scenes[sc];
   const uint32_t slot = tile * kTile + threadIdx.x;
   const uint32_t out = blockIdx.x * kTile + threadIdx.x;  // keys/vals are relative to tile_base
   const uint32_t local = slot - S.body_off;
@@ -543,7 +545,7 @@ __global__ void __launch_bounds__(256) k_keys(const SceneDesc *__restrict__ scen
   }
   keys[out] = key;
   vals[out] = slot;
-  if (fresh_ids) ids[slot] = local;
+  if (fresh_ids == 1 || (fresh_ids == 2 && ((fresh.bits[sc >> 5] >> (sc & 31u)) & 1u))) ids[slot] = local;
 }
 
 // Apply a permutation to the resident bodies (and their caller ids).  With
@@ -761,9 +763,10 @@ void launch_deposit(const LaunchCtx &L, uint4 *moments, uint32_t tiles) {
 }
 
 void launch_keys(const LaunchCtx &L, uint32_t *keys, uint32_t *vals, uint32_t *ids, int fresh_ids,
-                 uint32_t tiles, uint32_t tile_base) {
+                 uint32_t tiles, uint32_t tile_base, const SceneMask *fresh) {
+  static const SceneMask kNone{};
   k_keys<<<tiles, kTile, 0, L.stream>>>(L.scenes, L.tile_scene, L.part, keys, vals, ids, fresh_ids,
-                                        tile_base);
+                                        tile_base, fresh != nullptr ? *fresh : kNone);
 }
 
 void launch_gather(const LaunchCtx &L, const uint32_t *perm, const float4 *part_in,

@@ -11,6 +11,15 @@
 
 namespace rfmm {
 
+// Most scenes one engine holds (the scene rank sits above an 18-bit Morton
+// code in the sort key).
+constexpr uint32_t kMaxSceneCount = 1u << 14;
+
+// One bit per scene, passed to kernels by value.
+struct SceneMask {
+  uint32_t bits[kMaxSceneCount / 32u];
+};
+
 // Device pointers one launch needs; filled by the engine for each step parity.
 struct LaunchCtx {
   cudaStream_t stream;
@@ -83,8 +92,10 @@ cudaError_t configure_tree_kernels();
 void launch_integrate(const LaunchCtx &L, uint32_t tiles);
 void launch_deposit(const LaunchCtx &L, uint4 *moments, uint32_t tiles);
 // keys/vals of tiles [tile_base, tile_base + tiles), written from index 0.
+// Body ids (caller order) are written too for every scene (fresh_ids 1) or
+// for the scenes set in *fresh (fresh_ids 2).
 void launch_keys(const LaunchCtx &L, uint32_t *keys, uint32_t *vals, uint32_t *ids, int fresh_ids,
-                 uint32_t tiles, uint32_t tile_base);
+                 uint32_t tiles, uint32_t tile_base, const SceneMask *fresh = nullptr);
 // Permute the bodies of tiles [tile_base, tile_base + tiles) (perm from index 0).
 // With `pos_out`, also writes each permuted body's position float4 there.
 void launch_gather(const LaunchCtx &L, const uint32_t *perm, const float4 *part_in,
