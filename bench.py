@@ -440,9 +440,10 @@ def run_gpu_batched(args, w):
     batch = rfmm.Batch(sizes, [params] * len(ps))
     batch.set_stream(stream.cuda_stream)
 
+    dev_ptrs = [d.data_ptr() for d in dev]
+
     def batched_step():
-        for i, d in enumerate(dev):
-            batch.upload_device(i, d.data_ptr(), d.numel())
+        batch.upload_device_all(dev_ptrs)  # one copy launch for all scenes
         batch.commit()
         batch.step(fmm_steps)
 

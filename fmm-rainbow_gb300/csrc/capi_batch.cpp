@@ -84,6 +84,11 @@ int rfmm_batch_upload_device(rfmm_batch *b, uint32_t scene, const void *device_a
   return b->engine->upload(scene, device_aos, bytes, cudaMemcpyDeviceToDevice);
 }
 
+int rfmm_batch_upload_device_all(rfmm_batch *b, const void *const *device_aos) {
+  if (bad(b)) return RFMM_ERR_INVALID;
+  return b->engine->upload_all_device(device_aos);
+}
+
 int rfmm_batch_seed_galaxy(rfmm_batch *b, uint32_t scene) {
   if (bad_scene(b, scene)) return RFMM_ERR_INVALID;
   return b->engine->seed_galaxy(scene);

@@ -472,6 +472,50 @@ int Engine::upload(uint32_t scene, const void *src, size_t bytes, cudaMemcpyKind
   return RFMM_OK;
 }
 
+int Engine::upload_all_device(const void *const *src) {
+  if (src == nullptr) return RFMM_ERR_INVALID;
+  for (uint32_t i = 0; i < scenes_.size(); i++)
+    if (scenes_[i].n != 0u && src[i] == nullptr) return RFMM_ERR_INVALID;
+  LaunchCtx L = ctx(mcur_, lpar_, pcur_);
+  static_assert(sizeof(UploadSources) <= 16384, "kernel parameter size");
+  UploadSources us;
+  for (uint32_t base = 0; base < scenes_.size(); base += kUploadChunk) {
+    const uint32_t count = std::min<uint32_t>(kUploadChunk, (uint32_t)scenes_.size() - base);
+    for (uint32_t j = 0; j < count; j++) {
+      const SceneDesc &d = scenes_[base + j];
+      us.p[j] = nullptr;
+      if (d.n == 0u) continue;
+      // The copy kernel takes 16-byte aligned device (or managed) memory;
+      // anything else is copied by the runtime.
+      cudaPointerAttributes a{};
+      const bool direct = cudaPointerGetAttributes(&a, src[base + j]) == cudaSuccess &&
+                          (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) &&
+                          (reinterpret_cast<uintptr_t>(src[base + j]) & 15u) == 0u;
+      if (direct) {
+        us.p[j] = static_cast<const float4 *>(src[base + j]);
+      } else {
+        (void)cudaGetLastError();  // a failed attribute query leaves no error behind
+        RF_CK(cudaMemcpyAsync(d_part_[pcur_] + 2ull * d.body_off, src[base + j], 32ull * d.n,
+                              cudaMemcpyDefault, stream_));
+      }
+    }
+    const SceneDesc &first = scenes_[base], &last = scenes_[base + count - 1u];
+    const uint32_t tile_end = last.tile_off + pad_tiles(last.n);
+    if (tile_end > first.tile_off) {
+      launch_upload_scenes(L, d_part_[pcur_], first.tile_off, tile_end - first.tile_off, base, us);
+      RF_CK(cudaGetLastError());
+      launches_ += 1;
+    }
+  }
+  for (uint32_t i = 0; i < scenes_.size(); i++) {
+    if (scenes_[i].n == 0u) continue;
+    mark_fresh(i);  // ids are numbered by the commit's key pass
+    uploaded_[i] = true;
+  }
+  committed_ = false;
+  return RFMM_OK;
+}
+
 int Engine::seed_galaxy(uint32_t scene) {
   if (scene >= scenes_.size()) return RFMM_ERR_INVALID;
   const SceneDesc &d = scenes_[scene];

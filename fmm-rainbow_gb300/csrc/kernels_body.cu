@@ -821,6 +821,29 @@ __global__ void k_iota(uint32_t *__restrict__ ids, uint32_t count) {
   if (i < count) ids[i] = i;
 }
 
+// Bulk upload, one CTA per 256-slot tile: two 16-byte loads and stores per body.
+__global__ void __launch_bounds__(256) k_upload_scenes(const SceneDesc *__restrict__ scenes,
+                                                       const uint32_t *__restrict__ tile_scene,
+                                                       float4 *__restrict__ part, uint32_t tile_base,
+                                                       uint32_t scene_base,
+                                                       const __grid_constant__ UploadSources src) {
+  const uint32_t tile = tile_base + blockIdx.x;
+  const uint32_t sc = tile_scene[tile];
+  const float4 *from = src.p[sc - scene_base];
+  const SceneDesc &S = scenes[sc];
+  const uint32_t slot = tile * kTile + threadIdx.x, local = slot - S.body_off;
+  if (from != nullptr && local < S.n) {
+    part[2u * slot] = from[2u * local];
+    part[2u * slot + 1u] = from[2u * local + 1u];
+  }
+}
+
+void launch_upload_scenes(const LaunchCtx &L, float4 *part, uint32_t tile_base, uint32_t tiles,
+                          uint32_t scene_base, const UploadSources &src) {
+  k_upload_scenes<<<tiles, kTile, 0, L.stream>>>(L.scenes, L.tile_scene, part, tile_base, scene_base,
+                                                 src);
+}
+
 void launch_iota(cudaStream_t stream, uint32_t *ids, uint32_t count) {
   k_iota<<<(count + 255u) / 256u, 256, 0, stream>>>(ids, count);
 }

@@ -20,6 +20,13 @@ struct SceneMask {
   uint32_t bits[kMaxSceneCount / 32u];
 };
 
+// Caller device buffers of up to kUploadChunk scenes for one bulk upload
+// launch (null: the scene is skipped), passed by value.
+constexpr uint32_t kUploadChunk = 1024u;
+struct UploadSources {
+  const float4 *p[kUploadChunk];
+};
+
 // Device pointers one launch needs; filled by the engine for each step parity.
 struct LaunchCtx {
   cudaStream_t stream;
@@ -106,6 +113,10 @@ void launch_leaf_starts(const LaunchCtx &L, const uint32_t *sorted_keys, uint32_
 void launch_unpermute(const LaunchCtx &L, const uint32_t *ids, float4 *out, uint32_t tile_base,
                       uint32_t tiles);
 void launch_initialize(const LaunchCtx &L, float4 *part_out, uint32_t tile_base, uint32_t tiles);
+// Bodies of the scenes whose tiles are [tile_base, tile_base + tiles) copied
+// from src.p[scene - scene_base] (caller order, 16-byte aligned) into their slots.
+void launch_upload_scenes(const LaunchCtx &L, float4 *part, uint32_t tile_base, uint32_t tiles,
+                          uint32_t scene_base, const UploadSources &src);
 void launch_iota(cudaStream_t stream, uint32_t *ids, uint32_t count);
 uint32_t body_ctas_per_sm();  // resident 256-thread CTAs per SM of the persistent body passes
 // FMM acceleration + potential per body of tiles [tile_base, +tiles), caller order.

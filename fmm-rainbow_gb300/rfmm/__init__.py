@@ -145,6 +145,7 @@ SIGNATURES = {
     "rfmm_batch_set_params": (_i, [_vp, _u32, _P]),
     "rfmm_batch_upload": (_i, [_vp, _u32, _vp, _sz]),
     "rfmm_batch_upload_device": (_i, [_vp, _u32, _vp, _sz]),
+    "rfmm_batch_upload_device_all": (_i, [_vp, _vp]),
     "rfmm_batch_seed_galaxy": (_i, [_vp, _u32]),
     "rfmm_batch_commit": (_i, [_vp]),
     "rfmm_batch_solve_fields": (_i, [_vp]),
@@ -479,6 +480,12 @@ class Batch:
 
     def upload_device(self, scene, ptr, nbytes):
         _check(lib().rfmm_batch_upload_device(self._h, scene, ptr, nbytes), "rfmm_batch_upload_device")
+
+    def upload_device_all(self, ptrs):
+        """Every scene at once: ptrs[s] is the device address of scene s's bodies."""
+        assert len(ptrs) == len(self.sizes)
+        arr = (C.c_void_p * len(ptrs))(*ptrs)
+        _check(lib().rfmm_batch_upload_device_all(self._h, arr), "rfmm_batch_upload_device_all")
 
     def commit(self):
         _check(lib().rfmm_batch_commit(self._h), "rfmm_batch_commit")

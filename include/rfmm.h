@@ -283,6 +283,10 @@ int rfmm_batch_set_params(rfmm_batch *b, uint32_t scene, const rfmm_params *para
  * every staged scene resident (sort + deposit) in one pass. */
 int rfmm_batch_upload(rfmm_batch *b, uint32_t scene, const void *host_aos, size_t bytes);
 int rfmm_batch_upload_device(rfmm_batch *b, uint32_t scene, const void *device_aos, size_t bytes);
+/* Stage every scene at once: device_aos[s] holds scene s's bodies (32 B each,
+ * caller order) in device memory; one copy launch for all scenes instead of
+ * one call per scene. */
+int rfmm_batch_upload_device_all(rfmm_batch *b, const void *const *device_aos);
 int rfmm_batch_seed_galaxy(rfmm_batch *b, uint32_t scene);
 int rfmm_batch_commit(rfmm_batch *b);
 int rfmm_batch_solve_fields(rfmm_batch *b);

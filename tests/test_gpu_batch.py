@@ -68,3 +68,32 @@ def test_batch_equals_plain_handles_and_reupload(rfmm_mod):
             ref.append(s.particles())
     for i in range(3):
         assert np.array_equal(_bits(got[i]), _bits(ref[i])), i
+
+
+def test_bulk_device_upload_equals_per_scene_uploads(rfmm_mod):
+    """rfmm_batch_upload_device_all (one copy launch, device buffers) leaves
+    exactly the state per-scene uploads leave; a misaligned buffer takes the
+    runtime copy."""
+    import torch
+    R = rfmm_mod
+    ps = _mixed_scenes()
+    prm = R.default_params(gravity=1.0, softening=1e-3, dt=5e-4)
+    dev = [torch.from_numpy(p.view(np.uint8).copy()).cuda() for p in ps]
+    # Scene 3 from a buffer offset by 4 bytes (not 16-byte aligned).
+    odd = torch.empty(dev[3].numel() + 4, dtype=torch.uint8, device="cuda")
+    odd[4:].copy_(dev[3])
+    ptrs = [d.data_ptr() for d in dev]
+    ptrs[3] = odd.data_ptr() + 4
+    out = []
+    for bulk in (False, True):
+        with R.Batch([len(p) for p in ps], [prm] * len(ps)) as b:
+            if bulk:
+                b.upload_device_all(ptrs)
+            else:
+                for i, d in enumerate(dev):
+                    b.upload_device(i, d.data_ptr(), d.numel())
+            b.commit()
+            b.step(3)
+            out.append([b.download(i) for i in range(len(ps))])
+    for i in range(len(ps)):
+        assert np.array_equal(_bits(out[0][i]), _bits(out[1][i])), i
