@@ -181,6 +181,11 @@ int rfmm_set_near_mode(rfmm_handle *h, uint32_t mode) {
   return h->engine->set_near_mode(mode);
 }
 
+int rfmm_check_wait_timeout(rfmm_handle *h, uint32_t polls) {
+  if (guard(h)) return RFMM_ERR_INVALID;
+  return h->engine->check_wait_timeout(polls);
+}
+
 int rfmm_device_error(rfmm_handle *h, uint32_t *code, uint32_t *info) {
   if (guard(h)) return RFMM_ERR_INVALID;
   return h->engine->device_error(code, info);

@@ -811,6 +811,21 @@ int Engine::sync() {
   return check_device_error();
 }
 
+int Engine::check_wait_timeout(uint32_t polls) {
+  if (polls == 0u || polls > (1u << 22)) return RFMM_ERR_INVALID;
+  // The check has its own status word; the engine's error word is untouched.
+  uint32_t *status = &d_ctr_->wait_check;
+  RF_CK(cudaMemsetAsync(status, 0xFF, sizeof(uint32_t), stream_));
+  launch_wait_check(stream_, polls, status);
+  RF_CK(cudaGetLastError());
+  launches_ += 1;
+  uint32_t got = 0xFFFFFFFFu;
+  RF_CK(cudaMemcpyAsync(&got, status, sizeof(got), cudaMemcpyDeviceToHost, stream_));
+  RF_CK(cudaStreamSynchronize(stream_));
+  if (got == (uint32_t)kDevErrTmaTimeout) return RFMM_ERR_TIMEOUT;
+  return got == (uint32_t)kDevErrNone ? RFMM_OK : RFMM_ERR_CUDA;
+}
+
 int Engine::device_error(uint32_t *code, uint32_t *info) {
   Counters c;
   RF_CK(cudaMemcpyAsync(&c, d_ctr_, sizeof(Counters), cudaMemcpyDeviceToHost, stream_));

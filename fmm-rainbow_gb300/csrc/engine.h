@@ -47,6 +47,8 @@ class Engine {
   // Copy a scene's bodies (caller order) into the resident buffer; the new
   // bodies take effect at the next commit().
   int upload(uint32_t scene, const void *src, size_t bytes, cudaMemcpyKind kind);
+  // Runs a bounded wait that cannot complete; RFMM_ERR_TIMEOUT when it gave up.
+  int check_wait_timeout(uint32_t polls);
   // Every scene's bodies from one device buffer per scene (caller order).
   int upload_all_device(const void *const *src);
   int seed_galaxy(uint32_t scene);

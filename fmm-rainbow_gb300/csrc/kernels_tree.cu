@@ -388,10 +388,12 @@ __device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, uint32_t
                : "memory");
 }
 
-// Bounded wait on an mbarrier phase; returns false when it gave up.
-__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, uint32_t parity) {
+// Bounded wait on an mbarrier phase (at most `polls` polls); returns false
+// when it gave up.
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, uint32_t parity,
+                                          uint32_t polls = 1u << 22) {
   const uint32_t addr = smem_u32(bar);
-  for (uint32_t it = 0; it < (1u << 22); ++it) {
+  for (uint32_t it = 0; it < polls; ++it) {
     uint32_t done;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
@@ -479,9 +481,14 @@ __global__ void __launch_bounds__(256) k_m2l(const SceneDesc *__restrict__ scene
     const float ctx = cell_center_lv(tx, l), cty = cell_center_lv(ty, l), ctz = cell_center_lv(tz, l);
     const float eps = (0.06f * kHalf) * pow2_neg(l);  // wgsl:507, / 2^l as an exact scaling
     if (l >= 3u) {
-      if (warp == 0u && !mbar_wait(&sh.mbar, phase) && lane == 0u) {
-        if (atomicCAS(&ctr->error, 0u, (uint32_t)kDevErrTmaTimeout) == 0u) ctr->error_info = item;
-        sh.stop = 1u;
+      if (warp == 0u && !mbar_wait(&sh.mbar, phase)) {
+        // Give the copy in flight a second bounded wait before the CTA
+        // leaves (its destination is this CTA's shared memory).
+        (void)mbar_wait(&sh.mbar, phase);
+        if (lane == 0u) {
+          if (atomicCAS(&ctr->error, 0u, (uint32_t)kDevErrTmaTimeout) == 0u) ctr->error_info = item;
+          sh.stop = 1u;
+        }
       }
       phase ^= 1u;
     }
@@ -708,6 +715,27 @@ __global__ void __launch_bounds__(256) k_l2l_near(const SceneDesc *__restrict__ 
     if (lane < 12u) fields[(size_t)target * 12u + lane] = f;
   }
   grid_dependents_may_launch();
+}
+
+// ------------------------------------------------------- wait self-check
+
+// One CTA waits, with the kernels' bounded wait, on an mbarrier phase that
+// nothing completes (no thread arrives, no copy is issued), then writes
+// kDevErrTmaTimeout to *status when the wait gave up as it must.  Nothing is
+// in flight, so the CTA leaves cleanly and the context stays usable.
+__global__ void __launch_bounds__(32) k_wait_check(uint32_t polls, uint32_t *__restrict__ status) {
+  __shared__ unsigned long long bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1u);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncwarp();
+  const bool done = mbar_wait(&bar, 0u, polls);
+  if (threadIdx.x == 0) *status = done ? (uint32_t)kDevErrNone : (uint32_t)kDevErrTmaTimeout;
+}
+
+void launch_wait_check(cudaStream_t stream, uint32_t polls, uint32_t *status) {
+  k_wait_check<<<1, 32, 0, stream>>>(polls, status);
 }
 
 // --------------------------------------------------------------- launches

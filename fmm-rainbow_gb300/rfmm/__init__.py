@@ -24,6 +24,8 @@ MOMENT_DTYPE = np.dtype([("count", "<u4"), ("sum", "<i4", 3)])
 FIELD_DTYPE = np.dtype([("a", "<f4", 4), ("j0", "<f4", 4), ("j1", "<f4", 4)])
 
 RFMM_OK = 0
+RFMM_ERR_INVALID = -1
+RFMM_ERR_TIMEOUT = -5
 STATUS = {
     0: "ok", -1: "invalid argument", -2: "CUDA runtime error", -3: "device memory exhausted",
     -4: "call out of order", -5: "kernel wait timed out", -6: "no sm_103 CUDA device",
@@ -146,6 +148,7 @@ SIGNATURES = {
     "rfmm_batch_upload": (_i, [_vp, _u32, _vp, _sz]),
     "rfmm_batch_upload_device": (_i, [_vp, _u32, _vp, _sz]),
     "rfmm_batch_upload_device_all": (_i, [_vp, _vp]),
+    "rfmm_check_wait_timeout": (_i, [_vp, _u32]),
     "rfmm_batch_seed_galaxy": (_i, [_vp, _u32]),
     "rfmm_batch_commit": (_i, [_vp]),
     "rfmm_batch_solve_fields": (_i, [_vp]),
@@ -338,6 +341,10 @@ class Solver:
         out = np.empty(count, dtype)
         _check(lib().rfmm_download(self._h, which, out.ctypes.data, out.nbytes), "rfmm_download")
         return out
+
+    def check_wait_timeout(self, polls: int = 1024) -> int:
+        """Run the bounded-wait self-check; returns the status code (ERR_TIMEOUT expected)."""
+        return lib().rfmm_check_wait_timeout(self._h, polls)
 
     def download_host_ptr(self, which: int, ptr: int, nbytes: int):
         _check(lib().rfmm_download(self._h, which, ptr, nbytes), "rfmm_download")

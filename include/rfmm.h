@@ -164,6 +164,11 @@ int rfmm_set_near_mode(rfmm_handle *h, uint32_t mode);
 
 /* Last kernel error word (0 = none) and its detail. */
 int rfmm_device_error(rfmm_handle *h, uint32_t *code, uint32_t *info);
+/* Self-check of the kernels' bounded waits: one CTA waits on an mbarrier
+ * phase nothing completes, giving up after `polls` polls (1 .. 2^22).
+ * Returns RFMM_ERR_TIMEOUT when the wait gave up as it must (the handle stays
+ * usable and its error word is untouched), RFMM_OK never in practice. */
+int rfmm_check_wait_timeout(rfmm_handle *h, uint32_t polls);
 
 /* Kernel kinds of rfmm_profile_steps. */
 enum rfmm_kernel_kind {
