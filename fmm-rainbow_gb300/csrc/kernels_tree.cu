@@ -150,7 +150,13 @@ __device__ __forceinline__ void upward_task(
     const uint32_t gsize = min(kTicketGroup, ntasks - group * kTicketGroup);
     uint32_t *t = tickets + scene * kTicketStride;
     uint32_t last = 0u;
-    if (atomic_add_acq_rel(&t[1u + group], 1u) == gsize - 1u) {  // last subtree of its group
+    // A live subtree releases its root write; an empty one has nothing to
+    // release and takes its ticket relaxed.  The group's last CTA acquires
+    // the group's releases (fence after observing the final count) before
+    // its scene ticket.
+    const uint32_t g_old = live ? atomic_add_acq_rel(&t[1u + group], 1u) : atomicAdd(&t[1u + group], 1u);
+    if (g_old == gsize - 1u) {  // last subtree of its group
+      if (!live) __threadfence();
       t[1u + group] = 0u;
       if (atomic_add_acq_rel(&t[0], 1u) == ngroups - 1u) {  // last group of the scene
         t[0] = 0u;
