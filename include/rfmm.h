@@ -257,7 +257,8 @@ typedef struct rfmm_tuning {
   uint32_t resort_interval;       /* steps between resident-order refreshes, 0 = never */
   uint32_t graph_steps;           /* steps per captured CUDA graph, 1..64 */
   uint32_t pdl;                   /* programmatic dependent launch between step kernels */
-  uint32_t m2l_compact;           /* 1: M2L lists each child's contributing slots first */
+  uint32_t m2l_compact;           /* 1 (default): M2L lists each child's contributing slots
+                                   * first; 0: every stencil slot, in chunks */
 } rfmm_tuning;
 
 int rfmm_get_tuning(rfmm_handle *h, rfmm_tuning *out);
