@@ -300,7 +300,7 @@ __global__ void __launch_bounds__(kLeafThreads) k_leaf_offsets(const SceneDesc *
 // atomic per CTA instead of one per warp: warp groups of a leaf reserve their
 // offsets in a shared-memory table of the CTA's leaves, then one thread per
 // leaf reserves the CTA's whole block of that leaf from `starts`.
-constexpr uint32_t kScatterTiles = 4u;
+constexpr uint32_t kScatterTiles = 2u;
 constexpr uint32_t kScatterSlots = 2048u;  // > bodies per CTA, so probing always ends
 
 __global__ void __launch_bounds__(256) k_leaf_scatter(const SceneDesc *__restrict__ scenes,
