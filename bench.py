@@ -512,6 +512,7 @@ def run_gpu_batched(args, w):
     # End to end: pinned host scenes in, every scene's particles out.
     pin = [torch.from_numpy(p.view(np.uint8).copy()).pin_memory() for p in ps]
     outs = [torch.empty(len(p) * 32, dtype=torch.uint8).pin_memory() for p in ps]
+    out_ptrs = [t.data_ptr() for t in outs]
     e2e_times = []
     for k in range(args.e2e_steps + 1 if args.e2e_steps > 0 else 0):
         torch.cuda.synchronize()
@@ -520,9 +521,7 @@ def run_gpu_batched(args, w):
             rfmm._check(rfmm.lib().rfmm_batch_upload(batch._h, i, t.data_ptr(), t.numel()), "upload")
         batch.commit()
         batch.step(fmm_steps)
-        for i, t in enumerate(outs):
-            rfmm._check(rfmm.lib().rfmm_batch_download(batch._h, i, rfmm.BUF_PARTICLES, t.data_ptr(),
-                                                       t.numel()), "download")
+        batch.download_all_into(rfmm.BUF_PARTICLES, out_ptrs)  # one synchronisation
         if k > 0:
             e2e_times.append(time.perf_counter() - t0)
     e2e = None

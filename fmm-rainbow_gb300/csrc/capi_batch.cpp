@@ -119,6 +119,11 @@ int rfmm_batch_download(rfmm_batch *b, uint32_t scene, int which, void *host_dst
   return b->engine->download(scene, which, host_dst, bytes, cudaMemcpyDeviceToHost);
 }
 
+int rfmm_batch_download_all(rfmm_batch *b, int which, void *const *host_dst) {
+  if (bad(b)) return RFMM_ERR_INVALID;
+  return b->engine->download_all(which, host_dst, cudaMemcpyDeviceToHost);
+}
+
 int rfmm_batch_download_device(rfmm_batch *b, uint32_t scene, int which, void *device_dst,
                                size_t bytes) {
   if (bad_scene(b, scene)) return RFMM_ERR_INVALID;

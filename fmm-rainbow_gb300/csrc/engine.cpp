@@ -868,6 +868,32 @@ int Engine::download(uint32_t scene, int which, void *dst, size_t bytes, cudaMem
   return sync();
 }
 
+int Engine::download_all(int which, void *const *dst, cudaMemcpyKind kind) {
+  if (dst == nullptr) return RFMM_ERR_INVALID;
+  for (uint32_t s = 0; s < scenes_.size(); s++)
+    if (scenes_[s].n != 0u && (dst[s] == nullptr || buffer_bytes(s, which) == 0)) return RFMM_ERR_INVALID;
+  if (which == RFMM_BUF_PARTICLES) {
+    if (!committed_) return RFMM_ERR_STATE;
+    LaunchCtx L = ctx(mcur_, lpar_, pcur_);
+    launch_unpermute(L, d_ids_[pcur_], d_part_[pcur_ ^ 1u], 0u, tiles_);  // every scene at once
+    RF_CK(cudaGetLastError());
+    launches_ += 1;
+  } else if (which == RFMM_BUF_MOMENTS) {
+    if (tree_buf_ < 0) return RFMM_ERR_STATE;
+  } else if (!solved_) {
+    return RFMM_ERR_STATE;
+  }
+  for (uint32_t s = 0; s < scenes_.size(); s++) {
+    const SceneDesc &d = scenes_[s];
+    if (d.n == 0u) continue;
+    const void *from = which == RFMM_BUF_PARTICLES ? (const void *)(d_part_[pcur_ ^ 1u] + 2ull * d.body_off)
+                       : which == RFMM_BUF_MOMENTS ? (const void *)(d_mom_[tree_buf_] + d.cell_off)
+                                                   : (const void *)(d_fields_ + 12ull * d.cell_off);
+    RF_CK(cudaMemcpyAsync(dst[s], from, buffer_bytes(s, which), kind, stream_));
+  }
+  return sync();
+}
+
 int Engine::digest(uint32_t scene, int which, uint32_t *out) {
   if (scene >= scenes_.size() || out == nullptr) return RFMM_ERR_INVALID;
   const size_t bytes = buffer_bytes(scene, which);

@@ -51,6 +51,9 @@ class Engine {
   int check_wait_timeout(uint32_t polls);
   // Every scene's bodies from one device buffer per scene (caller order).
   int upload_all_device(const void *const *src);
+  // Every scene's buffer `which` to dst[scene]: one reorder launch, one copy
+  // per scene, one synchronisation.
+  int download_all(int which, void *const *dst, cudaMemcpyKind kind);
   int seed_galaxy(uint32_t scene);
   // Sort every scene into leaf order and deposit the leaf moments.
   int commit();

@@ -148,6 +148,7 @@ SIGNATURES = {
     "rfmm_batch_upload": (_i, [_vp, _u32, _vp, _sz]),
     "rfmm_batch_upload_device": (_i, [_vp, _u32, _vp, _sz]),
     "rfmm_batch_upload_device_all": (_i, [_vp, _vp]),
+    "rfmm_batch_download_all": (_i, [_vp, _i, _vp]),
     "rfmm_check_wait_timeout": (_i, [_vp, _u32]),
     "rfmm_batch_seed_galaxy": (_i, [_vp, _u32]),
     "rfmm_batch_commit": (_i, [_vp]),
@@ -487,6 +488,12 @@ class Batch:
 
     def upload_device(self, scene, ptr, nbytes):
         _check(lib().rfmm_batch_upload_device(self._h, scene, ptr, nbytes), "rfmm_batch_upload_device")
+
+    def download_all_into(self, which, ptrs):
+        """Every scene's buffer `which` into host addresses ptrs[s], one synchronisation."""
+        assert len(ptrs) == len(self.sizes)
+        arr = (C.c_void_p * len(ptrs))(*ptrs)
+        _check(lib().rfmm_batch_download_all(self._h, which, arr), "rfmm_batch_download_all")
 
     def upload_device_all(self, ptrs):
         """Every scene at once: ptrs[s] is the device address of scene s's bodies."""

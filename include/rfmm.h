@@ -299,6 +299,10 @@ int rfmm_batch_solve_fields(rfmm_batch *b);
 int rfmm_batch_step(rfmm_batch *b, uint32_t steps);
 int rfmm_batch_sync(rfmm_batch *b);
 int rfmm_batch_download(rfmm_batch *b, uint32_t scene, int which, void *host_dst, size_t bytes);
+/* Every scene's buffer `which` at once: host_dst[s] receives scene s's
+ * buffer (sized as for rfmm_batch_download); one synchronisation in total
+ * instead of one per scene. */
+int rfmm_batch_download_all(rfmm_batch *b, int which, void *const *host_dst);
 int rfmm_batch_download_device(rfmm_batch *b, uint32_t scene, int which, void *device_dst,
                                size_t bytes);
 int rfmm_batch_digest(rfmm_batch *b, uint32_t scene, int which, uint32_t *out);

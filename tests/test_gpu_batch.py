@@ -97,3 +97,23 @@ def test_bulk_device_upload_equals_per_scene_uploads(rfmm_mod):
             out.append([b.download(i) for i in range(len(ps))])
     for i in range(len(ps)):
         assert np.array_equal(_bits(out[0][i]), _bits(out[1][i])), i
+
+
+def test_bulk_download_equals_per_scene_downloads(rfmm_mod):
+    """rfmm_batch_download_all returns, for every buffer kind, exactly what
+    per-scene downloads return."""
+    R = rfmm_mod
+    ps = _mixed_scenes()
+    prm = R.default_params(gravity=1.0, softening=1e-3, dt=5e-4)
+    with R.Batch([len(p) for p in ps], [prm] * len(ps)) as b:
+        for i, p in enumerate(ps):
+            b.upload(i, p)
+        b.commit()
+        b.step(3)
+        for which, dt in ((R.BUF_PARTICLES, R.PARTICLE_DTYPE), (R.BUF_MOMENTS, R.MOMENT_DTYPE),
+                          (R.BUF_FIELDS, R.FIELD_DTYPE)):
+            one = [b.download(i, which) for i in range(len(ps))]
+            bulk = [np.empty(len(a), dt) for a in one]
+            b.download_all_into(which, [a.ctypes.data for a in bulk])
+            for i in range(len(ps)):
+                assert np.array_equal(_bits(one[i]), _bits(bulk[i])), (which, i)
