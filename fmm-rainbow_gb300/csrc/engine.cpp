@@ -204,7 +204,13 @@ int Engine::create(const std::vector<SceneSpec> &specs, Engine **out) {
     delete E;
     return st;
   }
-  cudaError_t e = cudaStreamCreateWithFlags(&E->own_stream_, cudaStreamNonBlocking);
+  cudaError_t e = cudaHostAlloc((void **)&E->h_ctr_, sizeof(Counters), cudaHostAllocDefault);
+  if (e != cudaSuccess) {
+    E->h_ctr_ = nullptr;
+    delete E;
+    return cuda_status(e);
+  }
+  e = cudaStreamCreateWithFlags(&E->own_stream_, cudaStreamNonBlocking);
   if (e == cudaSuccess) {
     E->stream_ = E->own_stream_;
     for (auto &ev : E->ev_)
@@ -295,6 +301,7 @@ Engine::~Engine() {
   for (auto &ev : ev_)
     if (ev != nullptr) cudaEventDestroy(ev);
   for (void *p : allocations_) cudaFree(p);
+  if (h_ctr_ != nullptr) cudaFreeHost(h_ctr_);
   if (own_stream_ != nullptr) cudaStreamDestroy(own_stream_);
 }
 
@@ -797,19 +804,17 @@ int Engine::step(uint32_t steps) {
   return RFMM_OK;
 }
 
+// The error word is copied into pinned host memory behind the work already
+// queued, so one synchronisation covers both.
 int Engine::check_device_error() {
-  Counters c;
-  RF_CK(cudaMemcpyAsync(&c, d_ctr_, sizeof(Counters), cudaMemcpyDeviceToHost, stream_));
+  RF_CK(cudaMemcpyAsync(h_ctr_, d_ctr_, sizeof(Counters), cudaMemcpyDeviceToHost, stream_));
   RF_CK(cudaStreamSynchronize(stream_));
-  if (c.error == kDevErrTmaTimeout) return RFMM_ERR_TIMEOUT;
-  if (c.error != 0u) return RFMM_ERR_DEVICE;
+  if (h_ctr_->error == kDevErrTmaTimeout) return RFMM_ERR_TIMEOUT;
+  if (h_ctr_->error != 0u) return RFMM_ERR_DEVICE;
   return RFMM_OK;
 }
 
-int Engine::sync() {
-  RF_CK(cudaStreamSynchronize(stream_));
-  return check_device_error();
-}
+int Engine::sync() { return check_device_error(); }
 
 int Engine::check_wait_timeout(uint32_t polls) {
   if (polls == 0u || polls > (1u << 22)) return RFMM_ERR_INVALID;

@@ -173,6 +173,7 @@ class Engine {
   uint32_t *d_choice_ = nullptr;
   float *d_lfield_ = nullptr, *d_fields_ = nullptr;
   WorkItem *d_plist_[2] = {nullptr, nullptr};
+  Counters *h_ctr_ = nullptr;  // pinned host copy of the counters (status reads)
   Counters *d_ctr_ = nullptr;
   uint32_t *d_tickets_ = nullptr;
   CUtensorMap *d_tmaps_ = nullptr;
