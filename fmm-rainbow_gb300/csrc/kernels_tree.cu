@@ -96,8 +96,7 @@ __device__ __forceinline__ void upward_task(
   if (tid == 0) s_nitems = 0;
 
   // Leaves of this subtree: 8x8x8 block, x fastest (rows of 128 B); two per
-  // thread.  Also read: the leaves of the previous deposit (mom_next) and
-  // this subtree's upper cells in the current buffer.
+  // thread.  Also read: the subtree root in both moment buffers.
   const uint32_t dim = 1u << D;
   uint32_t seen = 0u;
   uint4 m[2];
@@ -107,7 +106,7 @@ __device__ __forceinline__ void upward_task(
     const uint32_t lx = t & 7u, ly = (t >> 3) & 7u, lz = t >> 6;
     const uint32_t leaf = level_offset_d(D) + lin3(sx * 8u + lx, sy * 8u + ly, sz * 8u + lz, dim);
     m[h] = mom[S.cell_off + leaf];
-    seen |= m[h].x | mom_next[S.cell_off + leaf].x;
+    seen |= m[h].x;
   }
   // Upper cell `tid` < 73 of the subtree: 64 of level D-1, 8 of D-2, the root.
   const uint32_t ul = tid < 64u ? D - 1u : (tid < 72u ? D - 2u : r);
@@ -115,12 +114,19 @@ __device__ __forceinline__ void upward_task(
   const uint32_t ui = tid < 64u ? tid : (tid < 72u ? tid - 64u : 0u);
   const uint32_t ucell = level_offset_d(ul) + lin3(sx * uw + ui % uw, sy * uw + (ui / uw) % uw,
                                                    sz * uw + ui / (uw * uw), 1u << ul);
-  if (tid < 73u) seen |= mom[S.cell_off + ucell].x;
-  // Empty now, empty in the previous deposit and cleared upper cells: the
-  // subtree's moments, sources and next-deposit leaves are all zero already
-  // (induction over steps; every rebuild of the moments clears the buffers),
-  // so it only takes part in the ticket count.  Bodies never sit in its
-  // leaves, so their sample cells are never read.
+  // A buffer's subtree-root count is the count of its leaves as of the last
+  // upward pass that built that buffer's tree (counts never wrap), and a
+  // zero count means zero sums and records in every cell of the subtree.
+  // The next-deposit buffer's tree was built by the previous step's upward
+  // pass from the leaves it still holds, so its root count is zero exactly
+  // when those leaves are; the current buffer's root is that of the pass
+  // before, so a zero root means its upper cells hold nothing stale.
+  if (tid == 72u) seen |= mom[S.cell_off + ucell].x | mom_next[S.cell_off + ucell].x;
+  // Empty now, empty in the previous deposit and nothing stale above the
+  // leaves: the subtree's moments, sources and next-deposit leaves are all
+  // zero already (induction over steps; every rebuild of the moments clears
+  // both buffers), so it only takes part in the ticket count.  Bodies never
+  // sit in its leaves, so their sample cells are never read.
   const bool live = __syncthreads_or(seen != 0u);
   if (live) {
     s0[tid] = m[0];
