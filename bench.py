@@ -43,30 +43,7 @@ for _p in (REPO, PKG):
     if _p not in sys.path:
         sys.path.insert(0, _p)
 
-WORKLOADS = {
-    # The reference's default preset (the metric's headline configuration).
-    "plummer_1m": dict(kind="plummer", n=1 << 20, seed=2, fmm_steps=60, dt=5e-4, eps=1e-3, G=1.0,
-                       desc="Plummer sphere a=0.1 at (0.5,0.5,0.5), r<0.5, N=1,048,576, "
-                            "G=1, eps=1e-3, 60 steps dt=5e-4, Plummer-DF velocities"),
-    # The reference's CPU-runnable case.
-    "uniform_64k": dict(kind="uniform", n=65536, seed=1, fmm_steps=1, dt=1e-3, eps=1e-3, G=1.0,
-                        desc="uniform [0,1)^3, N=65,536, G=1, eps=1e-3, v=0, 1 step dt=1e-3"),
-    # The budget maximum.
-    "clusters_5m": dict(kind="clusters", n=5242880, seed=3, fmm_steps=60, dt=5e-4, eps=5e-4, G=1.0,
-                        desc="8 Plummer clusters a~logU[0.02,0.1], centres U[0.2,0.8]^3, "
-                             "N=5,242,880, eps=5e-4, bulk sigma 0.05, 60 steps dt=5e-4"),
-    # Served form: Poisson request arrivals, continuous batching.
-    "served": dict(kind="served", n_min=16384, n_max=2097152, steps_max=60, seed=5, dt=5e-4,
-                   eps=1e-3, G=1.0, rates=[50, 200, 1000, 2000], requests=300, slots=128,
-                   budget=150 << 30, fmm_steps=None,
-                   desc="requests with N log-uniform [16384, 2097152] (uniform / Plummer / "
-                        "4-cluster), steps U[1,60], dt=5e-4, eps=1e-3, Poisson arrivals"),
-    # Batched form: many scenes per launch, against the same scenes back to back.
-    "batched_256": dict(kind="batched", scenes=256, n_min=4096, n_max=262144, seed=4,
-                        fmm_steps=60, dt=5e-4, eps=1e-3, G=1.0,
-                        desc="256 scenes, N log-uniform [4096, 262144], half uniform cube, "
-                             "half Plummer a=0.1, G=1, eps=1e-3, 60 steps dt=5e-4"),
-}
+from rfmm import workloads  # noqa: E402  (numpy only; the solver library loads later)
 
 PEAKS_FILE = os.path.join(REPO, "MEASURED_PEAKS.json")
 TRAFFIC_FILE = os.path.join(REPO, "profiles", "ncu_traffic.json")
@@ -79,7 +56,7 @@ def parse_args():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--workload", default="plummer_1m", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="plummer_1m", choices=sorted(workloads.WORKLOADS))
     ap.add_argument("--impl", default="fmm", choices=["fmm", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=8)
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
@@ -100,29 +77,18 @@ def dist_env():
 
 
 def make_scene(w):
-    from rfmm import scenes
-    return scenes.make(w["kind"], w["n"], w["seed"])
+    from rfmm import workloads
+    return workloads.scene(w)
 
 
 def batch_scenes(w):
-    """The batched workload's scenes: seeded sizes, alternating uniform / Plummer."""
-    import numpy as np
-    from rfmm import scenes
-    rng = np.random.default_rng(w["seed"])
-    sizes = np.exp(rng.uniform(np.log(w["n_min"]), np.log(w["n_max"]), w["scenes"])).astype(int)
-    return [scenes.make("uniform" if i % 2 == 0 else "plummer", int(n), 1000 + i)
-            for i, n in enumerate(sizes)]
+    from rfmm import workloads
+    return workloads.batch_scenes(w)
 
 
 def roofline_bytes_integrate(n, cells, depth):
-    """Algorithmic bytes of one fused integrate launch.
-
-    64 B per body (32 B particle in, 32 B out), 64 B per tree cell (48 B field
-    + 16 B moment gathered once) and 16 B per leaf cell (the next step's leaf
-    deposit written once).
-    """
-    leaves = 8 ** depth
-    return 64 * n + 64 * cells + 16 * leaves
+    from rfmm import workloads
+    return workloads.roofline_bytes_integrate(n, cells, depth)
 
 
 def clocks_sampler(gpu_index):
@@ -650,7 +616,7 @@ def run_gpu_served(args, w):
 
 def main():
     args = parse_args()
-    w = WORKLOADS[args.workload]
+    w = workloads.WORKLOADS[args.workload]
     if args.impl == "reference":
         return run_reference(args, w)
     if w["kind"] == "batched":

@@ -18,12 +18,16 @@
 //     threads without ordering) race on it and give wrong results;
 //   * the first call on a device resolves the array's device address with
 //     cudaGetSymbolAddress and encodes the TMA tensor maps; make that first
-//     call before any stream capture.
+//     call before any stream capture;
+//   * kernel-side errors (a bounded TMA wait that gave up, a work list over
+//     its capacity) land in the array's status word, which the next call
+//     clears: after synchronising, read it with rfmm_noalloc_device_error.
 #include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstddef>
 #include <cstdint>
+#include <atomic>
 #include <cstring>
 #include <mutex>
 
@@ -72,8 +76,11 @@ using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_
                                    const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
                                    CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
+// `ready` is published with release order after the other fields are set,
+// and read with acquire order before they are used, so a thread that sees it
+// true also sees the set-up; set-up itself runs under g_setup_mutex.
 struct DeviceState {
-  bool ready = false;
+  std::atomic<bool> ready{false};
   Scratch *scratch = nullptr;  // device address of g_scratch on this device
   int sms = 0;
   uint32_t body_ctas = 0;
@@ -93,7 +100,7 @@ int cuda_rc(cudaError_t e) {
 // kernel attributes and the tensor maps over the array's source records.
 int setup_device(int dev, DeviceState &st) {
   std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (st.ready) return RFMM_OK;
+  if (st.ready.load(std::memory_order_relaxed)) return RFMM_OK;
   cudaDeviceProp prop;
   cudaError_t e = cudaGetDeviceProperties(&prop, dev);
   if (e != cudaSuccess) return cuda_rc(e);
@@ -129,7 +136,22 @@ int setup_device(int dev, DeviceState &st) {
   st.scratch = S;
   st.sms = prop.multiProcessorCount;
   st.body_ctas = (uint32_t)st.sms * body_ctas_per_sm();
-  st.ready = true;
+  st.ready.store(true, std::memory_order_release);
+  return RFMM_OK;
+}
+
+// The current device's state, set up on first use.
+int device_state(DeviceState **out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_rc(e);
+  if (dev < 0 || dev >= kMaxDevices) return RFMM_ERR_NO_DEVICE;
+  DeviceState &st = g_state[dev];
+  if (!st.ready.load(std::memory_order_acquire)) {
+    const int rc = setup_device(dev, st);
+    if (rc != RFMM_OK) return rc;
+  }
+  *out = &st;
   return RFMM_OK;
 }
 
@@ -155,16 +177,14 @@ extern "C" int rfmm_solve_fields_noalloc(const void *device_particles, uint32_t 
   const uint32_t depth = p.depth ? p.depth : depth_for_particles(n);
   if (depth < 4u || depth > kMaxDepth || !(p.fixed_point_scale >= 0.0f)) return RFMM_ERR_INVALID;
 
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return cuda_rc(e);
-  if (dev < 0 || dev >= kMaxDevices) return RFMM_ERR_NO_DEVICE;
-  DeviceState &st = g_state[dev];
-  if (!st.ready) {
-    const int rc = setup_device(dev, st);
+  DeviceState *stp = nullptr;
+  {
+    const int rc = device_state(&stp);
     if (rc != RFMM_OK) return rc;
   }
+  const DeviceState &st = *stp;
   Scratch *S = st.scratch;
+  cudaError_t e = cudaSuccess;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
 
   SceneDesc d{};
@@ -238,4 +258,22 @@ extern "C" int rfmm_solve_fields_noalloc(const void *device_particles, uint32_t 
   launch_m2l(L, 0u);
   launch_l2l_near(L, 0u);
   return cuda_rc(cudaGetLastError());
+}
+
+extern "C" int rfmm_noalloc_device_error(uint32_t *code, uint32_t *info, void *stream) {
+  using namespace rfmm;
+  DeviceState *st = nullptr;
+  const int rc = device_state(&st);
+  if (rc != RFMM_OK) return rc;
+  // Read behind the work queued on `stream`; the copy goes to a local and
+  // the stream is synchronised before it is read.
+  Counters c{};
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaMemcpyAsync(&c, &st->scratch->ctr, sizeof(Counters), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_rc(e);
+  if (code != nullptr) *code = c.error;
+  if (info != nullptr) *info = c.error_info;
+  if (c.error == kDevErrTmaTimeout) return RFMM_ERR_TIMEOUT;
+  return c.error != 0u ? RFMM_ERR_DEVICE : RFMM_OK;
 }

@@ -140,6 +140,7 @@ SIGNATURES = {
     "rfmm_profile_steps": (_i, [_vp, _u32, C.POINTER(_f32), C.POINTER(_u32)]),
     "rfmm_launch_count": (_i, [_vp, C.POINTER(C.c_uint64)]),
     "rfmm_solve_fields_noalloc": (_i, [_vp, _u32, _P, _vp, _vp, _vp]),
+    "rfmm_noalloc_device_error": (_i, [C.POINTER(_u32), C.POINTER(_u32), _vp]),
     "rfmm_batch_create": (_i, [_u32, C.POINTER(_u32), _P, C.POINTER(_vp)]),
     "rfmm_batch_destroy": (_i, [_vp]),
     "rfmm_batch_set_stream": (_i, [_vp, _vp]),
@@ -265,6 +266,14 @@ def solve_fields_noalloc(particles_ptr: int, n: int, params: Params | None, mome
     _check(lib().rfmm_solve_fields_noalloc(particles_ptr, n, C.byref(params) if params else None,
                                            moments_ptr, fields_ptr, stream_ptr or None),
            "rfmm_solve_fields_noalloc")
+
+
+def noalloc_device_error(stream_ptr: int | None = None):
+    """(status, code, info) of the last allocation-free solve on this device,
+    read after the work queued on the stream."""
+    code, info = C.c_uint32(), C.c_uint32()
+    st = lib().rfmm_noalloc_device_error(C.byref(code), C.byref(info), stream_ptr or None)
+    return st, code.value, info.value
 
 
 class Solver:

@@ -376,9 +376,24 @@ int rfmm_server_get_stats(rfmm_server *server, rfmm_server_stats *out);
  * returns RFMM_ERR_INVALID.  Every call reuses that one array: calls that
  * overlap on the GPU race on it.  The first call on a device does a one-time
  * set-up (resolving the array's device address, encoding TMA descriptors);
- * make that first call before any stream capture. */
+ * make that first call before any stream capture.
+ *
+ * The call returns once its work is enqueued, so a kernel-side error (a
+ * bounded TMA wait that gave up, a work list over its capacity) cannot be
+ * its return value: it is left in the array's status word, which the next
+ * call clears.  Read it with rfmm_noalloc_device_error after the call's work
+ * and before the next call. */
 int rfmm_solve_fields_noalloc(const void *device_particles, uint32_t n, const rfmm_params *params,
                               void *device_moments, void *device_fields, void *stream);
+
+/* Status word of the last rfmm_solve_fields_noalloc call on the current
+ * device (no counterpart in the reference; companion of the entry point
+ * above).  Waits for the work queued on `stream` (a cudaStream_t, NULL = the
+ * default stream), then copies the word: *code 0 = no error, 1 = a bounded
+ * TMA wait gave up, 2 = a work list overflowed; *info is its detail.
+ * Returns RFMM_OK, RFMM_ERR_TIMEOUT (code 1) or RFMM_ERR_DEVICE (other
+ * codes).  Allocates nothing. */
+int rfmm_noalloc_device_error(uint32_t *code, uint32_t *info, void *stream);
 
 #ifdef __cplusplus
 }

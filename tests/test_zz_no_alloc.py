@@ -46,6 +46,8 @@ def test_noalloc_matches_handle_two_calls(rfmm_mod, calls):
         torch.cuda.synchronize()
         R.solve_fields_noalloc(dev_p.data_ptr(), n, params, mom.data_ptr(), fld.data_ptr(),
                                stream.cuda_stream)
+        # The kernels' status word, read behind the call's work: no error.
+        assert R.noalloc_device_error(stream.cuda_stream) == (R.RFMM_OK, 0, 0)
         stream.synchronize()
         ref_mom, ref_fld = _handle_solve(R, scene, params)
         got_mom, got_fld = mom.cpu().numpy(), fld.cpu().numpy()
