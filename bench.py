@@ -7,7 +7,9 @@ A bench step is one full solve of the workload: the scene is reset from a
 device-resident pristine copy (upload + leaf sort + deposit) and advanced
 `fmm_steps` leapfrog steps.  The default workload is the reference's default
 preset, a 1,048,576-body Plummer sphere (a = 0.1, centred in the unit box,
-truncated at r = 0.5, G = 1, eps = 1e-3, dt = 5e-4) run for 60 steps.
+truncated at r = 0.5, G = 1, eps = 1e-3, dt = 5e-4) run for 60 steps; its line
+also carries the batched form (256 scenes, one set of launches per step)
+measured against the same scenes solved back to back through plain handles.
 
 Timing: W untimed warm-up steps, then exactly K timed steps, each bracketed by
 CUDA events on the solver's stream; L2 is flushed (512 MiB write) between
@@ -16,16 +18,24 @@ over ranks.  N GPUs run N independent replicas (one process per GPU; the
 plain solve does not shard), so `value` is the sum of all replicas' work over
 the slowest replica's time.
 
+Per-phase times come from a second timed pass with the in-graph timeline on
+(rfmm_set_timeline): every step kernel stamps, with %globaltimer, its first
+CTA's begin (after its dependency wait) and its last CTA's end inside the
+same CUDA graphs and programmatic dependent launches that produce `value`.
+Each phase's algorithmic bytes (flops for M2L) are counted exactly from the
+tree the run ends on (rfmm/roofline.py).
+
 The JSON line adds: `e2e` (the same metric through the C ABI from pinned host
 buffers, host<->device copies inside the timed region), `roofline` for the
-dominant kernel (integrate), `cpu_baseline` (the CPU oracle on the host cores,
-rank 0 only), `clocks` sampled during the timed region, `gpu_launches`, and
-per-kernel times.
+dominant kernel (integrate) with `phases` for every step kernel,
+`cpu_baseline` (the CPU oracle on the host cores, rank 0 only), `clocks`
+sampled during the timed region and `gpu_launches`.
 
 `--impl reference` times the reference algorithm's CPU implementation (the
 oracle port: the reference's Rust/WGSL harness needs a Vulkan adapter and a
-Rust toolchain, neither of which exists here) on the host cores, one FMM step
-of the same workload per bench step.
+Rust toolchain, neither of which exists here) on all host cores, with the
+same protocol as `cpu_baseline`: each bench step resets the scene and runs
+the workload's FMM steps.
 """
 from __future__ import annotations
 
@@ -49,23 +59,30 @@ PEAKS_FILE = os.path.join(REPO, "MEASURED_PEAKS.json")
 TRAFFIC_FILE = os.path.join(REPO, "profiles", "ncu_traffic.json")
 FALLBACK_HBM_GBS = 6800.0
 P2P_MAX_BODIES = 1 << 18
+REFERENCE_BUDGET_S = 150.0  # the reference arm's whole run
 
 
 def parse_args():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--workload", default="plummer_1m", choices=sorted(workloads.WORKLOADS))
     ap.add_argument("--impl", default="fmm", choices=["fmm", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=8)
-    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="plain workload only")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="timed steps only (no timeline, fast-variant, accuracy or render pass): "
+                         "the command profilers capture")
     ap.add_argument("--requests", type=int, default=0, help="served: requests per rate point")
     ap.add_argument("--rates", type=float, nargs="*", default=None, help="served: arrival rates /s")
     ap.add_argument("--near", default="reference", choices=["reference", "p2p"],
                     help="near field: the reference's cell monopoles, or exact pair sums")
+    ap.add_argument("--float", default="exact", choices=["exact", "fast"],
+                    help="float variant of the headline run (exact: the oracle's contract)")
     return ap.parse_args()
 
 
@@ -76,19 +93,17 @@ def dist_env():
     return rank, world, local
 
 
-def make_scene(w):
-    from rfmm import workloads
-    return workloads.scene(w)
-
-
-def batch_scenes(w):
-    from rfmm import workloads
-    return workloads.batch_scenes(w)
-
-
-def roofline_bytes_integrate(n, cells, depth):
-    from rfmm import workloads
-    return workloads.roofline_bytes_integrate(n, cells, depth)
+def host_cpu():
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return {"nproc": os.cpu_count(), "model": model}
 
 
 def clocks_sampler(gpu_index):
@@ -149,71 +164,98 @@ def traffic_for(workload):
         return None
 
 
-def cpu_baseline(w, seconds, near="reference"):
-    """The CPU oracle (the reference algorithm restated in C, OpenMP) on this
-    host: all host threads, then one thread on a shorter sample."""
-    from oracle import oracle as O
-    scene = make_scene(w)
+# ---------------------------------------------------------------- CPU oracle
 
-    def sample(threads, budget):
-        cores = O.set_threads(threads)
-        st = O.OracleState(scene, O.make_params(w["n"], gravity=w["G"], softening=w["eps"], dt=w["dt"],
-                                                near_mode=1 if near == "p2p" else 0))
-        done, t0 = 0, time.perf_counter()
-        while True:
-            st.step(1)
-            done += 1
-            el = time.perf_counter() - t0
-            if el >= budget or done >= w["fmm_steps"]:
-                break
-        return w["n"] * done / el, cores, done, el
+class CpuRuns:
+    """The CPU oracle (the reference algorithm restated in C, OpenMP) on the
+    workload's scenes.  One run = reset every scene to its starting state and
+    advance it `steps` FMM steps, the same unit the GPU bench step times."""
 
-    value, cores, done, el = sample(os.cpu_count() or 1, seconds)
-    v1, _, d1, e1 = sample(1, seconds / 3.0)
+    def __init__(self, w, near="reference"):
+        from oracle import oracle as O
+        self.O = O
+        if w["kind"] == "batched":
+            self.scenes = workloads.batch_scenes(w)
+        else:
+            self.scenes = [workloads.scene(w)]
+        self.params = [O.make_params(len(p), gravity=w["G"], softening=w["eps"], dt=w["dt"],
+                                     near_mode=1 if near == "p2p" else 0) for p in self.scenes]
+        self.bodies = sum(len(p) for p in self.scenes)
+
+    def run(self, steps):
+        states = [self.O.OracleState(p, prm) for p, prm in zip(self.scenes, self.params)]
+        t0 = time.perf_counter()
+        for st in states:
+            st.step(steps)
+        return time.perf_counter() - t0
+
+
+def cpu_baseline(w, seconds, near="reference", warmup=1):
+    """All host threads: whole runs of the workload until `seconds` have
+    passed (at least one); then one thread on a shorter sample."""
+    runs = CpuRuns(w, near)
+    O = runs.O
+    cores = O.set_threads(os.cpu_count() or 1)
+    steps = w["fmm_steps"]
+    for _ in range(warmup):
+        runs.run(steps)
+    el, done = 0.0, 0
+    while el < seconds or done == 0:
+        el += runs.run(steps)
+        done += 1
+    value = runs.bodies * steps * done / el
+    O.set_threads(1)
+    s1 = max(1, min(steps, 8))
+    e1 = runs.run(s1)
     O.set_threads(os.cpu_count() or 1)
     return {"value": value, "unit": "body-steps/s", "cores": cores, "kind": "port",
-            "sample": "%d FMM step(s) of the same workload (%d bodies, %s near field) on %d host "
-                      "threads, %.1f s" % (done, w["n"], near, cores, el),
-            "single_thread": {"value": v1, "sample": "%d step(s), %.1f s" % (d1, e1)}}
+            "sample": "%d run(s) of %d FMM steps of the same workload (%d bodies, %s near field) "
+                      "after %d warm-up run(s), %d host threads, %.1f s"
+                      % (done, steps, runs.bodies, near, warmup, cores, el),
+            "single_thread": {"value": runs.bodies * s1 / e1,
+                              "sample": "%d FMM step(s) from the starting state, %.1f s" % (s1, e1)},
+            "host": host_cpu()}
 
 
 def run_reference(args, w):
+    """The reference arm: the CPU oracle on the same config, same protocol
+    as cpu_baseline (each bench step resets the scene and runs the workload's
+    FMM steps); a bounded sample of those steps when the whole run would
+    exceed REFERENCE_BUDGET_S."""
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    from oracle import oracle as O
+    if w["kind"] == "served":
+        print(json.dumps({"impl": "reference", "unavailable": "the reference has no request server "
+                          "(its only loop is native/main.rs:522-534); the served workload has no "
+                          "CPU counterpart"}), flush=True)
+        return 0
+    runs = CpuRuns(w, args.near)
+    O = runs.O
     cores = O.set_threads(os.cpu_count() or 1)
-    if w["kind"] == "batched":
-        ps = batch_scenes(w)
-        states = [O.OracleState(p, O.make_params(len(p), gravity=w["G"], softening=w["eps"],
-                                                 dt=w["dt"])) for p in ps]
-        bodies = sum(len(p) for p in ps)
-    else:
-        states = [O.OracleState(make_scene(w), O.make_params(w["n"], gravity=w["G"],
-                                                             softening=w["eps"], dt=w["dt"]))]
-        bodies = w["n"]
+    steps = w["fmm_steps"]
+    probe = runs.run(1)  # one FMM step: sizes the sample
+    est = probe * steps * (args.warmup + args.steps)
+    if est > REFERENCE_BUDGET_S:
+        steps = max(1, int(steps * REFERENCE_BUDGET_S / est))
     for _ in range(args.warmup):
-        for st in states:
-            st.step(1)
-    times = []
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        for st in states:
-            st.step(1)
-        times.append(time.perf_counter() - t0)
+        runs.run(steps)
+    times = [runs.run(steps) for _ in range(args.steps)]
     total = sum(times)
-    value = bodies * args.steps / total
+    value = runs.bodies * steps * args.steps / total
     line = {
         "impl": "reference", "metric": "body-steps/s", "value": value, "unit": "body-steps/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded): " + w["desc"],
-        "config": {"workload": args.workload, "bodies": bodies, "fmm_steps_per_bench_step": 1,
+        "config": {"workload": args.workload, "bodies": runs.bodies,
+                   "fmm_steps_per_bench_step": steps,
                    "implementation": "CPU oracle port of the reference compute passes "
                                      "(reference wgpu/Vulkan harness unavailable on this box)"},
         "cpu_baseline": {"value": value, "unit": "body-steps/s", "cores": cores, "kind": "port",
-                         "sample": "one FMM step of %d bodies per bench step, %d host threads"
-                                   % (bodies, cores)},
+                         "sample": "%d bench steps of %d FMM steps (scene reset each), %d host "
+                                   "threads" % (args.steps, steps, cores),
+                         "host": host_cpu()},
         "e2e": {"value": value, "unit": "body-steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -221,34 +263,106 @@ def run_reference(args, w):
     return 0
 
 
-def run_gpu(args, w):
-    import numpy as np
-    import torch
+# ---------------------------------------------------------------- GPU helpers
 
-    rank, world, local = dist_env()
-    torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    from rfmm import build as pkg_build
-    pkg_build.build()
-    import rfmm
+def timed_events(torch, stream, flush, fn, k):
+    """k calls of fn, each bracketed by CUDA events on `stream`, L2 flushed
+    before each (outside the events); returns the summed device ms."""
+    st = [torch.cuda.Event(enable_timing=True) for _ in range(k)]
+    en = [torch.cuda.Event(enable_timing=True) for _ in range(k)]
+    for j in range(k):
+        flush.zero_()
+        st[j].record(stream)
+        fn()
+        en[j].record(stream)
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in zip(st, en))
+
+
+def timeline_pass(torch, stream, flush, handle, fn, k, fmm_steps, ms_per_step):
+    """A second timed pass with the in-graph timeline on; returns its summary."""
+    handle.set_timeline(True)
+    fn()  # captures the stamped graphs
+    torch.cuda.synchronize()
+    ms = timed_events(torch, stream, flush, fn, k) / k
+    tl = handle.timeline()
+    handle.set_timeline(False)
+    steps = max(tl["steps"], 1)
+    per_step = {kk: {"busy_us": 1e3 * v["busy_ms"] / steps, "gap_us": 1e3 * v["gap_ms"] / steps}
+                for kk, v in tl["kinds"].items()}
+    return tl, {
+        "steps_recorded": tl["steps"],
+        "fmm_step_span_us": 1e3 * tl["span_ms"] / steps,
+        "per_fmm_step": per_step,
+        "busy_sum_us": sum(v["busy_us"] for v in per_step.values()),
+        "gap_sum_us": sum(v["gap_us"] for v in per_step.values()),
+        "bench_ms_per_step_with_timeline": ms,
+        "bench_ms_per_step_without": ms_per_step,
+        "fmm_step_us_from_bench": 1e3 * ms_per_step / fmm_steps,
+        "timer": "%globaltimer stamps inside the graphs: first CTA begin (after its dependency "
+                 "wait) to last CTA end, per launch; each graph's last run",
+    }
+
+
+def dominant_roofline(phases, timeline, work, workload, peak, peak_kind, event_ms):
+    k = timeline["kinds"]["integrate"]
+    ms = k["busy_ms"] / max(k["launches"], 1)
+    alg = work["integrate"]["bytes"]
+    achieved = alg / (ms * 1e-3) / 1e9
+    return {"kernel": "k_integrate", "bound": "hbm", "achieved": achieved, "peak": peak,
+            "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+            "algorithmic_bytes_per_launch": alg, "avg_launch_ms": ms,
+            "avg_launch_timer": "in-graph %globaltimer (timeline pass)",
+            "event_avg_launch_ms": event_ms,
+            "event_timer": "CUDA events around direct (non-graph) launches of the same kernel",
+            "traffic": traffic_for(workload), "phases": phases, "phase_work": work}
+
+
+def float_variant_pass(args, torch, rfmm, stream, flush, handle, fn, body_steps, fmm_steps, peak,
+                       peak_kind, fp32, clocks, work_fn):
+    """The same bench steps with the fast float variant: value, per-phase
+    rates from its own timeline pass, dominant-kernel roofline."""
+    from rfmm import replicas, roofline
+    handle.set_float_mode(rfmm.FLOAT_FAST)
+    for _ in range(max(2, args.warmup)):
+        fn()
+    torch.cuda.synchronize()
+    ms = timed_events(torch, stream, flush, fn, args.steps)
+    value, _, slowest_s = replicas.reduce_throughput(body_steps * args.steps, ms * 1e-3)
+    ms_per_step = slowest_s * 1e3 / args.steps
+    tl, tl_summary = timeline_pass(torch, stream, flush, handle, fn, min(args.steps, 5), fmm_steps,
+                                   ms_per_step)
+    work = work_fn()
+    phases = roofline.phases_roofline(work, tl, peak, fp32, peak_kind)
+    k = tl["kinds"]["integrate"]
+    ims = k["busy_ms"] / max(k["launches"], 1)
+    ach = work["integrate"]["bytes"] / (ims * 1e-3) / 1e9
+    return {"value": value, "unit": "body-steps/s", "ms_per_step": ms_per_step,
+            "float_mode": "fast (contraction, approximate div/sqrt, hardware rsqrt)",
+            "parity": "integer work bit-exact; fields rel rms <= 1e-5, accelerations rel rms "
+                      "<= 1e-4 against the oracle (tests/test_gpu_fast_mode.py)",
+            "roofline": {"kernel": "k_integrate", "bound": "hbm", "achieved": ach, "peak": peak,
+                         "unit": "GB/s", "frac": ach / peak, "avg_launch_ms": ims,
+                         "phases": phases},
+            "timeline": tl_summary}
+
+
+def run_gpu_plain(args, w, torch, rfmm, stream, flush, rank, world, local):
+    import numpy as np
+    from rfmm import replicas, roofline
 
     n, fmm_steps = w["n"], w["fmm_steps"]
     if args.near == "p2p" and n > P2P_MAX_BODIES:
-        raise SystemExit("--near p2p: at most %d bodies (the depth-6 cap leaves Plummer cores with "
-                         "thousands of bodies per leaf, ~1e5 pairs per body)" % P2P_MAX_BODIES)
-    scene = make_scene(w)
+        raise SystemExit("--near p2p: at most %d bodies" % P2P_MAX_BODIES)
+    scene = workloads.scene(w)
     params = rfmm.default_params(gravity=w["G"], softening=w["eps"], dt=w["dt"])
-    # A real (non-default) stream shared by torch's events/flush and the solver.
-    stream = torch.cuda.Stream()
-    torch.cuda.set_stream(stream)
     solver = rfmm.Solver(n, params)
     solver.set_stream(stream.cuda_stream)
     if args.near == "p2p":
         solver.set_near_mode(rfmm.NEAR_P2P)
+    if args.float == "fast":
+        solver.set_float_mode(rfmm.FLOAT_FAST)
     pristine = torch.from_numpy(scene.view(np.uint8).copy()).cuda()
-    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
 
     def bench_step():
         solver.upload_device(pristine.data_ptr(), pristine.numel())
@@ -267,38 +381,51 @@ def run_gpu(args, w):
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     clk = clocks_sampler(local)
     time.sleep(0.3)
     barrier()
     l0 = solver.launch_count()
-    for k in range(args.steps):
-        flush.zero_()
-        starts[k].record(stream)
-        bench_step()
-        ends[k].record(stream)
+    local_ms = timed_events(torch, stream, flush, bench_step, args.steps)
     barrier()
     launches = solver.launch_count() - l0
     clocks = clocks_summary(clk)
-    local_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
-    from rfmm import replicas
     value, _, slowest_s = replicas.reduce_throughput(n * fmm_steps * args.steps, local_ms * 1e-3)
-    total_ms = slowest_s * 1e3
+    ms_per_step = slowest_s * 1e3 / args.steps
     solver.sync()
+    if args.no_extras:
+        solver.close()
+        return {"metric": "body-steps/s", "value": value, "unit": "body-steps/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+                "config": {"workload": args.workload, "bodies": n,
+                           "fmm_steps_per_bench_step": fmm_steps, "extras": "skipped"},
+                "clocks": clocks, "gpu_launches": launches}
 
-    # Per-kernel device times over the same workload (event pair around every launch).
+    # Per-phase times inside the graphs, and the work of the tree the run ends on.
+    tl, tl_summary = timeline_pass(torch, stream, flush, solver, bench_step, min(args.steps, 5),
+                                   fmm_steps, ms_per_step)
+    tw = roofline.tree_work(solver.moments(), solver.depth)
+    work = roofline.phase_work(n, tw)
+    peak, peak_kind = hbm_peak()
+    sm_mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0
+    fp32 = roofline.fp32_peak_tflops(torch.cuda.get_device_properties(local).multi_processor_count,
+                                     sm_mhz)
+    phases = roofline.phases_roofline(work, tl, peak, fp32, peak_kind)
+    # The same kernels launched directly between CUDA events (no graph, no PDL).
     solver.upload_device(pristine.data_ptr(), pristine.numel())
     prof = solver.profile_steps(fmm_steps)
-    integ_ms, integ_n = prof["integrate"]
-    alg_bytes = roofline_bytes_integrate(n, solver.cells, solver.depth)
-    peak, peak_kind = hbm_peak()
-    achieved = alg_bytes / (integ_ms / integ_n * 1e-3) / 1e9
-    roofline = {"kernel": "k_integrate", "bound": "hbm", "achieved": achieved, "peak": peak,
-                "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                "algorithmic_bytes_per_launch": alg_bytes,
-                "avg_launch_ms": integ_ms / integ_n, "traffic": traffic_for(args.workload)}
-    kernel_ms = {k: (v[0] / v[1] if v[1] else 0.0) for k, v in prof.items()}
+    event_ms = {k: (v[0] / v[1] if v[1] else 0.0) for k, v in prof.items()}
+    roof = dominant_roofline(phases, tl, work, args.workload, peak, peak_kind, event_ms["integrate"])
+    roof["tree"] = tw
+
+    # The fast float variant on the same workload, same protocol.
+    fast = None
+    if args.near == "reference" and args.float == "exact":
+        fast = float_variant_pass(args, torch, rfmm, stream, flush, solver, bench_step,
+                                  n * fmm_steps, fmm_steps, peak, peak_kind, fp32, clocks,
+                                  lambda: roofline.phase_work(
+                                      n, roofline.tree_work(solver.moments(), solver.depth)))
+        fast["force_rms_rel"], fast["force_max_rel"] = solver.force_error(4096, 1)
+        solver.set_float_mode(rfmm.FLOAT_EXACT)
 
     # End to end through the C ABI with host buffers: pinned input upload
     # (H2D + leaf sort), the solve, pinned download of the result (D2H).
@@ -318,7 +445,7 @@ def run_gpu(args, w):
         e2e_s = statistics.median(e2e_times)  # host wall clock: the median resists scheduler jitter
         e2e = {"value": world * n * fmm_steps / e2e_s, "unit": "body-steps/s",
                "h2d_bytes_per_step": n * 32, "d2h_bytes_per_step": n * 32,
-               "ms_per_step": 1e3 * e2e_s, "timer": "host wall clock"}
+               "ms_per_step": 1e3 * e2e_s, "timer": "host wall clock (median of %d)" % len(e2e_times)}
 
     # Accuracy of the state the bench ends on (outside every timed region):
     # FP64 direct-sum force error on a seeded target sample, FP64 energy.
@@ -351,78 +478,46 @@ def run_gpu(args, w):
         torch.cuda.synchronize()
         render = {"canvas": [1920, 1080], "points": n, "frame_ms": r0.elapsed_time(r1) / frames,
                   "kernels_per_frame": 5, "note": "includes the host round trip of each call"}
+    solver.close()
 
-    line = {
+    return {
         "metric": "body-steps/s", "value": value, "unit": "body-steps/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded, numpy PCG64): " + w["desc"],
         "config": {"workload": args.workload, "form": "plain single-scene solve",
-                   "near_field": args.near,
-                   "bodies": n, "fmm_steps_per_bench_step": fmm_steps, "depth": solver.depth,
-                   "cells": solver.cells, "fixed_point_scale": solver.scale,
+                   "near_field": args.near, "float_mode": args.float,
+                   "bodies": n, "fmm_steps_per_bench_step": fmm_steps, "depth": tw["depth"],
+                   "cells": tw["cells"], "fixed_point_scale": rfmm.plan_unclamped(n)[2],
                    "l2": "flushed between timed steps (512 MiB write outside the events)",
                    "parallelism": "replicas x%d" % world},
-        "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
-        "kernel_avg_ms": kernel_ms, "tuning": tuning.as_dict(), "accuracy": accuracy,
-        "render": render,
+        "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "roofline": roof,
+        "timeline": tl_summary, "kernel_event_avg_ms": event_ms, "tuning": tuning.as_dict(),
+        "accuracy": accuracy, "render": render, "fast_float": fast,
     }
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds, args.near)
-    if rank == 0:
-        print(json.dumps(line), flush=True)
-    solver.close()
-    if world > 1:
-        torch.distributed.destroy_process_group()
-    return 0
 
 
-def run_gpu_batched(args, w):
-    """Batched form vs the same scenes solved back to back through plain handles."""
+def run_gpu_batched(args, w, torch, rfmm, stream, flush, rank, world, local):
+    """Batched form vs the same scenes back to back through plain handles."""
     import numpy as np
-    import torch
+    from rfmm import replicas, roofline
 
-    rank, world, local = dist_env()
-    torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    from rfmm import build as pkg_build
-    pkg_build.build()
-    import rfmm
-    from rfmm import replicas
-
-    all_scenes = batch_scenes(w)
+    all_scenes = workloads.batch_scenes(w)
     mine = replicas.shard_scenes([len(p) for p in all_scenes], world)[rank]
     ps = [all_scenes[i] for i in mine]
     sizes = [len(p) for p in ps]
     bodies = sum(sizes)
     fmm_steps = w["fmm_steps"]
     params = rfmm.default_params(gravity=w["G"], softening=w["eps"], dt=w["dt"])
-    stream = torch.cuda.Stream()
-    torch.cuda.set_stream(stream)
     dev = [torch.from_numpy(p.view(np.uint8).copy()).cuda() for p in ps]
-    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
     batch = rfmm.Batch(sizes, [params] * len(ps))
     batch.set_stream(stream.cuda_stream)
-
     dev_ptrs = [d.data_ptr() for d in dev]
 
     def batched_step():
         batch.upload_device_all(dev_ptrs)  # one copy launch for all scenes
         batch.commit()
         batch.step(fmm_steps)
-
-    def timed(fn, k):
-        st = [torch.cuda.Event(enable_timing=True) for _ in range(k)]
-        en = [torch.cuda.Event(enable_timing=True) for _ in range(k)]
-        for j in range(k):
-            flush.zero_()
-            st[j].record(stream)
-            fn()
-            en[j].record(stream)
-        torch.cuda.synchronize()
-        return sum(a.elapsed_time(b) for a, b in zip(st, en))
 
     batched_step()
     tuning = batch.tuning()
@@ -437,12 +532,29 @@ def run_gpu_batched(args, w):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     l0 = batch.launch_count()
-    local_ms = timed(batched_step, args.steps)
+    local_ms = timed_events(torch, stream, flush, batched_step, args.steps)
     if world > 1:
         torch.distributed.barrier()
     launches = batch.launch_count() - l0
     clocks = clocks_summary(clk)
     value, _, slowest_s = replicas.reduce_throughput(bodies * fmm_steps * args.steps, local_ms * 1e-3)
+    ms_per_step = slowest_s * 1e3 / args.steps
+
+    tl, tl_summary = timeline_pass(torch, stream, flush, batch, batched_step, min(args.steps, 3),
+                                   fmm_steps, ms_per_step)
+    moms = [np.empty(pl[1], rfmm.MOMENT_DTYPE) for pl in batch.plans]
+    batch.download_all_into(rfmm.BUF_MOMENTS, [a.ctypes.data for a in moms])
+    work = None
+    for m, pl, nb in zip(moms, batch.plans, sizes):
+        work = roofline.add_work(work, roofline.phase_work(nb, roofline.tree_work(m, pl[0])))
+    peak, peak_kind = hbm_peak()
+    sm_mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0
+    fp32 = roofline.fp32_peak_tflops(torch.cuda.get_device_properties(local).multi_processor_count,
+                                     sm_mhz)
+    phases = roofline.phases_roofline(work, tl, peak, fp32, peak_kind)
+    prof = batch.profile_steps(fmm_steps)
+    event_ms = {k: (v[0] / v[1] if v[1] else 0.0) for k, v in prof.items()}
+    roof = dominant_roofline(phases, tl, work, "batched_256", peak, peak_kind, event_ms["integrate"])
 
     # The same scenes back to back through plain handles (one handle per scene).
     solvers = []
@@ -459,21 +571,10 @@ def run_gpu_batched(args, w):
     plain_step()
     torch.cuda.synchronize()
     plain_k = max(1, min(args.steps, 3))
-    plain_ms = timed(plain_step, plain_k)
+    plain_ms = timed_events(torch, stream, flush, plain_step, plain_k)
     plain_value = bodies * fmm_steps * plain_k / (plain_ms * 1e-3)
     for s in solvers:
         s.close()
-
-    prof = batch.profile_steps(fmm_steps)
-    kernel_ms = {k: (v[0] / v[1] if v[1] else 0.0) for k, v in prof.items()}
-    integ_ms, integ_n = prof["integrate"]
-    alg = sum(64 * n for n in sizes) + sum(64 * pl[1] + 16 * 8 ** pl[0] for pl in batch.plans)
-    peak, peak_kind = hbm_peak()
-    achieved = alg / (integ_ms / integ_n * 1e-3) / 1e9
-    roofline = {"kernel": "k_integrate", "bound": "hbm", "achieved": achieved, "peak": peak,
-                "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                "algorithmic_bytes_per_launch": alg, "avg_launch_ms": integ_ms / integ_n,
-                "traffic": traffic_for(args.workload)}
 
     # End to end: pinned host scenes in, every scene's particles out.
     pin = [torch.from_numpy(p.view(np.uint8).copy()).pin_memory() for p in ps]
@@ -492,105 +593,179 @@ def run_gpu_batched(args, w):
             e2e_times.append(time.perf_counter() - t0)
     e2e = None
     if e2e_times:
-        e2e_s = statistics.mean(e2e_times)
+        e2e_s = statistics.median(e2e_times)
         e2e = {"value": world * bodies * fmm_steps / e2e_s, "unit": "body-steps/s",
                "h2d_bytes_per_step": bodies * 32, "d2h_bytes_per_step": bodies * 32,
-               "ms_per_step": 1e3 * e2e_s, "timer": "host wall clock"}
-    line = {
+               "ms_per_step": 1e3 * e2e_s, "timer": "host wall clock (median of %d)" % len(e2e_times)}
+    batch.close()
+    return {
         "metric": "body-steps/s", "value": value, "unit": "body-steps/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": slowest_s * 1e3 / args.steps,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded, numpy PCG64): " + w["desc"],
-        "config": {"workload": args.workload, "form": "batched (all scenes per launch)",
+        "config": {"workload": "batched_256", "form": "batched (all scenes per launch)",
                    "scenes": len(ps), "bodies": bodies, "fmm_steps_per_bench_step": fmm_steps,
-                   "plain_back_to_back_body_steps_per_s": plain_value,
-                   "batched_over_plain": value / world / plain_value,
                    "l2": "flushed between timed steps (512 MiB write outside the events)",
                    "parallelism": "scenes sharded over %d rank(s)" % world},
-        "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
-        "kernel_avg_ms": kernel_ms, "tuning": tuning.as_dict(),
+        "plain_back_to_back": {"value": plain_value, "unit": "body-steps/s",
+                               "timed_steps": plain_k,
+                               "form": "one plain handle per scene, solved one after another"},
+        "batched_over_plain": value / world / plain_value,
+        "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "roofline": roof,
+        "timeline": tl_summary, "kernel_event_avg_ms": event_ms, "tuning": tuning.as_dict(),
     }
+
+
+def gpu_setup(world, local):
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from rfmm import build as pkg_build
+    pkg_build.build()
+    import rfmm
+    # A real (non-default) stream shared by torch's events/flush and the solver.
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    return torch, rfmm, stream, flush
+
+
+def run_gpu(args, w):
+    rank, world, local = dist_env()
+    torch, rfmm, stream, flush = gpu_setup(world, local)
+    if w["kind"] == "batched":
+        line = run_gpu_batched(args, w, torch, rfmm, stream, flush, rank, world, local)
+    else:
+        line = run_gpu_plain(args, w, torch, rfmm, stream, flush, rank, world, local)
+        if args.workload == "plummer_1m" and not args.no_batched and args.near == "reference":
+            b = run_gpu_batched(args, workloads.WORKLOADS["batched_256"], torch, rfmm, stream,
+                                flush, rank, world, local)
+            line["batched"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "data", "config",
+                                                 "plain_back_to_back", "batched_over_plain",
+                                                 "clocks", "e2e", "gpu_launches", "roofline",
+                                                 "timeline", "tuning")}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds, args.near)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    batch.close()
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
 
 
-def served_requests(w, count):
-    """Seeded request pool: (particles, steps)."""
-    import numpy as np
-    from rfmm import scenes
-    rng = np.random.default_rng(w["seed"])
-    out = []
-    for i in range(count):
-        n = int(np.exp(rng.uniform(np.log(w["n_min"]), np.log(w["n_max"]))))
-        steps = int(rng.integers(1, w["steps_max"] + 1))
-        kind = ("uniform", "plummer", "clusters4")[i % 3]
-        out.append((scenes.make(kind, n, 2000 + i), steps))
-    return out
-
+# ------------------------------------------------------------------ serving
 
 def run_gpu_served(args, w):
-    """Throughput and p50/p99 latency of the continuous-batching server."""
+    """Continuous-batching server under Poisson arrivals (open loop), against
+    the same request list solved back to back through plain handles.
+
+    Producer threads submit each request at its scheduled arrival time and
+    pass that time to the server (rfmm_server_submit_at), so latency runs from
+    the scheduled arrival whether or not a submission starts late; a
+    collector thread takes the results as they finish.  The achieved
+    submission rate and the producers' lag behind the schedule are reported
+    beside the offered rate.
+    """
     import threading
-    import torch
+    import numpy as np
 
     rank, world, local = dist_env()
-    torch.cuda.set_device(local)
-    from rfmm import build as pkg_build
-    pkg_build.build()
-    import rfmm
-
-    import numpy as np
-    count = max(4, args.requests or w["requests"])
-    pool = served_requests(w, count)
+    torch, rfmm, stream, flush = gpu_setup(world, local)
+    count = args.requests or w["requests"]
+    pool = workloads.served_pool(w, count)
     params = rfmm.default_params(gravity=w["G"], softening=w["eps"], dt=w["dt"])
     rates = args.rates or w["rates"]
-    sweep = []
-    clk = None
-    launches = 0
-    # Warm-up: module load and first graph captures on a small server.
-    warm = rfmm.Server(max_bodies=w["n_max"], memory_budget_bytes=w["budget"], max_slots=4,
+    producers, collectors = 8, 4
+    staging = 8 << 30  # pinned host staging of the server (inputs 6 GiB, results 2 GiB)
+    body_steps = pool.body_steps()
+
+    # Warm-up: module load and graph captures on a small server.
+    warm = rfmm.Server(max_bodies=w["n_max"], memory_budget_bytes=2 << 30, max_slots=2,
                        max_chunk_steps=4)
-    for p, steps in pool[: min(3, len(pool))]:
-        rid = warm.submit(p, steps, params)
+    for i in range(min(3, count)):
+        rid = warm.submit(pool.bodies(i), int(pool.steps[i]), params)
         warm.wait(rid, 600000)
         warm.result(rid)
     warm.close()
+
+    sweep = []
+    clk = None
     for ri, rate in enumerate(rates):
         srv = rfmm.Server(max_bodies=w["n_max"], memory_budget_bytes=w["budget"],
-                          max_slots=w["slots"], max_chunk_steps=4)
+                          max_chunk_steps=4, staging_bytes=staging)
         arrivals = np.cumsum(np.random.default_rng(w["seed"] + ri).exponential(1.0 / rate, count))
         ids = [None] * count
+        actual = np.zeros(count)
+        errors = []
         if ri == len(rates) - 1:
             clk = clocks_sampler(local)
-        t0 = time.perf_counter()
+        offset = srv.clock() - time.perf_counter()  # server clock minus this clock
+        t0 = time.perf_counter() + 0.05
 
-        def producer():
-            for i, (p, steps) in enumerate(pool):
-                delay = t0 + arrivals[i] - time.perf_counter()
-                if delay > 0:
-                    time.sleep(delay)
-                ids[i] = srv.submit(p, steps, params)
+        def producer(k):
+            try:
+                for i in range(k, count, producers):
+                    d = t0 + arrivals[i] - time.perf_counter()
+                    if d > 0:
+                        time.sleep(d)
+                    actual[i] = time.perf_counter()
+                    ids[i] = srv.submit_at(pool.bodies(i), int(pool.steps[i]), params,
+                                           t0 + arrivals[i] + offset)
+            except Exception as e:  # surfaced after the run
+                errors.append(e)
 
-        th = threading.Thread(target=producer)
-        th.start()
-        th.join()
-        for rid in ids:
-            srv.wait(rid, 3600000)
-            srv.result(rid)
+        def collector(k):
+            try:
+                for i in range(k, count, collectors):
+                    while ids[i] is None and not errors:
+                        time.sleep(0.0002)
+                    if errors:
+                        return
+                    srv.wait(ids[i], 3600000)
+                    srv.result(ids[i])
+            except Exception as e:
+                errors.append(e)
+
+        ths = [threading.Thread(target=producer, args=(k,)) for k in range(producers)]
+        ths += [threading.Thread(target=collector, args=(k,)) for k in range(collectors)]
+        for th in ths:
+            th.start()
+        for th in ths:
+            th.join()
+        if errors:
+            raise errors[0]
         wall = time.perf_counter() - t0
         st = srv.stats()
         srv.close()
-        sweep.append({"rate_per_s": rate, "requests": count, "p50_ms": st["p50_ms"],
-                      "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"], "max_ms": st["max_ms"],
+        lag = (actual - (t0 + arrivals)) * 1e3
+        sweep.append({"offered_rate_per_s": rate,
+                      "achieved_rate_per_s": (count - 1) / (actual.max() - actual.min()),
+                      "submit_lag_ms": {"p50": float(np.percentile(lag, 50)),
+                                        "p99": float(np.percentile(lag, 99)),
+                                        "max": float(lag.max())},
+                      "requests": count, "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
+                      "mean_ms": st["mean_ms"], "max_ms": st["max_ms"],
                       "body_steps_per_s": st["body_steps_per_s"], "wall_s": wall,
-                      "slots": st["slots"]})
+                      "slots": st["slots"], "device_bytes": st["device_bytes"]})
     clocks = clocks_summary(clk)
-    top = sweep[-1]
-    body_steps = sum(len(p) * s for p, s in pool)
+
+    # The same request list back to back through plain handles: each request
+    # gets its own handle (created and destroyed outside the timer), then its
+    # upload, steps and download are timed on the host clock.
+    plain_s = 0.0
+    for i in range(count):
+        s = rfmm.Solver(int(pool.n[i]), params)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        s.upload(pool.bodies(i))
+        s.step(int(pool.steps[i]))
+        s.particles()
+        plain_s += time.perf_counter() - t
+        s.close()
+    plain_value = body_steps / plain_s
+    top = max(sweep, key=lambda r: r["body_steps_per_s"])
     line = {
         "metric": "body-steps/s", "value": top["body_steps_per_s"], "unit": "body-steps/s",
         "n_gpus": world, "steps": count, "warmup": 3, "ms_per_step": top["wall_s"] * 1e3 / count,
@@ -599,13 +774,19 @@ def run_gpu_served(args, w):
         "config": {"workload": args.workload, "form": "served (continuous batching)",
                    "requests_per_rate": count, "body_steps_per_rate": body_steps,
                    "memory_budget_bytes": w["budget"], "slot_capacity": w["n_max"],
-                   "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"], "sweep": sweep,
-                   "timer": "host wall clock, submit to result on host",
+                   "producer_threads": producers, "collector_threads": collectors,
+                   "staging_bytes": staging, "sweep": sweep,
+                   "timer": "host monotonic clock, scheduled arrival to result in host memory",
                    "parallelism": "1 GPU"},
+        "plain_back_to_back": {"value": plain_value, "unit": "body-steps/s",
+                               "requests": count,
+                               "timer": "host clock around upload + steps + download per request "
+                                        "(handle creation outside)"},
+        "served_over_plain": top["body_steps_per_s"] / plain_value,
         "clocks": clocks,
         "e2e": {"value": top["body_steps_per_s"], "unit": "body-steps/s",
-                "h2d_bytes_per_step": body_steps and int(sum(len(p) for p, _ in pool) * 32 / count),
-                "d2h_bytes_per_step": int(sum(len(p) for p, _ in pool) * 32 / count),
+                "h2d_bytes_per_step": int(np.sum(pool.n) * 32 / count),
+                "d2h_bytes_per_step": int(np.sum(pool.n) * 32 / count),
                 "note": "a step is one request; the served path is end to end by construction"},
         "gpu_launches": None,
     }
@@ -619,8 +800,6 @@ def main():
     w = workloads.WORKLOADS[args.workload]
     if args.impl == "reference":
         return run_reference(args, w)
-    if w["kind"] == "batched":
-        return run_gpu_batched(args, w)
     if w["kind"] == "served":
         return run_gpu_served(args, w)
     return run_gpu(args, w)

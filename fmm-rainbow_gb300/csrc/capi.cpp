@@ -181,6 +181,11 @@ int rfmm_set_near_mode(rfmm_handle *h, uint32_t mode) {
   return h->engine->set_near_mode(mode);
 }
 
+int rfmm_set_float_mode(rfmm_handle *h, uint32_t mode) {
+  if (guard(h)) return RFMM_ERR_INVALID;
+  return h->engine->set_float_mode(mode);
+}
+
 int rfmm_check_wait_timeout(rfmm_handle *h, uint32_t polls) {
   if (guard(h)) return RFMM_ERR_INVALID;
   return h->engine->check_wait_timeout(polls);
@@ -200,6 +205,16 @@ int rfmm_launch_count(rfmm_handle *h, uint64_t *out) {
   if (guard(h) || out == nullptr) return RFMM_ERR_INVALID;
   *out = h->engine->launch_count();
   return RFMM_OK;
+}
+
+int rfmm_set_timeline(rfmm_handle *h, uint32_t enable) {
+  if (guard(h) || enable > 1u) return RFMM_ERR_INVALID;
+  return h->engine->set_timeline(enable != 0u);
+}
+
+int rfmm_get_timeline(rfmm_handle *h, rfmm_timeline *out) {
+  if (guard(h) || out == nullptr) return RFMM_ERR_INVALID;
+  return h->engine->get_timeline(out);
 }
 
 int rfmm_accelerations(rfmm_handle *h, float *host_out, size_t bytes) {

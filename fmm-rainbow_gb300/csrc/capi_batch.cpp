@@ -146,6 +146,21 @@ int rfmm_batch_profile_steps(rfmm_batch *b, uint32_t steps, float *kernel_ms, ui
   return b->engine->profile_steps(steps, kernel_ms, launches);
 }
 
+int rfmm_batch_set_timeline(rfmm_batch *b, uint32_t enable) {
+  if (bad(b) || enable > 1u) return RFMM_ERR_INVALID;
+  return b->engine->set_timeline(enable != 0u);
+}
+
+int rfmm_batch_get_timeline(rfmm_batch *b, rfmm_timeline *out) {
+  if (bad(b) || out == nullptr) return RFMM_ERR_INVALID;
+  return b->engine->get_timeline(out);
+}
+
+int rfmm_batch_set_float_mode(rfmm_batch *b, uint32_t mode) {
+  if (bad(b)) return RFMM_ERR_INVALID;
+  return b->engine->set_float_mode(mode);
+}
+
 int rfmm_batch_set_resort_interval(rfmm_batch *b, uint32_t steps) {
   if (bad(b)) return RFMM_ERR_INVALID;
   return b->engine->set_resort_interval(steps);

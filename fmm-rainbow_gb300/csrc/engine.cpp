@@ -41,7 +41,25 @@ EncodeTiledFn get_encode_tiled() {
   return fn;
 }
 
+const StepLaunchers kExactLaunchers = {launch_upward, launch_m2l, launch_l2l_near, launch_integrate,
+                                       launch_accel, launch_accel_targets};
+const StepLaunchers kFastLaunchers = {fast::launch_upward, fast::launch_m2l, fast::launch_l2l_near,
+                                      fast::launch_integrate, fast::launch_accel,
+                                      fast::launch_accel_targets};
+
 }  // namespace
+
+const StepLaunchers &Engine::K() const {
+  return float_mode_ == RFMM_FLOAT_FAST ? kFastLaunchers : kExactLaunchers;
+}
+
+int Engine::set_float_mode(uint32_t mode) {
+  if (mode != RFMM_FLOAT_EXACT && mode != RFMM_FLOAT_FAST) return RFMM_ERR_INVALID;
+  if (mode == float_mode_) return RFMM_OK;
+  clear_graphs();  // captured with the other variant's kernels
+  float_mode_ = mode;
+  return RFMM_OK;
+}
 
 int cuda_status(cudaError_t e) {
   if (e == cudaSuccess) return RFMM_OK;
@@ -217,7 +235,9 @@ int Engine::create(const std::vector<SceneSpec> &specs, Engine **out) {
       if (e == cudaSuccess) e = cudaEventCreate(&ev);
   }
   if (e == cudaSuccess) e = configure_tree_kernels();
-  if (e == cudaSuccess) E->body_limit_ = body_ctas_per_sm();
+  if (e == cudaSuccess) e = fast::configure_tree_kernels();
+  // Both variants' integrate grids must fit: the smaller resident count.
+  if (e == cudaSuccess) E->body_limit_ = std::min(body_ctas_per_sm(), fast::body_ctas_per_sm());
   {
     rfmm_tuning t{};
     t.upward_ctas_per_sm = 6;
@@ -342,6 +362,59 @@ void Engine::clear_graphs() {
   if (stream_ != nullptr) cudaStreamSynchronize(stream_);
   for (auto &kv : graphs_) cudaGraphExecDestroy(kv.second.exec);
   graphs_.clear();
+  stamp_regions_used_ = 0;
+}
+
+int Engine::set_timeline(bool on) {
+  if (on && d_stamps_ == nullptr) {
+    const int st = alloc((void **)&d_stamps_, 8ull * kStampRegions * kStampSteps * kStampWordsPerStep);
+    if (st != RFMM_OK) return st;
+  }
+  clear_graphs();  // recaptured with (or without) the stamps
+  timeline_ = on;
+  return RFMM_OK;
+}
+
+// Each region holds the last run of its graph.  Per step and kernel kind:
+// busy = last CTA end - first CTA begin (after the dependency wait); gap =
+// that begin - the previous recorded kernel's end in the same graph run (the
+// launch and dependency latency in front of the kernel).
+int Engine::get_timeline(rfmm_timeline *out) {
+  if (out == nullptr) return RFMM_ERR_INVALID;
+  *out = rfmm_timeline{};
+  if (d_stamps_ == nullptr || stamp_regions_used_ == 0u) return RFMM_OK;
+  const size_t words = (size_t)stamp_regions_used_ * kStampSteps * kStampWordsPerStep;
+  std::vector<unsigned long long> h(words);
+  RF_CK(cudaMemcpyAsync(h.data(), d_stamps_, 8ull * words, cudaMemcpyDeviceToHost, stream_));
+  const int st = sync();
+  if (st != RFMM_OK) return st;
+  for (const auto &kv : graphs_) {
+    const Graph &g = kv.second;
+    if (g.region < 0) continue;
+    const unsigned long long *r = h.data() + (size_t)g.region * kStampSteps * kStampWordsPerStep;
+    unsigned long long first = 0, prev_end = 0, last = 0;
+    bool any = false;
+    for (uint32_t j = 0; j < g.len; j++) {
+      for (uint32_t k = 0; k < (uint32_t)kKernelKinds; k++) {
+        const unsigned long long *w = r + (size_t)j * kStampWordsPerStep + 2u * k;
+        if (w[1] == 0ull) continue;  // not launched in this step (or not stamped)
+        const unsigned long long begin = ~w[0], end = w[1];
+        if (end < begin) continue;
+        out->launches[k] += 1u;
+        out->busy_ms[k] += (double)(end - begin) * 1e-6;
+        if (any && begin > prev_end) out->gap_ms[k] += (double)(begin - prev_end) * 1e-6;
+        if (!any) first = begin;
+        any = true;
+        prev_end = end;
+        last = end;
+      }
+    }
+    if (any) {
+      out->steps += g.len;
+      out->span_ms += (double)(last - first) * 1e-6;
+    }
+  }
+  return RFMM_OK;
 }
 
 int Engine::get_tuning(rfmm_tuning *out) const {
@@ -465,6 +538,7 @@ LaunchCtx Engine::ctx(uint32_t mpar, uint32_t lpar, uint32_t ppar) const {
   L.p2p = near_mode_ == kNearP2P;
   L.pos4 = d_pos4_;
   L.starts_out = d_starts_;
+  L.stamps = nullptr;
   return L;
 }
 
@@ -538,9 +612,11 @@ int Engine::seed_galaxy(uint32_t scene) {
 
 uint32_t Engine::radix_sort_kernels() const { return 2u + 3u * ((key_bits_ + 7u) / 8u); }
 
-void Engine::enqueue_resort(uint32_t ppar, uint32_t count_par) {
-  // Leaf counting sort from the deposit of the current positions.
+void Engine::enqueue_resort(uint32_t ppar, uint32_t count_par, unsigned long long *stamps) {
+  // Leaf counting sort from the deposit of the current positions; `stamps`
+  // is the timeline record block of the step it follows.
   LaunchCtx L = ctx(mcur_, lpar_, ppar);
+  L.stamps = stamps;
   leaf_counting_sort(L, (uint32_t)scenes_.size(), max_depth_, d_mom_[count_par], d_leaf_blocks_,
                      d_starts_, d_part_[ppar], d_ids_[ppar], d_part_[ppar ^ 1u], d_ids_[ppar ^ 1u],
                      tiles_);
@@ -591,7 +667,7 @@ int Engine::commit_scene(uint32_t scene) {
 }
 
 int Engine::activate(uint32_t scene, uint32_t n, const rfmm_params &p, const void *src,
-                     cudaMemcpyKind kind) {
+                     cudaMemcpyKind kind, bool lists) {
   if (scene >= scenes_.size() || n == 0u) return RFMM_ERR_INVALID;
   SceneDesc &d = scenes_[scene];
   if (d.n != 0u) return RFMM_ERR_STATE;
@@ -623,25 +699,25 @@ int Engine::activate(uint32_t scene, uint32_t n, const rfmm_params &p, const voi
   if (st != RFMM_OK) return st;
   uploaded_[scene] = true;
   committed_ = true;
-  return rebuild_lists();
+  return lists ? rebuild_lists() : RFMM_OK;
 }
 
-int Engine::retire(uint32_t scene) {
+int Engine::retire(uint32_t scene, bool lists) {
   if (scene >= scenes_.size() || scenes_[scene].n == 0u) return RFMM_ERR_INVALID;
   const SceneDesc &d = scenes_[scene];
   LaunchCtx L = ctx(mcur_, lpar_, pcur_);
   launch_unpermute(L, d_ids_[pcur_], d_part_[pcur_ ^ 1u], d.tile_off, pad_tiles(d.n));
   RF_CK(cudaGetLastError());
   launches_ += 1;
-  return deactivate(scene);
+  return deactivate(scene, lists);
 }
 
-int Engine::deactivate(uint32_t scene) {
+int Engine::deactivate(uint32_t scene, bool lists) {
   if (scene >= scenes_.size()) return RFMM_ERR_INVALID;
   SceneDesc &d = scenes_[scene];
   d.n = 0u;
   RF_CK(cudaMemcpyAsync(d_scenes_ + scene, &d, sizeof(SceneDesc), cudaMemcpyHostToDevice, stream_));
-  return rebuild_lists();
+  return lists ? rebuild_lists() : RFMM_OK;
 }
 
 int Engine::commit() {
@@ -677,12 +753,13 @@ int Engine::commit() {
   return RFMM_OK;
 }
 
-void Engine::enqueue_step(uint32_t mpar, uint32_t lpar, uint32_t ppar) {
+void Engine::enqueue_step(uint32_t mpar, uint32_t lpar, uint32_t ppar, unsigned long long *stamps) {
   LaunchCtx L = ctx(mpar, lpar, ppar);
-  launch_upward(L, lpar, tasks_);
-  launch_m2l(L, lpar);
-  launch_l2l_near(L, lpar);
-  launch_integrate(L, tiles_);
+  L.stamps = stamps;
+  K().upward(L, lpar, tasks_);
+  K().m2l(L, lpar);
+  K().l2l_near(L, lpar);
+  K().integrate(L, tiles_);
   if (near_mode_ == kNearP2P) enqueue_p2p_sort(mpar, lpar, ppar, d_mom_[mpar ^ 1u]);
 }
 
@@ -729,9 +806,9 @@ int Engine::set_near_mode(uint32_t mode) {
 int Engine::solve_fields() {
   if (!committed_) return RFMM_ERR_STATE;
   LaunchCtx L = ctx(mcur_, lpar_, pcur_);
-  launch_upward(L, lpar_, tasks_);
-  launch_m2l(L, lpar_);
-  launch_l2l_near(L, lpar_);
+  K().upward(L, lpar_, tasks_);
+  K().m2l(L, lpar_);
+  K().l2l_near(L, lpar_);
   RF_CK(cudaGetLastError());
   launches_ += 3;
   lpar_ ^= 1u;
@@ -744,10 +821,24 @@ int Engine::launch_chunk(uint32_t len, bool sort_at_end) {
   const auto key = std::make_tuple(len, mcur_, lpar_, pcur_, sort_at_end);
   auto it = graphs_.find(key);
   if (it == graphs_.end()) {
+    // Timeline: this graph's records, cleared by its first node.
+    int region = -1;
+    unsigned long long *rec = nullptr;
+    if (timeline_ && d_stamps_ != nullptr && stamp_regions_used_ < kStampRegions &&
+        len <= kStampSteps) {
+      region = (int)stamp_regions_used_++;
+      rec = d_stamps_ + (size_t)region * kStampSteps * kStampWordsPerStep;
+    }
     cudaGraph_t g = nullptr;
     RF_CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
-    for (uint32_t j = 0; j < len; j++) enqueue_step(mcur_ ^ (j & 1u), lpar_ ^ (j & 1u), pcur_);
-    if (sort_at_end) enqueue_resort(pcur_, mcur_ ^ (len & 1u));
+    if (rec != nullptr)
+      cudaMemsetAsync(rec, 0, 8ull * kStampSteps * kStampWordsPerStep, stream_);
+    for (uint32_t j = 0; j < len; j++)
+      enqueue_step(mcur_ ^ (j & 1u), lpar_ ^ (j & 1u), pcur_,
+                   rec != nullptr ? rec + (size_t)j * kStampWordsPerStep : nullptr);
+    if (sort_at_end)
+      enqueue_resort(pcur_, mcur_ ^ (len & 1u),
+                     rec != nullptr ? rec + (size_t)(len - 1u) * kStampWordsPerStep : nullptr);
     cudaError_t e = cudaStreamEndCapture(stream_, &g);
     if (e != cudaSuccess) {
       if (g != nullptr) cudaGraphDestroy(g);
@@ -758,7 +849,7 @@ int Engine::launch_chunk(uint32_t len, bool sort_at_end) {
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return cuda_status(e);
     const uint32_t kernels = len * kernels_per_step() + (sort_at_end ? resort_kernels() : 0u);
-    it = graphs_.emplace(key, Graph{exec, kernels}).first;
+    it = graphs_.emplace(key, Graph{exec, kernels, len, sort_at_end, region}).first;
   }
   RF_CK(cudaGraphLaunch(it->second.exec, stream_));
   launches_ += it->second.kernels;
@@ -929,13 +1020,13 @@ int Engine::phase_times(float ms[7]) {
   RF_CK(cudaEventRecord(ev_[6], stream_));
   // One instrumented frame.
   RF_CK(cudaEventRecord(ev_[0], stream_));
-  launch_upward(L, lpar_, tasks_);
+  K().upward(L, lpar_, tasks_);
   RF_CK(cudaEventRecord(ev_[1], stream_));
-  launch_m2l(L, lpar_);
+  K().m2l(L, lpar_);
   RF_CK(cudaEventRecord(ev_[2], stream_));
-  launch_l2l_near(L, lpar_);
+  K().l2l_near(L, lpar_);
   RF_CK(cudaEventRecord(ev_[3], stream_));
-  launch_integrate(L, tiles_);
+  K().integrate(L, tiles_);
   RF_CK(cudaEventRecord(ev_[4], stream_));
   if (near_mode_ == kNearP2P) {
     enqueue_p2p_sort(mcur_, lpar_, pcur_, d_mom_[mcur_ ^ 1u]);
@@ -996,10 +1087,10 @@ int Engine::profile_steps(uint32_t steps, float ms[kKernelKinds], uint32_t launc
       since_sort_ = 0;
     }
     LaunchCtx L = ctx(mcur_, lpar_, pcur_);
-    timed(kKUpward, [&] { launch_upward(L, lpar_, tasks_); });
-    timed(kKM2L, [&] { launch_m2l(L, lpar_); });
-    timed(kKL2LNear, [&] { launch_l2l_near(L, lpar_); });
-    timed(kKIntegrate, [&] { launch_integrate(L, tiles_); });
+    timed(kKUpward, [&] { K().upward(L, lpar_, tasks_); });
+    timed(kKM2L, [&] { K().m2l(L, lpar_); });
+    timed(kKL2LNear, [&] { K().l2l_near(L, lpar_); });
+    timed(kKIntegrate, [&] { K().integrate(L, tiles_); });
     if (near_mode_ == kNearP2P)
       timed(kKResort, [&] { enqueue_p2p_sort(mcur_, lpar_, pcur_, d_mom_[mcur_ ^ 1u]); });
     launches_ += kernels_per_step();
@@ -1043,7 +1134,7 @@ int Engine::diag_prepare(uint32_t scene, size_t doubles, bool all_bodies) {
   if (st != RFMM_OK) return st;
   const SceneDesc &d = scenes_[scene];
   LaunchCtx L = ctx(tree_buf_ < 0 ? mcur_ : (uint32_t)tree_buf_, lpar_, pcur_);
-  if (all_bodies) launch_accel(L, d_ids_[pcur_], d_accphi_, d.tile_off, pad_tiles(d.n));
+  if (all_bodies) K().accel(L, d_ids_[pcur_], d_accphi_, d.tile_off, pad_tiles(d.n));
   launch_unpermute(L, d_ids_[pcur_], d_part_[pcur_ ^ 1u], d.tile_off, pad_tiles(d.n));
   RF_CK(cudaGetLastError());
   launches_ += all_bodies ? 2u : 1u;
@@ -1089,7 +1180,7 @@ int Engine::force_error(uint32_t scene, uint32_t targets, uint64_t seed, double 
   RF_CK(cudaMemcpyAsync(tgt, idx.data(), 4ull * nt, cudaMemcpyHostToDevice, stream_));
   {
     LaunchCtx L = ctx(tree_buf_ < 0 ? mcur_ : (uint32_t)tree_buf_, lpar_, pcur_);
-    launch_accel_targets(L, scene, d.tile_off, pad_tiles(d.n), d_ids_[pcur_], d_slot_of_, tgt, nt,
+    K().accel_targets(L, scene, d.tile_off, pad_tiles(d.n), d_ids_[pcur_], d_slot_of_, tgt, nt,
                          d_accphi_);
     launches_ += 2;
   }

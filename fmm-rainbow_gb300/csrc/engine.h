@@ -24,6 +24,18 @@ namespace rfmm {
 // Kernel kinds reported by profile_steps.
 enum KernelKind { kKUpward = 0, kKM2L, kKL2LNear, kKIntegrate, kKResort, kKernelKinds };
 
+// Launchers of the kernels whose arithmetic differs between the exact
+// contract and the fast float variant.
+struct StepLaunchers {
+  void (*upward)(const LaunchCtx &, uint32_t, uint32_t);
+  void (*m2l)(const LaunchCtx &, uint32_t);
+  void (*l2l_near)(const LaunchCtx &, uint32_t);
+  void (*integrate)(const LaunchCtx &, uint32_t);
+  void (*accel)(const LaunchCtx &, const uint32_t *, float4 *, uint32_t, uint32_t);
+  void (*accel_targets)(const LaunchCtx &, uint32_t, uint32_t, uint32_t, const uint32_t *,
+                        uint32_t *, const uint32_t *, uint32_t, float4 *);
+};
+
 struct SceneSpec {
   uint32_t n;          // bodies (or, for a slot, the capacity)
   rfmm_params params;  // for a slot: params.depth = deepest tree it must hold (0 = planner)
@@ -63,12 +75,15 @@ class Engine {
 
   // Serving slots: put `n` bodies with `params` into an empty slot (sorted
   // and deposited on the spot, other scenes untouched) or empty it again.
+  // With lists = false the active tile/task lists are left for one
+  // refresh_lists() after several slot changes.
   int activate(uint32_t scene, uint32_t n, const rfmm_params &params, const void *src,
-               cudaMemcpyKind kind);
-  int deactivate(uint32_t scene);
+               cudaMemcpyKind kind, bool lists = true);
+  int deactivate(uint32_t scene, bool lists = true);
   // Bodies of a finished slot back to the caller's order in the scratch
   // range (slot_scratch), then the slot is emptied.
-  int retire(uint32_t scene);
+  int retire(uint32_t scene, bool lists = true);
+  int refresh_lists() { return rebuild_lists(); }
   float4 *slot_bodies(uint32_t scene) const { return d_part_[pcur_] + 2ull * scenes_[scene].body_off; }
   float4 *slot_scratch(uint32_t scene) const {
     return d_part_[pcur_ ^ 1u] + 2ull * scenes_[scene].body_off;
@@ -84,6 +99,10 @@ class Engine {
   // kernel; adds per-kind device time (ms) and launch counts.
   int profile_steps(uint32_t steps, float ms[kKernelKinds], uint32_t launches[kKernelKinds]);
   uint64_t launch_count() const { return launches_; }
+  // Timeline mode: graphs captured from now on stamp every step kernel's
+  // first-CTA begin and last-CTA end (see rfmm_timeline).
+  int set_timeline(bool on);
+  int get_timeline(rfmm_timeline *out);
   int device_error(uint32_t *code, uint32_t *info);
 
   // Diagnostics on the current positions (each runs a field solve first).
@@ -102,6 +121,9 @@ class Engine {
   // state is re-sorted for the new mode.
   int set_near_mode(uint32_t mode);
   uint32_t near_mode() const { return near_mode_; }
+  // RFMM_FLOAT_EXACT (the oracle's contract) or RFMM_FLOAT_FAST.
+  int set_float_mode(uint32_t mode);
+  uint32_t float_mode() const { return float_mode_; }
   uint32_t total_tiles() const { return tiles_; }
 
  private:
@@ -109,11 +131,12 @@ class Engine {
   int alloc(void **p, size_t bytes);
   int build_tensor_maps();
   LaunchCtx ctx(uint32_t mpar, uint32_t lpar, uint32_t ppar) const;
-  void enqueue_step(uint32_t mpar, uint32_t lpar, uint32_t ppar);
+  void enqueue_step(uint32_t mpar, uint32_t lpar, uint32_t ppar,
+                    unsigned long long *stamps = nullptr);
   // Refresh of the resident leaf order: bodies of particle buffer `ppar` are
   // bucketed by leaf into the other buffer using the leaf counts of
   // moments buffer `count_par` (the deposit of the current positions).
-  void enqueue_resort(uint32_t ppar, uint32_t count_par);
+  void enqueue_resort(uint32_t ppar, uint32_t count_par, unsigned long long *stamps = nullptr);
   uint32_t radix_sort_kernels() const;  // keys + radix sort + gather (uploads)
   uint32_t max_depth_ = 0;
   uint32_t *d_leaf_blocks_ = nullptr;  // leaf counting sort: per-block sums
@@ -122,6 +145,8 @@ class Engine {
   void enqueue_p2p_sort(uint32_t mpar, uint32_t lpar, uint32_t ppar, uint4 *mom_into);
   uint32_t p2p_sort_kernels() const { return 4u + 3u * ((key_bits_ + 7u) / 8u); }
   uint32_t near_mode_ = kNearReference;
+  uint32_t float_mode_ = RFMM_FLOAT_EXACT;
+  const StepLaunchers &K() const;
   float4 *d_pos4_ = nullptr;      // kNearP2P: leaf-sorted positions
   uint32_t *d_starts_ = nullptr;  // per-leaf start slots (leaf sorts)
   int launch_chunk(uint32_t len, bool sort_at_end);
@@ -195,7 +220,17 @@ class Engine {
   struct Graph {
     cudaGraphExec_t exec;
     uint32_t kernels;  // kernel launches per graph launch
+    uint32_t len;      // steps per graph launch
+    bool sort_at_end;  // ends with a resort
+    int region;        // timeline region (-1: captured without stamps)
   };
+  // Timeline records: per captured graph one region of kStampSteps steps x
+  // kKernelKinds kinds x 2 words, cleared by the graph's first node.
+  static constexpr uint32_t kStampSteps = 64u, kStampRegions = 32u;
+  static constexpr uint32_t kStampWordsPerStep = 2u * kKernelKinds;
+  bool timeline_ = false;
+  uint32_t stamp_regions_used_ = 0;
+  unsigned long long *d_stamps_ = nullptr;
   std::map<std::tuple<uint32_t, uint32_t, uint32_t, uint32_t, bool>, Graph> graphs_;
   uint64_t launches_ = 0;  // kernels this engine has launched (graph nodes included)
   uint32_t resort_kernels() const { return 4u; }

@@ -19,7 +19,7 @@
 #include "rfmm_kernels.h"
 #include "rfmm_math.h"
 
-namespace rfmm {
+RFMM_KERNEL_NS_BEGIN
 
 // Leaf (level `depth`) cell of a position, local to the scene's tree.
 __device__ __forceinline__ uint32_t leaf_cell(float x, float y, float z, uint32_t depth) {
@@ -100,7 +100,7 @@ __device__ __forceinline__ void p2p_sums(const SceneDesc &S, const P2PView &V, u
           const float4 q = __ldg(&V.pos[j]);
           const float dx = q.x - px, dy = q.y - py, dz = q.z - pz;
           const float r2 = ((dx * dx + dy * dy) + dz * dz) + eps2;
-          const float inv = 1.0f / sqrtf(r2);
+          const float inv = inv_sqrt(r2);
           const float w = (inv * inv) * inv;
           sx = sx + dx * w;
           sy = sy + dy * w;
@@ -185,7 +185,7 @@ __device__ __forceinline__ uint32_t body_acceleration(const SceneDesc &S, float 
       const float4 s = __ldg(&src[cell_index]);
       const float dx = s.x - px, dy = s.y - py, dz = s.z - pz;
       const float eps = fmaxf(S.softening, (0.62f * kHalf) * pow2_neg(chosen));
-      const float inv_r = 1.0f / sqrtf((dx * dx + dy * dy) + dz * dz + eps * eps);
+      const float inv_r = inv_sqrt((dx * dx + dy * dy) + dz * dz + eps * eps);
       const float gsm = ax4.x;  // G * f32(count - 1) / f32(N)
       ax = ax + gsm * dx * inv_r * inv_r * inv_r;
       ay = ay + gsm * dy * inv_r * inv_r * inv_r;
@@ -233,7 +233,7 @@ __device__ __forceinline__ void integrate_body(const SceneDesc &S, float4 &p0, f
       const float cr = fmaxf(S.control_radius, 0.02f);
       control_influence = rf_expf(-2.0f * d2 / (cr * cr));
       const float strength = S.control_strength;
-      const float inv = 1.0f / sqrtf(d2 + cr * cr * 0.018f);
+      const float inv = inv_sqrt(d2 + cr * cr * 0.018f);
       const float dirx = cdx * inv, diry = cdy * inv, dirz = cdz * inv;
       const float mode = S.control_axis_mode[3];
       if (mode < 1.5f) {
@@ -327,12 +327,14 @@ __global__ void __launch_bounds__(256, 6) k_integrate(const SceneDesc *__restric
                                                    const uint32_t *__restrict__ tile_list,
                                                    Counters *__restrict__ ctr, int dynamic,
                                                    const float4 *__restrict__ pos4,
-                                                   const uint32_t *__restrict__ starts) {
+                                                   const uint32_t *__restrict__ starts,
+                                                   unsigned long long *__restrict__ stamp) {
   __shared__ DepositTable T;
   __shared__ SceneDesc S;
   __shared__ uint32_t s_next;
   if (!kP2P) T.clear();
   grid_dependency_wait();  // fields of this step are complete
+  stamp_begin(stamp);
   const uint32_t ntiles = tile_list != nullptr ? min(ctr->tiles_active, tiles) : tiles;
   // Static schedule: interleaved tiles.  Dynamic: tiles are taken one at a
   // time from a counter (reset by this step's upward pass).
@@ -383,6 +385,7 @@ __global__ void __launch_bounds__(256, 6) k_integrate(const SceneDesc *__restric
     __syncthreads();
     T.flush(mom_next);
   }
+  stamp_end(stamp);
   grid_dependents_may_launch();
 }
 
@@ -754,7 +757,8 @@ void launch_integrate(const LaunchCtx &L, uint32_t tiles) {
                      dim3(kTile), 0, L.scenes, L.tile_scene, L.part, (const uint4 *)L.mom,
                      (const float4 *)L.src, (const float4 *)L.aux, (const uint32_t *)L.choice,
                      (const float *)L.fields, L.mom_next, tiles, L.tile_list, L.ctr,
-                     L.integrate_dynamic ? 1 : 0, L.pos4, (const uint32_t *)L.starts_out);
+                     L.integrate_dynamic ? 1 : 0, L.pos4, (const uint32_t *)L.starts_out,
+                     stamp_rec(L, 3u));
 }
 
 void launch_deposit(const LaunchCtx &L, uint4 *moments, uint32_t tiles) {
@@ -848,4 +852,4 @@ void launch_iota(cudaStream_t stream, uint32_t *ids, uint32_t count) {
   k_iota<<<(count + 255u) / 256u, 256, 0, stream>>>(ids, count);
 }
 
-}  // namespace rfmm
+RFMM_KERNEL_NS_END

@@ -212,8 +212,10 @@ __device__ __forceinline__ uint32_t block_sum_1024(uint32_t v, uint32_t *warp_bu
 __global__ void __launch_bounds__(kLeafThreads) k_leaf_block_sums(const SceneDesc *__restrict__ scenes,
                                                                   const uint4 *__restrict__ mom,
                                                                   uint32_t *__restrict__ block_sums,
-                                                                  uint32_t max_blocks) {
+                                                                  uint32_t max_blocks,
+                                                                  unsigned long long *__restrict__ stamp) {
   __shared__ uint32_t warp_buf[32];
+  stamp_begin(stamp);  // first of the resort's four kernels
   const SceneDesc &S = scenes[blockIdx.y];
   const uint32_t leaves = 1u << (3u * S.depth);
   const uint32_t base = blockIdx.x * kLeafBlock;
@@ -309,7 +311,8 @@ __global__ void __launch_bounds__(256) k_leaf_scatter(const SceneDesc *__restric
                                                       const uint32_t *__restrict__ ids_in,
                                                       float4 *__restrict__ part_out,
                                                       uint32_t *__restrict__ ids_out,
-                                                      uint32_t *__restrict__ starts, uint32_t tiles) {
+                                                      uint32_t *__restrict__ starts, uint32_t tiles,
+                                                      unsigned long long *__restrict__ stamp) {
   __shared__ uint32_t hkey[kScatterSlots], hcnt[kScatterSlots];
   constexpr uint32_t kEmptyKey = 0xFFFFFFFFu;
   for (uint32_t i = threadIdx.x; i < kScatterSlots; i += blockDim.x) {
@@ -367,6 +370,7 @@ __global__ void __launch_bounds__(256) k_leaf_scatter(const SceneDesc *__restric
     part_out[2u * dst + 1u] = p1[r];
     ids_out[dst] = ids_in[src[r]];
   }
+  stamp_end(stamp);  // last of the resort's four kernels
 }
 
 uint32_t leaf_sort_blocks(uint32_t max_depth) {
@@ -378,12 +382,13 @@ void leaf_counting_sort(const LaunchCtx &L, uint32_t scenes, uint32_t max_depth,
                         const uint32_t *ids_in, float4 *part_out, uint32_t *ids_out,
                         uint32_t tiles) {
   const uint32_t nb = leaf_sort_blocks(max_depth);
-  k_leaf_block_sums<<<dim3(nb, scenes), kLeafThreads, 0, L.stream>>>(L.scenes, counts, block_scratch, nb);
+  k_leaf_block_sums<<<dim3(nb, scenes), kLeafThreads, 0, L.stream>>>(L.scenes, counts, block_scratch, nb,
+                                                                      stamp_rec(L, 4u));
   k_leaf_block_scan<<<scenes, 32, 0, L.stream>>>(L.scenes, block_scratch, nb);
   k_leaf_offsets<<<dim3(nb, scenes), kLeafThreads, 0, L.stream>>>(L.scenes, counts, block_scratch, nb,
                                                                     starts);
   k_leaf_scatter<<<(tiles + kScatterTiles - 1u) / kScatterTiles, 256, 0, L.stream>>>(
-      L.scenes, L.tile_scene, part_in, ids_in, part_out, ids_out, starts, tiles);
+      L.scenes, L.tile_scene, part_in, ids_in, part_out, ids_out, starts, tiles, stamp_rec(L, 4u));
 }
 
 }  // namespace rfmm

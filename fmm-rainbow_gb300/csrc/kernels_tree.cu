@@ -36,7 +36,7 @@
 #include "rfmm_device.cuh"
 #include "rfmm_kernels.h"
 
-namespace rfmm {
+RFMM_KERNEL_NS_BEGIN
 
 // ----------------------------------------------------------------- upward
 
@@ -272,7 +272,8 @@ __global__ void __launch_bounds__(256) k_upward(const SceneDesc *__restrict__ sc
                                                 WorkItem *__restrict__ plist, uint32_t plist_cap,
                                                 const WorkItem *__restrict__ plist_prev,
                                                 Counters *__restrict__ ctr, uint32_t list_par,
-                                                uint32_t *__restrict__ tickets, uint32_t clear_ctas) {
+                                                uint32_t *__restrict__ tickets, uint32_t clear_ctas,
+                                                unsigned long long *__restrict__ stamp) {
   __shared__ uint4 s0[512];
   __shared__ uint4 s1[64];
   __shared__ uint4 s2[9];     // level D-2, then the subtree root
@@ -283,6 +284,7 @@ __global__ void __launch_bounds__(256) k_upward(const SceneDesc *__restrict__ sc
   const uint32_t tid = threadIdx.x;
   if (blockIdx.x < clear_ctas) {
     grid_dependency_wait();  // the previous integrate read the fields
+    stamp_begin(stamp);
     if (blockIdx.x == 0 && tid == 0) ctr->tile_cursor = 0u;  // for this step's integrate
     // Each warp takes 32 listed parents at a time (one per lane), then clears
     // their 8 children's 48-byte fields with one 16-byte store per lane.
@@ -309,6 +311,7 @@ __global__ void __launch_bounds__(256) k_upward(const SceneDesc *__restrict__ sc
         }
       }
     }
+    stamp_end(stamp);
     grid_dependents_may_launch();
     return;
   }
@@ -325,6 +328,7 @@ __global__ void __launch_bounds__(256) k_upward(const SceneDesc *__restrict__ sc
     load_scene(sS, scenes, scene);
   }
   grid_dependency_wait();  // the previous integrate deposited into mom_next
+  stamp_begin(stamp);
   for (uint32_t it = cta; it < ntasks; it += ncta) {
     if (it != cta) {
       task = task_list != nullptr ? task_list[it] : it;
@@ -334,6 +338,7 @@ __global__ void __launch_bounds__(256) k_upward(const SceneDesc *__restrict__ sc
     upward_task(sS, scene, task - sS.task_off, mom, mom_next, src, aux, choice, plist, plist_cap,
                 ctr, list_par, tickets, s0, s1, s2, s_top, s_items, s_nitems, s_base, s_last);
   }
+  stamp_end(stamp);
   grid_dependents_may_launch();
 }
 
@@ -435,7 +440,8 @@ __global__ void __launch_bounds__(256) k_m2l(const SceneDesc *__restrict__ scene
                                              const uint4 *__restrict__ mom,
                                              const float4 *__restrict__ src,
                                              float *__restrict__ lfield,
-                                             const CUtensorMap *__restrict__ tmaps) {
+                                             const CUtensorMap *__restrict__ tmaps,
+                                             unsigned long long *__restrict__ stamp) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   // The TMA destination must be 128-byte aligned: align the carve-out by hand
   // (the launch reserves 128 spare bytes).
@@ -450,6 +456,7 @@ __global__ void __launch_bounds__(256) k_m2l(const SceneDesc *__restrict__ scene
   }
   for (uint32_t k = tid; k < kTileCells; k += blockDim.x) sh.slot_info[k] = m2l_slot_info(k);
   grid_dependency_wait();  // the upward pass built the tree and the parent list
+  stamp_begin(stamp);
   const uint32_t count = min(ctr->parents[list_par], plist_cap);
   if (blockIdx.x == 0 && tid == 0) ctr->parents[list_par ^ 1u] = 0u;  // reset for the next step
   __syncthreads();
@@ -607,6 +614,7 @@ __global__ void __launch_bounds__(256) k_m2l(const SceneDesc *__restrict__ scene
     }
     __syncthreads();
   }
+  stamp_end(stamp);
   grid_dependents_may_launch();
 }
 
@@ -624,7 +632,8 @@ __global__ void __launch_bounds__(256) k_l2l_near(const SceneDesc *__restrict__ 
                                                   uint32_t list_par, const uint4 *__restrict__ mom,
                                                   const float4 *__restrict__ src,
                                                   const float *__restrict__ lfield,
-                                                  float *__restrict__ fields) {
+                                                  float *__restrict__ fields,
+                                                  unsigned long long *__restrict__ stamp) {
   __shared__ L2LShared sh;
   const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
   if (tid < 127u) {
@@ -632,6 +641,7 @@ __global__ void __launch_bounds__(256) k_l2l_near(const SceneDesc *__restrict__ 
     sh.centre[tid] = cell_center_lv(tid + 1u - (1u << l), l);
   }
   grid_dependency_wait();  // M2L results of every target are complete
+  stamp_begin(stamp);
   const uint32_t count = min(ctr->parents[list_par], plist_cap);
   // Lane c < 12 owns field component c (ax ay az phi Jxx Jxy Jxz Jyy Jyz Jzz 0 0).
   const uint32_t c = lane < 12u ? lane : 11u;
@@ -726,6 +736,7 @@ __global__ void __launch_bounds__(256) k_l2l_near(const SceneDesc *__restrict__ 
     }
     if (lane < 12u) fields[(size_t)target * 12u + lane] = f;
   }
+  stamp_end(stamp);
   grid_dependents_may_launch();
 }
 
@@ -760,7 +771,8 @@ void launch_upward(const LaunchCtx &L, uint32_t list_par, uint32_t tasks) {
   clear = clear < 8u ? 8u : (clear > 64u ? 64u : clear);
   launch_step_kernel(L, k_upward, dim3(grid + clear), dim3(256), 0, L.scenes, L.task_scene,
                      L.task_list, tasks, L.mom, L.mom_next, L.src, L.aux, L.choice, L.fields,
-                     L.plist, L.plist_cap, L.plist_prev, L.ctr, list_par, L.tickets, clear);
+                     L.plist, L.plist_cap, L.plist_prev, L.ctr, list_par, L.tickets, clear,
+                     stamp_rec(L, 0u));
 }
 
 size_t m2l_smem_bytes(bool compact) {
@@ -771,13 +783,13 @@ void launch_m2l(const LaunchCtx &L, uint32_t list_par) {
   launch_step_kernel(L, L.m2l_compact ? k_m2l<true> : k_m2l<false>, dim3(L.m2l_ctas), dim3(256),
                      m2l_smem_bytes(L.m2l_compact), L.scenes,
                      (const WorkItem *)L.plist, L.plist_cap, L.ctr, list_par, (const uint4 *)L.mom,
-                     (const float4 *)L.src, L.lfield, L.tmaps);
+                     (const float4 *)L.src, L.lfield, L.tmaps, stamp_rec(L, 1u));
 }
 
 void launch_l2l_near(const LaunchCtx &L, uint32_t list_par) {
   launch_step_kernel(L, k_l2l_near, dim3(L.l2l_ctas), dim3(256), 0, L.scenes, (const WorkItem *)L.plist,
                      L.plist_cap, (const Counters *)L.ctr, list_par, (const uint4 *)L.mom,
-                     (const float4 *)L.src, (const float *)L.lfield, L.fields);
+                     (const float4 *)L.src, (const float *)L.lfield, L.fields, stamp_rec(L, 2u));
 }
 
 cudaError_t configure_tree_kernels() {
@@ -789,4 +801,4 @@ cudaError_t configure_tree_kernels() {
   return e;
 }
 
-}  // namespace rfmm
+RFMM_KERNEL_NS_END

@@ -10,6 +10,14 @@
 // rounds exactly like the CPU oracle (binary32, round-to-nearest, no
 // contraction).  The expression trees follow the WGSL source left to right;
 // changing an association here changes results bit-wise.
+//
+// The fast float variant (RFMM_FAST_FLOAT, namespace rfmm::fast) compiles the
+// tree and body kernels a second time with contraction on, approximate
+// division and square root, and WGSL inverseSqrt as the hardware reciprocal
+// square root: the latitude WGSL itself gives these operations.  The leaf and
+// fixed-point arithmetic (unit_coord, cell_of_unit, the deposit rounding) is
+// written with explicit round-to-nearest intrinsics or exact scalings, so
+// leaf assignment and every integer result are the same in both variants.
 #pragma once
 
 #include <cstdint>
@@ -17,7 +25,19 @@
 
 #include "rfmm_shared.h"
 
-namespace rfmm {
+#ifdef RFMM_FAST_FLOAT
+#define RFMM_KERNEL_NS_BEGIN \
+  namespace rfmm {           \
+  namespace fast {
+#define RFMM_KERNEL_NS_END \
+  }                        \
+  }
+#else
+#define RFMM_KERNEL_NS_BEGIN namespace rfmm {
+#define RFMM_KERNEL_NS_END }
+#endif
+
+RFMM_KERNEL_NS_BEGIN
 
 constexpr float kHalf = 1.60f;           // WORLD_HALF_EXTENT, wgsl:12
 constexpr uint32_t kAdaptive = 16u;      // ADAPTIVE_LEAF_CAPACITY, wgsl:10
@@ -113,6 +133,36 @@ __device__ __forceinline__ void grid_dependents_may_launch() {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
+// Optional per-launch timeline record, two 64-bit words: rec[0] holds the
+// largest ~t_begin over the launch's CTAs (so ~rec[0] is the earliest begin)
+// and rec[1] the latest t_end, in %globaltimer nanoseconds; both start at 0.
+// t_begin is taken after the dependency wait (when the CTA can work), t_end
+// when the CTA is done.  A null record costs one predicated branch.
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void stamp_begin(unsigned long long *rec) {
+  if (rec != nullptr && threadIdx.x == 0) atomicMax(rec, ~global_ns());
+}
+// Every thread of the CTA calls it: with a record it waits for the CTA's
+// other threads before stamping.
+__device__ __forceinline__ void stamp_end(unsigned long long *rec) {
+  if (rec != nullptr) {
+    __syncthreads();
+    if (threadIdx.x == 0) atomicMax(rec + 1, global_ns());
+  }
+}
+
+// WGSL inverseSqrt (wgsl:179, 654, 670): IEEE 1 / sqrt in the exact
+// contract, the hardware reciprocal square root in the fast variant.
+#ifdef RFMM_FAST_FLOAT
+__device__ __forceinline__ float inv_sqrt(float x) { return rsqrtf(x); }
+#else
+__device__ __forceinline__ float inv_sqrt(float x) { return 1.0f / sqrtf(x); }
+#endif
+
 // pair_field (wgsl:170-203) for a source cell whose centre of mass `src`
 // and gravity-times-mass `gm` were precomputed exactly as the reference
 // computes them per pair (moment_com_read and G * count / N).
@@ -121,7 +171,7 @@ __device__ __forceinline__ void pair_field_d(float4 src, float tx, float ty, flo
   const float gm = src.w;
   const float rx = src.x - tx, ry = src.y - ty, rz = src.z - tz;
   const float r2 = (rx * rx + ry * ry) + rz * rz + eps * eps;
-  const float inv_r = 1.0f / sqrtf(r2);
+  const float inv_r = inv_sqrt(r2);
   const float inv_r3 = inv_r * inv_r * inv_r;
   const float inv_r5 = inv_r3 * inv_r * inv_r;
   const float diagonal = -gm * inv_r3;
@@ -252,4 +302,4 @@ __device__ __forceinline__ void load_scene(SceneDesc &dst, const SceneDesc *scen
   __syncthreads();
 }
 
-}  // namespace rfmm
+RFMM_KERNEL_NS_END

@@ -59,7 +59,15 @@ struct LaunchCtx {
   bool p2p;                    // near field by exact pair sums (every scene in kNearP2P)
   float4 *pos4;                // leaf-sorted position snapshot (kNearP2P)
   uint32_t *starts_out;        // per-leaf start table (kNearP2P)
+  // Timeline records of this step (2 words per kernel kind, upward, M2L,
+  // L2L + near, integrate, resort), or null: no stamps.
+  unsigned long long *stamps;
 };
+
+// Record of kernel kind `kind` (0..4) within a step's timeline, or null.
+inline unsigned long long *stamp_rec(const LaunchCtx &L, uint32_t kind) {
+  return L.stamps != nullptr ? L.stamps + 2u * kind : nullptr;
+}
 
 // Launch `kernel` on L.stream, with programmatic dependent launch when L.pdl:
 // the kernel may start while its predecessor drains and waits for it with
@@ -156,6 +164,24 @@ void launch_direct_sum_f64(cudaStream_t stream, const float4 *part_caller, uint3
                            double *partial, uint32_t splits, double *out);
 void launch_diagnostics(cudaStream_t stream, const float4 *part_caller, const float4 *accphi,
                         uint32_t n, double *partial, uint32_t blocks, double *out);
+
+// The step kernels of the fast float variant (kernels_tree.cu and
+// kernels_body.cu compiled a second time with RFMM_FAST_FLOAT: contraction
+// on, approximate division and square root, hardware reciprocal square root
+// for WGSL inverseSqrt).  Same signatures and launch shapes as above.
+namespace fast {
+void launch_upward(const LaunchCtx &L, uint32_t list_par, uint32_t tasks);
+void launch_m2l(const LaunchCtx &L, uint32_t list_par);
+void launch_l2l_near(const LaunchCtx &L, uint32_t list_par);
+void launch_integrate(const LaunchCtx &L, uint32_t tiles);
+void launch_accel(const LaunchCtx &L, const uint32_t *ids, float4 *out, uint32_t tile_base,
+                  uint32_t tiles);
+void launch_accel_targets(const LaunchCtx &L, uint32_t scene, uint32_t tile_base, uint32_t tiles,
+                          const uint32_t *ids, uint32_t *slot_of, const uint32_t *targets,
+                          uint32_t nt, float4 *out);
+cudaError_t configure_tree_kernels();
+uint32_t body_ctas_per_sm();
+}  // namespace fast
 
 // LSD radix sort of (key, value) pairs, 8-bit digits (kernels_sort.cu).
 struct SortScratch {

@@ -8,17 +8,28 @@
 // the same launches (the batched step).  Finished scenes leave their slot at
 // a step boundary and the slot is refilled.
 //
-// Three host threads keep copies off the critical path:
-//   stage-in  copies a request's bodies into its slot on a copy stream;
-//   worker    activates staged slots (sort + deposit), steps the engine, and
-//             retires finished slots (bodies back to the caller's order in a
-//             scratch range, then an event);
-//   drain     waits for that event and copies the result to host memory on
-//             its own stream, then frees the slot.
+// Host staging: submit copies the caller's bodies into a pinned input ring
+// (a pageable copy when the ring is full), so the device copy runs at the
+// host-link rate; the ring space returns as soon as the request is on the
+// device.  Results land in a pinned output ring until the caller takes them.
+// Host threads keep the copies off the critical path:
+//   stage-in (kStageThreads)  copy queued requests into free slots, each on
+//                             its own copy stream;
+//   worker                    activates staged slots (sort + deposit), steps
+//                             the engine, and retires finished slots (bodies
+//                             back to the caller's order in a scratch range,
+//                             then an event);
+//   drain                     waits for that event, copies the result into
+//                             the output ring on its own stream, frees the
+//                             slot.
+// Latency runs from the request's arrival (the entry into submit, or the
+// arrival time the caller gives rfmm_server_submit_at) to the moment its
+// result is in host memory.
 // Results are bit-identical to a plain solve of the same scene (same kernels,
 // order-independent arithmetic), whatever else shares the batch.
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
@@ -43,15 +54,98 @@ double now_s() {
 enum ReqState { kQueued = 0, kRunning = 1, kDone = 2, kFailed = 3 };
 enum SlotState { kFree, kStaging, kStaged, kActive, kDraining };
 
+constexpr int kStageThreads = 4;
+constexpr uint64_t kDefaultStagingBytes = 4ull << 30;
+
+// A ring of pinned host memory handing out contiguous blocks in allocation
+// order; blocks may be released in any order, and the space of the oldest
+// block returns once every older block is released too.
+class PinnedRing {
+ public:
+  ~PinnedRing() {
+    if (base_ != nullptr) cudaFreeHost(base_);
+  }
+  bool init(size_t bytes) {
+    if (bytes == 0) return true;
+    void *p = nullptr;
+    if (cudaHostAlloc(&p, bytes, cudaHostAllocPortable) != cudaSuccess) {
+      (void)cudaGetLastError();
+      return false;
+    }
+    base_ = static_cast<uint8_t *>(p);
+    cap_ = bytes;
+    return true;
+  }
+  // A block of `bytes`, or null when the ring cannot hold it now.
+  uint8_t *alloc(size_t bytes) {
+    bytes = (bytes + 255u) & ~size_t(255);
+    std::lock_guard<std::mutex> lk(m_);
+    if (base_ == nullptr || bytes > cap_) return nullptr;
+    size_t off;
+    if (blocks_.empty()) {
+      off = 0;
+    } else {
+      const size_t tail = blocks_.front().off;
+      if (head_ > tail) {  // live region [tail, head): free [head, cap) and [0, tail)
+        if (bytes <= cap_ - head_) {
+          off = head_;
+        } else if (bytes < tail) {
+          off = 0;
+        } else {
+          return nullptr;
+        }
+      } else if (head_ < tail) {  // wrapped: free [head, tail)
+        if (bytes < tail - head_) {
+          off = head_;
+        } else {
+          return nullptr;
+        }
+      } else {
+        return nullptr;  // head == tail with live blocks: full
+      }
+    }
+    blocks_.push_back({off, true});
+    head_ = off + bytes;
+    return base_ + off;
+  }
+  // Blocks may come back in any order; null and foreign pointers are ignored.
+  void release(uint8_t *p) {
+    if (p == nullptr || base_ == nullptr || p < base_ || p >= base_ + cap_) return;
+    std::lock_guard<std::mutex> lk(m_);
+    const size_t off = (size_t)(p - base_);
+    for (Block &b : blocks_)
+      if (b.off == off && b.live) {
+        b.live = false;
+        break;
+      }
+    while (!blocks_.empty() && !blocks_.front().live) blocks_.pop_front();
+    if (blocks_.empty()) head_ = 0;
+  }
+
+ private:
+  struct Block {
+    size_t off;
+    bool live;
+  };
+  uint8_t *base_ = nullptr;
+  size_t cap_ = 0, head_ = 0;
+  std::deque<Block> blocks_;
+  std::mutex m_;
+};
+
 struct Request {
   uint64_t id = 0;
   uint32_t n = 0, steps = 0, left = 0;
   rfmm_params params{};
+  uint8_t *in_ring = nullptr;   // input in the pinned input ring, or null: `input`
+  uint8_t *out_ring = nullptr;  // result in the pinned output ring, or null: `output`
   std::vector<uint8_t> input, output;
   int state = kQueued;
   int status = RFMM_OK;
   int slot = -1;
-  double t_submit = 0, t_admit = 0, t_done = 0;
+  double t_arrival = 0, t_admit = 0, t_done = 0;
+  const uint8_t *in() const { return in_ring != nullptr ? in_ring : input.data(); }
+  uint8_t *out() { return out_ring != nullptr ? out_ring : output.data(); }
 };
 
 struct Slot {
@@ -66,14 +160,16 @@ class Server {
  public:
   static int create(const rfmm_server_config &cfg, Server **out);
   ~Server();
-  int submit(const void *host, uint32_t n, const rfmm_params *p, uint32_t steps, uint64_t *id);
+  // arrival_s: the request's arrival on now_s()'s clock; NaN = now.
+  int submit(const void *host, uint32_t n, const rfmm_params *p, uint32_t steps, double arrival_s,
+             uint64_t *id);
   int status(uint64_t id, int *state);
   int wait(uint64_t id, uint32_t timeout_ms);
   int result(uint64_t id, void *dst, size_t bytes);
   int stats(rfmm_server_stats *out);
 
  private:
-  void stage_loop();
+  void stage_loop(int k);
   void worker_loop();
   void drain_loop();
   int pick_free_slot(uint32_t n) const;
@@ -81,7 +177,8 @@ class Server {
   Engine *E_ = nullptr;
   int device_ = 0;
   uint32_t max_chunk_ = 4;
-  cudaStream_t copy_in_ = nullptr, copy_out_ = nullptr;
+  cudaStream_t copy_in_[kStageThreads] = {}, copy_out_ = nullptr;
+  PinnedRing in_ring_, out_ring_;
   std::vector<Slot> slots_;
   std::mutex m_;
   std::condition_variable cv_;  // any state change
@@ -91,7 +188,8 @@ class Server {
   uint64_t next_id_ = 1;
   bool stop_ = false;
   int failure_ = RFMM_OK;
-  std::thread stage_thr_, worker_thr_, drain_thr_;
+  std::vector<std::thread> stage_thr_;
+  std::thread worker_thr_, drain_thr_;
   // statistics
   std::vector<double> latencies_ms_;
   double first_submit_ = 0, last_done_ = 0, body_steps_ = 0;
@@ -111,6 +209,8 @@ int Server::create(const rfmm_server_config &cfg, Server **out) {
   uint64_t nslots = cfg.memory_budget_bytes / per_slot;
   if (cfg.max_slots != 0u) nslots = std::min<uint64_t>(nslots, cfg.max_slots);
   nslots = std::min<uint64_t>(nslots, 4096u);
+  // The engine indexes body slots with 32-bit arithmetic (at most 2^30 slots).
+  nslots = std::min<uint64_t>(nslots, (1ull << 30) / ((uint64_t)((cap + 255u) / 256u) * 256u));
   if (nslots == 0u) return RFMM_ERR_BUDGET;
 
   std::vector<SceneSpec> specs(nslots);
@@ -129,8 +229,19 @@ int Server::create(const rfmm_server_config &cfg, Server **out) {
   }
   cudaGetDevice(&S->device_);
   S->max_chunk_ = cfg.max_chunk_steps ? cfg.max_chunk_steps : 4u;
+  // Staging: three quarters for inputs (they wait in the queue), one quarter
+  // for results; at least one largest request each.
+  const uint64_t staging = cfg.staging_bytes ? cfg.staging_bytes : kDefaultStagingBytes;
+  const uint64_t one = 32ull * cap;
+  if (!S->in_ring_.init(std::max<uint64_t>(staging / 4 * 3, one)) ||
+      !S->out_ring_.init(std::max<uint64_t>(staging / 4, one))) {
+    delete S;
+    return RFMM_ERR_OOM;
+  }
   S->slots_.resize(nslots);
-  cudaError_t e = cudaStreamCreateWithFlags(&S->copy_in_, cudaStreamNonBlocking);
+  cudaError_t e = cudaSuccess;
+  for (auto &cs : S->copy_in_)
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&S->copy_out_, cudaStreamNonBlocking);
   for (auto &sl : S->slots_)
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.ready, cudaEventDisableTiming);
@@ -138,7 +249,7 @@ int Server::create(const rfmm_server_config &cfg, Server **out) {
     delete S;
     return cuda_status(e);
   }
-  S->stage_thr_ = std::thread(&Server::stage_loop, S);
+  for (int k = 0; k < kStageThreads; k++) S->stage_thr_.emplace_back(&Server::stage_loop, S, k);
   S->worker_thr_ = std::thread(&Server::worker_loop, S);
   S->drain_thr_ = std::thread(&Server::drain_loop, S);
   *out = S;
@@ -151,14 +262,23 @@ Server::~Server() {
     stop_ = true;
   }
   cv_.notify_all();
-  if (stage_thr_.joinable()) stage_thr_.join();
+  for (auto &t : stage_thr_)
+    if (t.joinable()) t.join();
   if (worker_thr_.joinable()) worker_thr_.join();
   if (drain_thr_.joinable()) drain_thr_.join();
+  if (E_ != nullptr) E_->sync();
   for (auto &kv : reqs_) delete kv.second;
   for (auto &sl : slots_)
     if (sl.ready != nullptr) cudaEventDestroy(sl.ready);
-  if (copy_in_ != nullptr) cudaStreamDestroy(copy_in_);
-  if (copy_out_ != nullptr) cudaStreamDestroy(copy_out_);
+  for (auto &cs : copy_in_) {
+    if (cs == nullptr) continue;
+    cudaStreamSynchronize(cs);
+    cudaStreamDestroy(cs);
+  }
+  if (copy_out_ != nullptr) {
+    cudaStreamSynchronize(copy_out_);
+    cudaStreamDestroy(copy_out_);
+  }
   delete E_;
 }
 
@@ -169,7 +289,8 @@ int Server::pick_free_slot(uint32_t n) const {
 }
 
 int Server::submit(const void *host, uint32_t n, const rfmm_params *p, uint32_t steps,
-                   uint64_t *id) {
+                   double arrival_s, uint64_t *id) {
+  const double t_entry = now_s();  // before any copy: the copy is part of the latency
   if (host == nullptr || n == 0u || steps == 0u || id == nullptr) return RFMM_ERR_INVALID;
   if (n > E_->capacity(0)) return RFMM_ERR_BUDGET;
   Request *r = new (std::nothrow) Request();
@@ -186,16 +307,18 @@ int Server::submit(const void *host, uint32_t n, const rfmm_params *p, uint32_t 
     delete r;
     return RFMM_ERR_BUDGET;
   }
-  r->input.resize(32ull * n);
-  std::memcpy(r->input.data(), host, r->input.size());
+  r->in_ring = in_ring_.alloc(32ull * n);
+  if (r->in_ring == nullptr) r->input.resize(32ull * n);
+  std::memcpy(r->in_ring != nullptr ? r->in_ring : r->input.data(), host, 32ull * n);
   std::lock_guard<std::mutex> lk(m_);
   if (failure_ != RFMM_OK) {
+    in_ring_.release(r->in_ring);
     delete r;
     return failure_;
   }
   r->id = next_id_++;
-  r->t_submit = now_s();
-  if (submitted_ == 0) first_submit_ = r->t_submit;
+  r->t_arrival = std::isnan(arrival_s) ? t_entry : arrival_s;
+  if (submitted_ == 0 || r->t_arrival < first_submit_) first_submit_ = r->t_arrival;
   submitted_++;
   reqs_[r->id] = r;
   queue_.push_back(r);
@@ -204,8 +327,9 @@ int Server::submit(const void *host, uint32_t n, const rfmm_params *p, uint32_t 
   return RFMM_OK;
 }
 
-// Copies the oldest queued request into a free slot on the input copy stream.
-void Server::stage_loop() {
+// Copies the oldest queued request into a free slot on this thread's copy
+// stream, then returns the request's input ring space.
+void Server::stage_loop(int k) {
   cudaSetDevice(device_);
   for (;;) {
     Request *r = nullptr;
@@ -224,10 +348,12 @@ void Server::stage_loop() {
       r->slot = s;
     }
     float4 *dst = E_->slot_bodies((uint32_t)s);
-    cudaError_t e = cudaMemcpyAsync(dst, r->input.data(), r->input.size(), cudaMemcpyHostToDevice,
-                                    copy_in_);
-    if (e == cudaSuccess) e = cudaEventRecord(slots_[s].ready, copy_in_);
+    cudaError_t e = cudaMemcpyAsync(dst, r->in(), 32ull * r->n, cudaMemcpyHostToDevice, copy_in_[k]);
+    if (e == cudaSuccess) e = cudaEventRecord(slots_[s].ready, copy_in_[k]);
     if (e == cudaSuccess) e = cudaEventSynchronize(slots_[s].ready);
+    in_ring_.release(r->in_ring);  // the input is on the device (or the copy failed)
+    r->in_ring = nullptr;
+    std::vector<uint8_t>().swap(r->input);
     std::lock_guard<std::mutex> lk(m_);
     if (e != cudaSuccess) {
       r->state = kFailed;
@@ -242,22 +368,33 @@ void Server::stage_loop() {
   }
 }
 
+// Slot changes (admissions, retirements) update the engine's active lists
+// once per iteration.  The worker stays at most kRunAhead chunks ahead of the
+// GPU, so a request staged meanwhile is admitted behind little queued work.
+constexpr int kRunAhead = 2;
+
 void Server::worker_loop() {
   cudaSetDevice(device_);
   std::vector<int> active;
+  cudaEvent_t ahead[kRunAhead] = {};
+  for (auto &ev : ahead) cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+  uint64_t chunks = 0;
   for (;;) {
     std::vector<int> to_activate;
     {
       std::unique_lock<std::mutex> lk(m_);
       cv_.wait(lk, [&] { return stop_ || !staged_fifo_.empty() || !active.empty(); });
-      if (stop_) return;
+      if (stop_) {
+        for (auto &ev : ahead) cudaEventDestroy(ev);
+        return;
+      }
       to_activate.assign(staged_fifo_.begin(), staged_fifo_.end());
       staged_fifo_.clear();
     }
     int st = RFMM_OK;
     for (int s : to_activate) {
       Request *r = slots_[s].req;
-      st = E_->activate((uint32_t)s, r->n, r->params, nullptr, cudaMemcpyDeviceToDevice);
+      st = E_->activate((uint32_t)s, r->n, r->params, nullptr, cudaMemcpyDeviceToDevice, false);
       std::lock_guard<std::mutex> lk(m_);
       if (st != RFMM_OK) {
         r->state = kFailed;
@@ -272,23 +409,31 @@ void Server::worker_loop() {
         active.push_back(s);
       }
     }
+    if (!to_activate.empty() && st == RFMM_OK) st = E_->refresh_lists();
     if (active.empty()) continue;
+    // Bounded run-ahead: wait for the chunk enqueued kRunAhead chunks ago.
+    cudaEvent_t &slot_ev = ahead[chunks % kRunAhead];
+    if (chunks >= (uint64_t)kRunAhead) cudaEventSynchronize(slot_ev);
     uint32_t chunk = max_chunk_;
     for (int s : active) chunk = std::min(chunk, slots_[s].req->left);
-    st = E_->step(chunk);
+    if (st == RFMM_OK) st = E_->step(chunk);
+    if (st == RFMM_OK) st = cuda_status(cudaEventRecord(slot_ev, E_->stream()));
+    chunks++;
     std::vector<int> finished;
     for (int s : active) {
       slots_[s].req->left -= chunk;
       if (slots_[s].req->left == 0u) finished.push_back(s);
     }
     for (int s : finished) {
-      if (st == RFMM_OK) st = E_->retire((uint32_t)s);  // unpermute into scratch, slot emptied
+      // Unpermute into scratch and empty the slot (lists refreshed below).
+      if (st == RFMM_OK) st = E_->retire((uint32_t)s, false);
       if (st == RFMM_OK) st = cuda_status(cudaEventRecord(slots_[s].ready, E_->stream()));
       active.erase(std::find(active.begin(), active.end(), s));
       std::lock_guard<std::mutex> lk(m_);
       slots_[s].state = kDraining;
       drain_fifo_.push_back(s);
     }
+    if (!finished.empty() && st == RFMM_OK) st = E_->refresh_lists();
     if (st != RFMM_OK) {
       std::lock_guard<std::mutex> lk(m_);
       failure_ = st;
@@ -309,10 +454,11 @@ void Server::drain_loop() {
       drain_fifo_.pop_front();
     }
     Request *r = slots_[s].req;
-    r->output.resize(32ull * r->n);
+    r->out_ring = out_ring_.alloc(32ull * r->n);
+    if (r->out_ring == nullptr) r->output.resize(32ull * r->n);
     cudaError_t e = cudaStreamWaitEvent(copy_out_, slots_[s].ready, 0);
     if (e == cudaSuccess)
-      e = cudaMemcpyAsync(r->output.data(), E_->slot_scratch((uint32_t)s), r->output.size(),
+      e = cudaMemcpyAsync(r->out(), E_->slot_scratch((uint32_t)s), 32ull * r->n,
                           cudaMemcpyDeviceToHost, copy_out_);
     if (e == cudaSuccess) e = cudaStreamSynchronize(copy_out_);
     std::lock_guard<std::mutex> lk(m_);
@@ -322,7 +468,7 @@ void Server::drain_loop() {
       r->status = cuda_status(e);
     } else {
       r->state = kDone;
-      latencies_ms_.push_back(1e3 * (r->t_done - r->t_submit));
+      latencies_ms_.push_back(1e3 * (r->t_done - r->t_arrival));
       body_steps_ += (double)r->n * r->steps;
       last_done_ = r->t_done;
       completed_++;
@@ -353,20 +499,25 @@ int Server::wait(uint64_t id, uint32_t timeout_ms) {
 }
 
 int Server::result(uint64_t id, void *dst, size_t bytes) {
-  std::unique_lock<std::mutex> lk(m_);
-  auto it = reqs_.find(id);
-  if (it == reqs_.end() || dst == nullptr) return RFMM_ERR_INVALID;
-  Request *r = it->second;
-  if (r->state == kFailed) {
-    const int st = r->status;
-    reqs_.erase(it);
-    delete r;
-    return st;
+  Request *r = nullptr;
+  {
+    std::unique_lock<std::mutex> lk(m_);
+    auto it = reqs_.find(id);
+    if (it == reqs_.end() || dst == nullptr) return RFMM_ERR_INVALID;
+    r = it->second;
+    if (r->state == kFailed) {
+      const int st = r->status;
+      reqs_.erase(it);
+      out_ring_.release(r->out_ring);
+      delete r;
+      return st;
+    }
+    if (r->state != kDone) return RFMM_ERR_STATE;
+    if (bytes != 32ull * r->n) return RFMM_ERR_INVALID;
+    reqs_.erase(it);  // this caller owns the request from here
   }
-  if (r->state != kDone) return RFMM_ERR_STATE;
-  if (bytes != r->output.size()) return RFMM_ERR_INVALID;
-  std::memcpy(dst, r->output.data(), bytes);
-  reqs_.erase(it);
+  std::memcpy(dst, r->out(), bytes);  // outside the lock: other threads keep going
+  out_ring_.release(r->out_ring);
   delete r;
   return RFMM_OK;
 }
@@ -432,7 +583,20 @@ int rfmm_server_destroy(rfmm_server *srv) {
 int rfmm_server_submit(rfmm_server *srv, const void *host_aos, uint32_t n, const rfmm_params *params,
                        uint32_t steps, uint64_t *request_id) {
   if (srv == nullptr) return RFMM_ERR_INVALID;
-  return srv->impl->submit(host_aos, n, params, steps, request_id);
+  return srv->impl->submit(host_aos, n, params, steps, std::nan(""), request_id);
+}
+
+int rfmm_server_submit_at(rfmm_server *srv, const void *host_aos, uint32_t n,
+                          const rfmm_params *params, uint32_t steps, double arrival_s,
+                          uint64_t *request_id) {
+  if (srv == nullptr || !std::isfinite(arrival_s)) return RFMM_ERR_INVALID;
+  return srv->impl->submit(host_aos, n, params, steps, arrival_s, request_id);
+}
+
+int rfmm_server_clock(double *now) {
+  if (now == nullptr) return RFMM_ERR_INVALID;
+  *now = rfmm::now_s();
+  return RFMM_OK;
 }
 
 int rfmm_server_status(rfmm_server *srv, uint64_t request_id, int *state) {

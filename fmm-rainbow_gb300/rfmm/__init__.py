@@ -33,6 +33,7 @@ STATUS = {
 }
 BUF_PARTICLES, BUF_MOMENTS, BUF_FIELDS = 0, 1, 2
 NEAR_REFERENCE, NEAR_P2P = 0, 1
+FLOAT_EXACT, FLOAT_FAST = 0, 1
 PHASES = ("clear", "deposit", "upward", "m2l", "downward", "near", "integrate")
 
 # Every symbol the headers in include/ declare, with its ctypes signature.
@@ -58,7 +59,8 @@ class Params(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("memory_budget_bytes", C.c_uint64), ("max_bodies", C.c_uint32),
-                ("max_slots", C.c_uint32), ("max_chunk_steps", C.c_uint32)]
+                ("max_slots", C.c_uint32), ("max_chunk_steps", C.c_uint32),
+                ("staging_bytes", C.c_uint64)]
 
 
 class ServerStats(C.Structure):
@@ -79,6 +81,19 @@ class Tuning(C.Structure):
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Timeline(C.Structure):
+    """`rfmm_timeline` (include/rfmm.h): step kernels as they ran inside the graphs."""
+
+    _fields_ = [("steps", C.c_uint32), ("launches", C.c_uint32 * 5), ("busy_ms", C.c_double * 5),
+                ("gap_ms", C.c_double * 5), ("span_ms", C.c_double)]
+
+    def as_dict(self):
+        kinds = ("upward", "m2l", "l2l_near", "integrate", "resort")
+        return {"steps": self.steps, "span_ms": self.span_ms,
+                "kinds": {k: {"launches": self.launches[i], "busy_ms": self.busy_ms[i],
+                              "gap_ms": self.gap_ms[i]} for i, k in enumerate(kinds)}}
 
 
 class Diagnostics(C.Structure):
@@ -136,9 +151,15 @@ SIGNATURES = {
     "rfmm_check_finite": (_i, [_vp, _u32, C.POINTER(_u32), C.POINTER(_f32)]),
     "rfmm_set_resort_interval": (_i, [_vp, _u32]),
     "rfmm_set_near_mode": (_i, [_vp, _u32]),
+    "rfmm_set_float_mode": (_i, [_vp, _u32]),
+    "rfmm_batch_set_float_mode": (_i, [_vp, _u32]),
     "rfmm_device_error": (_i, [_vp, C.POINTER(_u32), C.POINTER(_u32)]),
     "rfmm_profile_steps": (_i, [_vp, _u32, C.POINTER(_f32), C.POINTER(_u32)]),
     "rfmm_launch_count": (_i, [_vp, C.POINTER(C.c_uint64)]),
+    "rfmm_set_timeline": (_i, [_vp, _u32]),
+    "rfmm_get_timeline": (_i, [_vp, C.POINTER(Timeline)]),
+    "rfmm_batch_set_timeline": (_i, [_vp, _u32]),
+    "rfmm_batch_get_timeline": (_i, [_vp, C.POINTER(Timeline)]),
     "rfmm_solve_fields_noalloc": (_i, [_vp, _u32, _P, _vp, _vp, _vp]),
     "rfmm_noalloc_device_error": (_i, [C.POINTER(_u32), C.POINTER(_u32), _vp]),
     "rfmm_batch_create": (_i, [_u32, C.POINTER(_u32), _P, C.POINTER(_vp)]),
@@ -180,6 +201,8 @@ SIGNATURES = {
     "rfmm_server_create": (_i, [C.POINTER(ServerConfig), C.POINTER(_vp)]),
     "rfmm_server_destroy": (_i, [_vp]),
     "rfmm_server_submit": (_i, [_vp, _vp, _u32, _P, _u32, C.POINTER(C.c_uint64)]),
+    "rfmm_server_submit_at": (_i, [_vp, _vp, _u32, _P, _u32, C.c_double, C.POINTER(C.c_uint64)]),
+    "rfmm_server_clock": (_i, [C.POINTER(C.c_double)]),
     "rfmm_server_status": (_i, [_vp, C.c_uint64, C.POINTER(_i)]),
     "rfmm_server_wait": (_i, [_vp, C.c_uint64, _u32]),
     "rfmm_server_result": (_i, [_vp, C.c_uint64, _vp, _sz]),
@@ -345,6 +368,9 @@ class Solver:
     def set_near_mode(self, mode: int):
         _check(lib().rfmm_set_near_mode(self._h, mode), "rfmm_set_near_mode")
 
+    def set_float_mode(self, mode: int):
+        _check(lib().rfmm_set_float_mode(self._h, mode), "rfmm_set_float_mode")
+
     def download(self, which: int = BUF_PARTICLES) -> np.ndarray:
         dtype, count = {BUF_PARTICLES: (PARTICLE_DTYPE, self.n), BUF_MOMENTS: (MOMENT_DTYPE, self.cells),
                         BUF_FIELDS: (FIELD_DTYPE, self.cells)}[which]
@@ -397,6 +423,14 @@ class Solver:
         out = C.c_uint64()
         _check(lib().rfmm_launch_count(self._h, C.byref(out)), "rfmm_launch_count")
         return out.value
+
+    def set_timeline(self, on: bool):
+        _check(lib().rfmm_set_timeline(self._h, 1 if on else 0), "rfmm_set_timeline")
+
+    def timeline(self) -> dict:
+        t = Timeline()
+        _check(lib().rfmm_get_timeline(self._h, C.byref(t)), "rfmm_get_timeline")
+        return t.as_dict()
 
     def accelerations(self) -> np.ndarray:
         """(N, 4) float32: FMM ax, ay, az, phi of the current positions (caller order)."""
@@ -490,6 +524,9 @@ class Batch:
     def set_near_mode(self, mode):
         _check(lib().rfmm_batch_set_near_mode(self._h, mode), "rfmm_batch_set_near_mode")
 
+    def set_float_mode(self, mode):
+        _check(lib().rfmm_batch_set_float_mode(self._h, mode), "rfmm_batch_set_float_mode")
+
     def upload(self, scene, particles):
         a = np.ascontiguousarray(particles)
         assert a.dtype == PARTICLE_DTYPE and len(a) == self.sizes[scene]
@@ -541,6 +578,14 @@ class Batch:
         _check(lib().rfmm_batch_launch_count(self._h, C.byref(out)), "rfmm_batch_launch_count")
         return out.value
 
+    def set_timeline(self, on):
+        _check(lib().rfmm_batch_set_timeline(self._h, 1 if on else 0), "rfmm_batch_set_timeline")
+
+    def timeline(self):
+        t = Timeline()
+        _check(lib().rfmm_batch_get_timeline(self._h, C.byref(t)), "rfmm_batch_get_timeline")
+        return t.as_dict()
+
     def force_error(self, scene, targets=1024, seed=1):
         rms, mx = C.c_double(), C.c_double()
         _check(lib().rfmm_batch_force_error(self._h, scene, targets, seed, C.byref(rms), C.byref(mx)),
@@ -570,8 +615,10 @@ class Batch:
 class Server:
     """Continuous-batching solve server (the `rfmm_server_*` handle)."""
 
-    def __init__(self, max_bodies, memory_budget_bytes=8 << 30, max_slots=0, max_chunk_steps=0):
-        cfg = ServerConfig(memory_budget_bytes, max_bodies, max_slots, max_chunk_steps)
+    def __init__(self, max_bodies, memory_budget_bytes=8 << 30, max_slots=0, max_chunk_steps=0,
+                 staging_bytes=0):
+        cfg = ServerConfig(memory_budget_bytes, max_bodies, max_slots, max_chunk_steps,
+                           staging_bytes)
         self._h = C.c_void_p()
         _check(lib().rfmm_server_create(C.byref(cfg), C.byref(self._h)), "rfmm_server_create")
         self._n = {}
@@ -602,6 +649,23 @@ class Server:
                                         C.byref(rid)), "rfmm_server_submit")
         self._n[rid.value] = len(a)
         return rid.value
+
+    def submit_at(self, particles, steps, params, arrival_s):
+        """Submit with an explicit arrival time on the server clock (see clock())."""
+        a = np.ascontiguousarray(particles)
+        assert a.dtype == PARTICLE_DTYPE
+        rid = C.c_uint64()
+        _check(lib().rfmm_server_submit_at(self._h, a.ctypes.data, len(a),
+                                           C.byref(params) if params is not None else None, steps,
+                                           arrival_s, C.byref(rid)), "rfmm_server_submit_at")
+        self._n[rid.value] = len(a)
+        return rid.value
+
+    @staticmethod
+    def clock():
+        t = C.c_double()
+        _check(lib().rfmm_server_clock(C.byref(t)), "rfmm_server_clock")
+        return t.value
 
     def status(self, rid):
         st = C.c_int()

@@ -6,7 +6,9 @@ in parallel, and links one shared library exporting the C ABI declared in
 
 Kernel translation units are compiled with ``-fmad=false`` and IEEE division
 and square root, which is the floating-point contract the kernels rely on to
-match the CPU oracle bit for bit.
+match the CPU oracle bit for bit.  The tree and body kernels are compiled a
+second time with ``-DRFMM_FAST_FLOAT`` (namespace ``rfmm::fast``), contraction
+on and approximate division and square root: the fast float variant.
 """
 from __future__ import annotations
 
@@ -28,6 +30,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I", CSRC, "-I", INCLUDE,
           "-I", BUILD]
 KERNEL_FLAGS = ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"]
+FAST_FLAGS = ["-DRFMM_FAST_FLOAT", "-fmad=true", "-prec-div=false", "-prec-sqrt=false", "-ftz=false"]
+# Compiled again in the fast float variant (object name, source).
+FAST_SOURCES = ["kernels_tree.cu", "kernels_body.cu"]
 
 SOURCES = [
     "kernels_tree.cu",
@@ -73,10 +78,10 @@ def _gen_source_text() -> str:
     return out
 
 
-def _compile(src: str, obj: str, extra=()) -> None:
+def _compile(src: str, obj: str, extra=(), fast: bool = False) -> None:
     flags = list(COMMON) + list(ARCH) + list(extra)
     if src.endswith(".cu"):
-        flags += KERNEL_FLAGS
+        flags += FAST_FLAGS if fast else KERNEL_FLAGS
     cmd = [nvcc(), *flags, "-c", src, "-o", obj]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
@@ -115,9 +120,16 @@ def build(force: bool = False, csrc: str | None = None, lib: str | None = None,
     os.makedirs(os.path.dirname(os.path.abspath(out_lib)), exist_ok=True)
     srcs = [os.path.join(csrc_dir, s) for s in SOURCES] + [_gen_source_text()]
     objs = [os.path.join(build_dir, os.path.basename(s) + ".o") for s in srcs]
+    jobs = [(s, o, False) for s, o in zip(srcs, objs)]
+    for f in FAST_SOURCES:
+        o = os.path.join(build_dir, f + ".fast.o")
+        jobs.append((os.path.join(csrc_dir, f), o, True))
+        objs.append(o)
     extra = list(extra_flags) + ["-I", csrc_dir]
-    with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
-        list(ex.map(lambda a: _compile(a[0], a[1], extra), zip(srcs, objs)))
+    # The largest translation units first, so they start before the short ones.
+    jobs.sort(key=lambda j: -os.path.getsize(j[0]))
+    with cf.ThreadPoolExecutor(max_workers=min(os.cpu_count() or 8, len(jobs))) as ex:
+        list(ex.map(lambda a: _compile(a[0], a[1], extra, a[2]), jobs))
     LIB_OUT = out_lib
     tmp = LIB_OUT + ".tmp%d" % os.getpid()
     cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-Xcompiler", "-fPIC"]

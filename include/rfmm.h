@@ -162,6 +162,22 @@ int rfmm_set_resort_interval(rfmm_handle *h, uint32_t steps);
 #define RFMM_NEAR_P2P 1u
 int rfmm_set_near_mode(rfmm_handle *h, uint32_t mode);
 
+/* Floating-point variant of the step kernels (no counterpart in the
+ * reference, whose WGSL leaves these details to the implementation).
+ * RFMM_FLOAT_EXACT (default): binary32 round-to-nearest without contraction,
+ * IEEE division and square root, inverseSqrt as 1/sqrt -- the CPU oracle's
+ * contract, so results are reproducible bit for bit.  RFMM_FLOAT_FAST: the
+ * latitude WGSL gives (multiply-add contraction, approximate division and
+ * square root within a few ulp, inverseSqrt as the hardware reciprocal
+ * square root).  Leaf assignment, moments and every integer result of a
+ * field solve are identical in both; floating-point results agree within
+ * the tolerances stated by the fast-mode tests (accelerations ~1e-6
+ * relative rms), and trajectories drift apart at that level per step.
+ * Switching drops the captured graphs. */
+#define RFMM_FLOAT_EXACT 0u
+#define RFMM_FLOAT_FAST 1u
+int rfmm_set_float_mode(rfmm_handle *h, uint32_t mode);
+
 /* Last kernel error word (0 = none) and its detail. */
 int rfmm_device_error(rfmm_handle *h, uint32_t *code, uint32_t *info);
 /* Self-check of the kernels' bounded waits: one CTA waits on an mbarrier
@@ -190,6 +206,26 @@ int rfmm_profile_steps(rfmm_handle *h, uint32_t steps, float *kernel_ms, uint32_
 /* Number of solver kernels this handle has launched so far (kernels inside
  * CUDA graphs included). */
 int rfmm_launch_count(rfmm_handle *h, uint64_t *out);
+
+/* Device timeline of the step kernels as they run inside the captured
+ * graphs (no counterpart in the reference; its harness reads per-pass GPU
+ * timestamps, native/main.rs:462-520).  With the timeline on, every graph
+ * captured afterwards stamps, for each step kernel, the %globaltimer time at
+ * which its first CTA passed its dependency wait and the time its last CTA
+ * finished; each graph keeps the records of its most recent run.  Turning
+ * it on or off drops the captured graphs (they are captured again on the
+ * next step).  The stamps cost one atomic per CTA and launch. */
+typedef struct rfmm_timeline {
+  uint32_t steps;                        /* steps the records cover */
+  uint32_t launches[RFMM_KERNEL_KINDS];  /* recorded launches per kernel kind */
+  double busy_ms[RFMM_KERNEL_KINDS];     /* sum of (last CTA end - first CTA begin) */
+  double gap_ms[RFMM_KERNEL_KINDS];      /* sum of (first CTA begin - previous kernel's end):
+                                          * launch and dependency latency in front of it */
+  double span_ms;                        /* sum over the recorded graph runs of
+                                          * (last end - first begin) */
+} rfmm_timeline;
+int rfmm_set_timeline(rfmm_handle *h, uint32_t enable);
+int rfmm_get_timeline(rfmm_handle *h, rfmm_timeline *out);
 
 /* ---------------------------------------------------------------- accuracy
  *
@@ -308,8 +344,11 @@ int rfmm_batch_download_device(rfmm_batch *b, uint32_t scene, int which, void *d
 int rfmm_batch_digest(rfmm_batch *b, uint32_t scene, int which, uint32_t *out);
 int rfmm_batch_launch_count(rfmm_batch *b, uint64_t *out);
 int rfmm_batch_profile_steps(rfmm_batch *b, uint32_t steps, float *kernel_ms, uint32_t *launches);
+int rfmm_batch_set_timeline(rfmm_batch *b, uint32_t enable);
+int rfmm_batch_get_timeline(rfmm_batch *b, rfmm_timeline *out);
 int rfmm_batch_set_resort_interval(rfmm_batch *b, uint32_t steps);
 int rfmm_batch_set_near_mode(rfmm_batch *b, uint32_t mode);
+int rfmm_batch_set_float_mode(rfmm_batch *b, uint32_t mode);
 int rfmm_batch_get_tuning(rfmm_batch *b, rfmm_tuning *out);
 int rfmm_batch_set_tuning(rfmm_batch *b, const rfmm_tuning *tuning);
 int rfmm_batch_autotune(rfmm_batch *b, uint32_t steps_per_trial, rfmm_tuning *best);
@@ -332,14 +371,16 @@ typedef struct rfmm_server_config {
   uint32_t max_bodies;          /* slot capacity = largest admissible request */
   uint32_t max_slots;           /* 0 = as many as the budget allows (<= 4096) */
   uint32_t max_chunk_steps;     /* steps between admission points (0 = 4) */
+  uint64_t staging_bytes;       /* pinned host memory for request inputs (3/4) and
+                                 * results (1/4); 0 = 4 GiB */
 } rfmm_server_config;
 
 typedef struct rfmm_server_stats {
   uint64_t submitted, completed, queued, in_flight;
   uint32_t slots, slot_capacity;
   uint64_t device_bytes;
-  double p50_ms, p99_ms, mean_ms, max_ms; /* submit -> result on host */
-  double body_steps_per_s;                /* completed work / (last done - first submit) */
+  double p50_ms, p99_ms, mean_ms, max_ms; /* arrival -> result in host memory */
+  double body_steps_per_s;                /* completed work / (last done - first arrival) */
   double body_steps;
 } rfmm_server_stats;
 
@@ -347,10 +388,20 @@ enum rfmm_request_state { RFMM_REQ_QUEUED = 0, RFMM_REQ_RUNNING = 1, RFMM_REQ_DO
 
 int rfmm_server_create(const rfmm_server_config *config, rfmm_server **out);
 int rfmm_server_destroy(rfmm_server *server);
-/* Copies the n bodies (n x 32 B); returns RFMM_ERR_BUDGET if n exceeds the
- * slot capacity. */
+/* Copies the n bodies (n x 32 B) before it returns (into a pinned staging
+ * buffer when one is free); returns RFMM_ERR_BUDGET if n exceeds the slot
+ * capacity.  The request's latency runs from the entry into this call. */
 int rfmm_server_submit(rfmm_server *server, const void *host_aos, uint32_t n,
                        const rfmm_params *params, uint32_t steps, uint64_t *request_id);
+/* The same, with the request's arrival time given on rfmm_server_clock's
+ * clock (seconds): latency runs from `arrival_s` instead of the call, so a
+ * load generator replaying an arrival schedule measures from the scheduled
+ * arrival even when its call starts late (no coordinated omission). */
+int rfmm_server_submit_at(rfmm_server *server, const void *host_aos, uint32_t n,
+                          const rfmm_params *params, uint32_t steps, double arrival_s,
+                          uint64_t *request_id);
+/* The server's clock (monotonic seconds). */
+int rfmm_server_clock(double *now_s);
 int rfmm_server_status(rfmm_server *server, uint64_t request_id, int *state);
 /* RFMM_ERR_TIMEOUT if the request is not done within timeout_ms. */
 int rfmm_server_wait(rfmm_server *server, uint64_t request_id, uint32_t timeout_ms);
