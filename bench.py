@@ -58,7 +58,6 @@ from rfmm import workloads  # noqa: E402  (numpy only; the solver library loads 
 PEAKS_FILE = os.path.join(REPO, "MEASURED_PEAKS.json")
 TRAFFIC_FILE = os.path.join(REPO, "profiles", "ncu_traffic.json")
 FALLBACK_HBM_GBS = 6800.0
-P2P_MAX_BODIES = 1 << 18
 REFERENCE_BUDGET_S = 150.0  # the reference arm's whole run
 
 
@@ -83,6 +82,8 @@ def parse_args():
                     help="near field: the reference's cell monopoles, or exact pair sums")
     ap.add_argument("--float", default="exact", choices=["exact", "fast"],
                     help="float variant of the headline run (exact: the oracle's contract)")
+    ap.add_argument("--fmm-steps", type=int, default=0,
+                    help="FMM steps per bench step (0: the workload's own count)")
     return ap.parse_args()
 
 
@@ -351,9 +352,7 @@ def run_gpu_plain(args, w, torch, rfmm, stream, flush, rank, world, local):
     import numpy as np
     from rfmm import replicas, roofline
 
-    n, fmm_steps = w["n"], w["fmm_steps"]
-    if args.near == "p2p" and n > P2P_MAX_BODIES:
-        raise SystemExit("--near p2p: at most %d bodies" % P2P_MAX_BODIES)
+    n, fmm_steps = w["n"], args.fmm_steps or w["fmm_steps"]
     scene = workloads.scene(w)
     params = rfmm.default_params(gravity=w["G"], softening=w["eps"], dt=w["dt"])
     solver = rfmm.Solver(n, params)
@@ -403,8 +402,12 @@ def run_gpu_plain(args, w, torch, rfmm, stream, flush, rank, world, local):
     # Per-phase times inside the graphs, and the work of the tree the run ends on.
     tl, tl_summary = timeline_pass(torch, stream, flush, solver, bench_step, min(args.steps, 5),
                                    fmm_steps, ms_per_step)
-    tw = roofline.tree_work(solver.moments(), solver.depth)
+    mom = solver.moments()
+    tw = roofline.tree_work(mom, solver.depth)
     work = roofline.phase_work(n, tw)
+    if args.near == "p2p":
+        tw["p2p_pairs"] = roofline.p2p_pairs(mom, solver.depth)
+        work["near_p2p"] = {"bytes": 32 * n, "flops": 20 * tw["p2p_pairs"]}
     peak, peak_kind = hbm_peak()
     sm_mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0
     fp32 = roofline.fp32_peak_tflops(torch.cuda.get_device_properties(local).multi_processor_count,

@@ -41,10 +41,12 @@ EncodeTiledFn get_encode_tiled() {
   return fn;
 }
 
-const StepLaunchers kExactLaunchers = {launch_upward, launch_m2l, launch_l2l_near, launch_integrate,
-                                       launch_accel, launch_accel_targets};
-const StepLaunchers kFastLaunchers = {fast::launch_upward, fast::launch_m2l, fast::launch_l2l_near,
-                                      fast::launch_integrate, fast::launch_accel,
+const StepLaunchers kExactLaunchers = {launch_upward,    launch_m2l,      launch_l2l_near,
+                                       launch_integrate, launch_near_p2p, launch_accel,
+                                       launch_accel_targets};
+const StepLaunchers kFastLaunchers = {fast::launch_upward,   fast::launch_m2l,
+                                      fast::launch_l2l_near, fast::launch_integrate,
+                                      fast::launch_near_p2p, fast::launch_accel,
                                       fast::launch_accel_targets};
 
 }  // namespace
@@ -537,6 +539,7 @@ LaunchCtx Engine::ctx(uint32_t mpar, uint32_t lpar, uint32_t ppar) const {
   L.pdl = pdl_;
   L.p2p = near_mode_ == kNearP2P;
   L.pos4 = d_pos4_;
+  L.near4 = d_near4_;
   L.starts_out = d_starts_;
   L.stamps = nullptr;
   return L;
@@ -759,6 +762,7 @@ void Engine::enqueue_step(uint32_t mpar, uint32_t lpar, uint32_t ppar, unsigned 
   K().upward(L, lpar, tasks_);
   K().m2l(L, lpar);
   K().l2l_near(L, lpar);
+  if (near_mode_ == kNearP2P) K().near_p2p(L, tiles_);
   K().integrate(L, tiles_);
   if (near_mode_ == kNearP2P) enqueue_p2p_sort(mpar, lpar, ppar, d_mom_[mpar ^ 1u]);
 }
@@ -783,7 +787,8 @@ int Engine::set_near_mode(uint32_t mode) {
     if (d.key_level < d.depth) return RFMM_ERR_INVALID;
   if (mode == near_mode_) return RFMM_OK;
   if (mode == kNearP2P && d_pos4_ == nullptr) {
-    const int st = alloc((void **)&d_pos4_, 16ull * slots_);
+    int st = alloc((void **)&d_pos4_, 16ull * slots_);
+    if (st == RFMM_OK) st = alloc((void **)&d_near4_, 16ull * slots_);
     if (st != RFMM_OK) return st;
   }
   clear_graphs();
@@ -1026,6 +1031,8 @@ int Engine::phase_times(float ms[7]) {
   RF_CK(cudaEventRecord(ev_[2], stream_));
   K().l2l_near(L, lpar_);
   RF_CK(cudaEventRecord(ev_[3], stream_));
+  if (near_mode_ == kNearP2P) K().near_p2p(L, tiles_);
+  RF_CK(cudaEventRecord(ev_[7], stream_));
   K().integrate(L, tiles_);
   RF_CK(cudaEventRecord(ev_[4], stream_));
   if (near_mode_ == kNearP2P) {
@@ -1041,18 +1048,19 @@ int Engine::phase_times(float ms[7]) {
   since_sort_++;
   const int st = sync();
   if (st != RFMM_OK) return st;
-  float t[5];
+  float t[6];
   RF_CK(cudaEventElapsedTime(&t[0], ev_[5], ev_[6]));
   RF_CK(cudaEventElapsedTime(&t[1], ev_[0], ev_[1]));
   RF_CK(cudaEventElapsedTime(&t[2], ev_[1], ev_[2]));
   RF_CK(cudaEventElapsedTime(&t[3], ev_[2], ev_[3]));
-  RF_CK(cudaEventElapsedTime(&t[4], ev_[3], ev_[4]));
+  RF_CK(cudaEventElapsedTime(&t[5], ev_[3], ev_[7]));
+  RF_CK(cudaEventElapsedTime(&t[4], ev_[7], ev_[4]));
   ms[0] = 0.0f;   // clear: folded into upward
   ms[1] = t[0];   // deposit (standalone P2M; fused into integrate in the step)
   ms[2] = t[1];   // upward
   ms[3] = t[2];   // m2l
   ms[4] = t[3];   // downward (L2L fused with near)
-  ms[5] = 0.0f;   // near: fused into downward
+  ms[5] = near_mode_ == kNearP2P ? t[5] : 0.0f;  // near: fused into downward, or P2P sums
   ms[6] = t[4];   // integrate (+ next deposit)
   return RFMM_OK;
 }
@@ -1090,6 +1098,7 @@ int Engine::profile_steps(uint32_t steps, float ms[kKernelKinds], uint32_t launc
     timed(kKUpward, [&] { K().upward(L, lpar_, tasks_); });
     timed(kKM2L, [&] { K().m2l(L, lpar_); });
     timed(kKL2LNear, [&] { K().l2l_near(L, lpar_); });
+    if (near_mode_ == kNearP2P) timed(kKNearP2P, [&] { K().near_p2p(L, tiles_); });
     timed(kKIntegrate, [&] { K().integrate(L, tiles_); });
     if (near_mode_ == kNearP2P)
       timed(kKResort, [&] { enqueue_p2p_sort(mcur_, lpar_, pcur_, d_mom_[mcur_ ^ 1u]); });

@@ -22,7 +22,8 @@
 namespace rfmm {
 
 // Kernel kinds reported by profile_steps.
-enum KernelKind { kKUpward = 0, kKM2L, kKL2LNear, kKIntegrate, kKResort, kKernelKinds };
+enum KernelKind { kKUpward = 0, kKM2L, kKL2LNear, kKIntegrate, kKResort, kKNearP2P, kKernelKinds };
+static_assert(kKernelKinds == RFMM_KERNEL_KINDS, "kernel kinds of the C ABI");
 
 // Launchers of the kernels whose arithmetic differs between the exact
 // contract and the fast float variant.
@@ -31,6 +32,7 @@ struct StepLaunchers {
   void (*m2l)(const LaunchCtx &, uint32_t);
   void (*l2l_near)(const LaunchCtx &, uint32_t);
   void (*integrate)(const LaunchCtx &, uint32_t);
+  void (*near_p2p)(const LaunchCtx &, uint32_t);
   void (*accel)(const LaunchCtx &, const uint32_t *, float4 *, uint32_t, uint32_t);
   void (*accel_targets)(const LaunchCtx &, uint32_t, uint32_t, uint32_t, const uint32_t *,
                         uint32_t *, const uint32_t *, uint32_t, float4 *);
@@ -116,7 +118,7 @@ class Engine {
   const SceneDesc &scene(uint32_t s) const { return scenes_[s]; }
   size_t buffer_bytes(uint32_t scene, int which) const;
   size_t device_bytes() const { return device_bytes_; }
-  uint32_t kernels_per_step() const { return near_mode_ == kNearP2P ? 4u + p2p_sort_kernels() : 4u; }
+  uint32_t kernels_per_step() const { return near_mode_ == kNearP2P ? 5u + p2p_sort_kernels() : 4u; }
   // Near-field mode of every scene (kNearReference / kNearP2P); a committed
   // state is re-sorted for the new mode.
   int set_near_mode(uint32_t mode);
@@ -148,6 +150,7 @@ class Engine {
   uint32_t float_mode_ = RFMM_FLOAT_EXACT;
   const StepLaunchers &K() const;
   float4 *d_pos4_ = nullptr;      // kNearP2P: leaf-sorted positions
+  float4 *d_near4_ = nullptr;     // kNearP2P: per-slot pair sums of the step
   uint32_t *d_starts_ = nullptr;  // per-leaf start slots (leaf sorts)
   int launch_chunk(uint32_t len, bool sort_at_end);
   int commit_scene(uint32_t scene);

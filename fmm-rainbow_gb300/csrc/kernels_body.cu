@@ -62,12 +62,54 @@ __device__ __forceinline__ void soft_wall(float &p, float &v, float world_edge, 
 
 // Near-field P2P inputs: the leaf-sorted position snapshot, the per-leaf
 // start table (Morton order, absolute slots, 8^depth + 1 entries per scene at
-// the scene's cell offset) and the body's own slot.
+// the scene's cell offset), the body's own slot, and (integrate) the pair
+// sums k_near_p2p already formed for every slot, or null: form them here.
 struct P2PView {
   const float4 *pos;
   const uint32_t *starts;
   uint32_t self;
+  const float4 *near = nullptr;
 };
+
+// The cell a body samples its field from (wgsl:625-639): the first level
+// whose cell holds at most 16 bodies, else the leaf level.  Resolved once per
+// leaf by the upward pass; bodies of unresolved leaves (sparse subtrees)
+// descend here.  Returns the global cell index; `level` and the leaf
+// coordinates (lx, ly, lz) describe it (coordinates at the level are the
+// leaf coordinates shifted right by depth - level).
+__device__ __forceinline__ uint32_t sample_cell(const SceneDesc &S, float px, float py, float pz,
+                                                const uint4 *__restrict__ mom,
+                                                const uint32_t *__restrict__ choice,
+                                                uint32_t &level, uint32_t &lx, uint32_t &ly,
+                                                uint32_t &lz) {
+  const uint32_t D = S.depth;
+  // Leaf coordinates; floor(u * 2^l) == floor(u * 2^D) >> (D - l).
+  const uint32_t dimD = 1u << D;
+  lx = cell_of_unit(unit_coord(px), dimD);
+  ly = cell_of_unit(unit_coord(py), dimD);
+  lz = cell_of_unit(unit_coord(pz), dimD);
+  uint32_t chosen = D, cell_index = 0u;
+  const uint32_t pick = __ldg(&choice[S.cell_off + level_offset_d(D) + lin3_lv(lx, ly, lz, D)]);
+  if (pick != kChoiceUnresolved) {
+    chosen = pick >> 28;
+    cell_index = S.cell_off + (pick & 0x0FFFFFFFu);
+  } else {
+#pragma unroll
+    for (uint32_t l = 6u; l >= 1u; l--) {
+      if (l <= D) {
+        const uint32_t sh = D - l;
+        const uint32_t idx = S.cell_off + level_offset_d(l) + lin3_lv(lx >> sh, ly >> sh, lz >> sh, l);
+        const uint32_t c = __ldg(&mom[idx].x);
+        if ((int32_t)c <= (int32_t)kAdaptive || l == D) {
+          chosen = l;
+          cell_index = idx;
+        }
+      }
+    }
+  }
+  level = chosen;
+  return cell_index;
+}
 
 // Softened pair sums over the bodies of the 3x3x3 cells (level `l`) around
 // cell (cx, cy, cz): cells z-, y-, x-major from -1 to +1, bodies of a cell in
@@ -127,32 +169,8 @@ __device__ __forceinline__ uint32_t body_acceleration(const SceneDesc &S, float 
                                                       float &ay, float &az, float &pulse,
                                                       float *phi, const P2PView *V = nullptr) {
     const uint32_t D = S.depth;
-    // Leaf coordinates; floor(u * 2^l) == floor(u * 2^D) >> (D - l).
-    const uint32_t dimD = 1u << D;
-    const uint32_t lx = cell_of_unit(unit_coord(px), dimD), ly = cell_of_unit(unit_coord(py), dimD),
-                   lz = cell_of_unit(unit_coord(pz), dimD);
-    // Adaptive descent (wgsl:625-639): first level whose cell holds at most
-    // 16 bodies, else the leaf level.  Resolved once per leaf by the upward
-    // pass; bodies of unresolved leaves (sparse subtrees) descend here.
-    uint32_t chosen = D, cell_index = 0u;
-    const uint32_t pick = __ldg(&choice[S.cell_off + level_offset_d(D) + lin3_lv(lx, ly, lz, D)]);
-    if (pick != kChoiceUnresolved) {
-      chosen = pick >> 28;
-      cell_index = S.cell_off + (pick & 0x0FFFFFFFu);
-    } else {
-#pragma unroll
-      for (uint32_t l = 6u; l >= 1u; l--) {
-        if (l <= D) {
-          const uint32_t sh = D - l;
-          const uint32_t idx = S.cell_off + level_offset_d(l) + lin3_lv(lx >> sh, ly >> sh, lz >> sh, l);
-          const uint32_t c = __ldg(&mom[idx].x);
-          if ((int32_t)c <= (int32_t)kAdaptive || l == D) {
-            chosen = l;
-            cell_index = idx;
-          }
-        }
-      }
-    }
+    uint32_t chosen, lx, ly, lz;
+    const uint32_t cell_index = sample_cell(S, px, py, pz, mom, choice, chosen, lx, ly, lz);
     const float4 ax4 = __ldg(&aux[cell_index]);
     const uint32_t count = __float_as_uint(ax4.z);
     const uint32_t csh = D - chosen;
@@ -168,8 +186,15 @@ __device__ __forceinline__ uint32_t body_acceleration(const SceneDesc &S, float 
     az = fa.z + (fj0.z * rx + fj1.x * ry + fj1.y * rz);
 
     if (kP2P) {
-      float sx, sy, sz, sp;
-      p2p_sums<kPhi>(S, *V, chosen, lx >> csh, ly >> csh, lz >> csh, px, py, pz, sx, sy, sz, sp);
+      float sx, sy, sz, sp = 0.0f;
+      if (!kPhi && V->near != nullptr) {
+        const float4 nr = V->near[V->self];
+        sx = nr.x;
+        sy = nr.y;
+        sz = nr.z;
+      } else {
+        p2p_sums<kPhi>(S, *V, chosen, lx >> csh, ly >> csh, lz >> csh, px, py, pz, sx, sy, sz, sp);
+      }
       const float gm = S.gravity / S.n_f;
       ax = ax + gm * sx;
       ay = ay + gm * sy;
@@ -328,6 +353,7 @@ __global__ void __launch_bounds__(256, 6) k_integrate(const SceneDesc *__restric
                                                    Counters *__restrict__ ctr, int dynamic,
                                                    const float4 *__restrict__ pos4,
                                                    const uint32_t *__restrict__ starts,
+                                                   const float4 *__restrict__ near4,
                                                    unsigned long long *__restrict__ stamp) {
   __shared__ DepositTable T;
   __shared__ SceneDesc S;
@@ -374,7 +400,7 @@ __global__ void __launch_bounds__(256, 6) k_integrate(const SceneDesc *__restric
     uint32_t key = DepositTable::kEmpty;
     int32_t qx = 0, qy = 0, qz = 0;
     if (active) {
-      const P2PView V{pos4, starts, slot};
+      const P2PView V{pos4, starts, slot, near4};
       integrate_body<kP2P>(S, p0, p1, mom, src, aux, choice, fields, key, qx, qy, qz, &V);
       part[2u * slot] = p0;
       part[2u * slot + 1u] = p1;
@@ -384,6 +410,168 @@ __global__ void __launch_bounds__(256, 6) k_integrate(const SceneDesc *__restric
   if (!kP2P) {
     __syncthreads();
     T.flush(mom_next);
+  }
+  stamp_end(stamp);
+  grid_dependents_may_launch();
+}
+
+// ------------------------------------------------------------ P2P near field
+//
+// Exact softened pair sums of every body over the bodies of the 3x3x3 cells
+// around its sample cell (kNearP2P), written per slot for the integrate that
+// follows.  Persistent CTAs walk interleaved tiles of 256 leaf-sorted bodies.
+// A tile whose bodies all share one sample cell (the common case: a dense
+// leaf holds thousands of bodies) stages its 27 cells' sources as coalesced
+// float4 chunks in shared memory and every thread reads each source by
+// broadcast; otherwise each warp whose bodies share a sample cell does the
+// same with its own 32-source slice, and the remaining bodies gather their
+// sources themselves.  Every thread sums in the same fixed order (cells z-,
+// y-, x-major, bodies in slot order, itself skipped) whichever way its
+// sources arrive, so the sums equal p2p_sums bit for bit under the exact
+// contract.
+
+// One source's contribution (the expression p2p_sums evaluates).
+__device__ __forceinline__ void p2p_pair(float4 q, float px, float py, float pz, float eps2,
+                                         float &sx, float &sy, float &sz) {
+  const float dx = q.x - px, dy = q.y - py, dz = q.z - pz;
+  const float r2 = ((dx * dx + dy * dy) + dz * dz) + eps2;
+  const float inv = inv_sqrt(r2);
+  const float w = (inv * inv) * inv;
+  sx = sx + dx * w;
+  sy = sy + dy * w;
+  sz = sz + dz * w;
+}
+
+// Sources [lo, hi) through a staging buffer of kWidth float4 shared by the
+// kWidth threads of a group (a CTA or a warp); `sync` orders the group.
+template <uint32_t kWidth, typename Sync>
+__device__ __forceinline__ void p2p_staged_range(const float4 *__restrict__ pos, uint32_t lo,
+                                                 uint32_t hi, float4 *buf, uint32_t rank,
+                                                 uint32_t self, float px, float py, float pz,
+                                                 float eps2, float &sx, float &sy, float &sz,
+                                                 Sync sync) {
+  for (uint32_t base = lo; base < hi; base += kWidth) {
+    sync();  // the previous chunk is consumed
+    if (base + rank < hi) buf[rank] = __ldg(&pos[base + rank]);
+    sync();
+    const uint32_t m = min(kWidth, hi - base);
+    if (self - base < m) {  // this chunk holds the body itself: skip it
+      for (uint32_t k = 0; k < m; k++)
+        if (base + k != self) p2p_pair(buf[k], px, py, pz, eps2, sx, sy, sz);
+    } else {
+#pragma unroll 4
+      for (uint32_t k = 0; k < m; k++) p2p_pair(buf[k], px, py, pz, eps2, sx, sy, sz);
+    }
+  }
+}
+
+// The 27 cells (level l, around (cx, cy, cz)) in the reference order, each as
+// its slot range [lo, hi) of the leaf-sorted bodies.
+template <typename F>
+__device__ __forceinline__ void for_neighbour_ranges(const SceneDesc &S, const uint32_t *starts,
+                                                     uint32_t l, uint32_t cx, uint32_t cy,
+                                                     uint32_t cz, F &&f) {
+  const int dim = 1 << l;
+  const uint32_t sh3 = 3u * (S.depth - l);
+  for (int oz = -1; oz <= 1; oz++) {
+    const int nz = (int)cz + oz;
+    if (nz < 0 || nz >= dim) continue;
+    for (int oy = -1; oy <= 1; oy++) {
+      const int ny = (int)cy + oy;
+      if (ny < 0 || ny >= dim) continue;
+      for (int ox = -1; ox <= 1; ox++) {
+        const int nx = (int)cx + ox;
+        if (nx < 0 || nx >= dim) continue;
+        const uint32_t m = morton3((uint32_t)nx, (uint32_t)ny, (uint32_t)nz);
+        f(__ldg(&starts[S.cell_off + (m << sh3)]), __ldg(&starts[S.cell_off + ((m + 1u) << sh3)]));
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) k_near_p2p(const SceneDesc *__restrict__ scenes,
+                                                  const uint32_t *__restrict__ tile_scene,
+                                                  const float4 *__restrict__ pos4,
+                                                  const uint32_t *__restrict__ starts,
+                                                  const uint4 *__restrict__ mom,
+                                                  const uint32_t *__restrict__ choice,
+                                                  uint32_t tiles,
+                                                  const uint32_t *__restrict__ tile_list,
+                                                  const Counters *__restrict__ ctr,
+                                                  float4 *__restrict__ near_out,
+                                                  unsigned long long *__restrict__ stamp) {
+  __shared__ float4 buf[kTile];
+  __shared__ SceneDesc S;
+  __shared__ uint32_t s_cell[5];  // tid 0's sample cell: key, level, x, y, z
+  const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  grid_dependency_wait();  // the upward pass resolved this step's sample cells
+  stamp_begin(stamp);
+  const uint32_t ntiles = tile_list != nullptr ? min(ctr->tiles_active, tiles) : tiles;
+  uint32_t cur = 0xFFFFFFFFu;
+  for (uint32_t i = blockIdx.x; i < ntiles; i += gridDim.x) {
+    const uint32_t tile = tile_list != nullptr ? tile_list[i] : i;
+    const uint32_t sc = tile_scene[tile];
+    if (sc != cur) {
+      load_scene(S, scenes, sc);  // barriers inside: the previous tile's buffer is free
+      cur = sc;
+    } else {
+      __syncthreads();
+    }
+    const uint32_t slot = tile * kTile + tid;
+    const bool active = slot - S.body_off < S.n;
+    float px = 0.0f, py = 0.0f, pz = 0.0f;
+    uint32_t level = 0u, lx = 0u, ly = 0u, lz = 0u, key = 0xFFFFFFFFu;
+    if (active) {
+      const float4 p = pos4[slot];
+      px = p.x;
+      py = p.y;
+      pz = p.z;
+      key = sample_cell(S, px, py, pz, mom, choice, level, lx, ly, lz);
+    }
+    const uint32_t csh = S.depth - level;
+    if (tid == 0) {  // slot 0 of a tile always holds a body
+      s_cell[0] = key;
+      s_cell[1] = level;
+      s_cell[2] = lx >> csh;
+      s_cell[3] = ly >> csh;
+      s_cell[4] = lz >> csh;
+    }
+    __syncthreads();
+    const float eps2 = S.softening * S.softening;
+    float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+    const bool tile_uniform = __syncthreads_and(!active || key == s_cell[0]) != 0;
+    if (tile_uniform) {
+      // Every thread takes the same branches: tid 0's cell drives the loops.
+      for_neighbour_ranges(S, starts, s_cell[1], s_cell[2], s_cell[3], s_cell[4],
+                           [&](uint32_t lo, uint32_t hi) {
+                             p2p_staged_range<kTile>(pos4, lo, hi, buf, tid, slot, px, py, pz,
+                                                     eps2, sx, sy, sz, [] { __syncthreads(); });
+                           });
+    } else {
+      // Warps whose active bodies share a cell stage their own 32-source slice.
+      const uint32_t amask = __ballot_sync(0xFFFFFFFFu, active);
+      const uint32_t lead = amask != 0u ? (uint32_t)__ffs(amask) - 1u : 0u;
+      const uint32_t wkey = __shfl_sync(0xFFFFFFFFu, key, lead);
+      const bool warp_uniform = __all_sync(0xFFFFFFFFu, !active || key == wkey);
+      if (amask == 0u) {
+        // Padding only: nothing to sum.
+      } else if (warp_uniform) {
+        const uint32_t wl = __shfl_sync(0xFFFFFFFFu, level, lead);
+        const uint32_t wx = __shfl_sync(0xFFFFFFFFu, lx >> csh, lead);
+        const uint32_t wy = __shfl_sync(0xFFFFFFFFu, ly >> csh, lead);
+        const uint32_t wz = __shfl_sync(0xFFFFFFFFu, lz >> csh, lead);
+        float4 *wbuf = buf + 32u * warp;
+        for_neighbour_ranges(S, starts, wl, wx, wy, wz, [&](uint32_t lo, uint32_t hi) {
+          p2p_staged_range<32u>(pos4, lo, hi, wbuf, lane, slot, px, py, pz, eps2, sx, sy, sz,
+                                [] { __syncwarp(); });
+        });
+      } else if (active) {
+        const P2PView V{pos4, starts, slot};
+        float sp;
+        p2p_sums<false>(S, V, level, lx >> csh, ly >> csh, lz >> csh, px, py, pz, sx, sy, sz, sp);
+      }
+    }
+    if (active) near_out[slot] = make_float4(sx, sy, sz, 0.0f);
   }
   stamp_end(stamp);
   grid_dependents_may_launch();
@@ -758,7 +946,14 @@ void launch_integrate(const LaunchCtx &L, uint32_t tiles) {
                      (const float4 *)L.src, (const float4 *)L.aux, (const uint32_t *)L.choice,
                      (const float *)L.fields, L.mom_next, tiles, L.tile_list, L.ctr,
                      L.integrate_dynamic ? 1 : 0, L.pos4, (const uint32_t *)L.starts_out,
-                     stamp_rec(L, 3u));
+                     (const float4 *)L.near4, stamp_rec(L, 3u));
+}
+
+void launch_near_p2p(const LaunchCtx &L, uint32_t tiles) {
+  launch_step_kernel(L, k_near_p2p, dim3(body_grid(L, tiles)), dim3(kTile), 0, L.scenes,
+                     L.tile_scene, (const float4 *)L.pos4, (const uint32_t *)L.starts_out,
+                     (const uint4 *)L.mom, (const uint32_t *)L.choice, tiles, L.tile_list,
+                     (const Counters *)L.ctr, L.near4, stamp_rec(L, 5u));
 }
 
 void launch_deposit(const LaunchCtx &L, uint4 *moments, uint32_t tiles) {

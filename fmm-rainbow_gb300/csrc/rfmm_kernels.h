@@ -58,13 +58,14 @@ struct LaunchCtx {
   bool pdl;                    // launch step kernels with programmatic stream serialization
   bool p2p;                    // near field by exact pair sums (every scene in kNearP2P)
   float4 *pos4;                // leaf-sorted position snapshot (kNearP2P)
+  float4 *near4;               // per-slot P2P pair sums of the step (kNearP2P)
   uint32_t *starts_out;        // per-leaf start table (kNearP2P)
   // Timeline records of this step (2 words per kernel kind, upward, M2L,
-  // L2L + near, integrate, resort), or null: no stamps.
+  // L2L + near, integrate, resort, P2P near field), or null: no stamps.
   unsigned long long *stamps;
 };
 
-// Record of kernel kind `kind` (0..4) within a step's timeline, or null.
+// Record of kernel kind `kind` (0..5) within a step's timeline, or null.
 inline unsigned long long *stamp_rec(const LaunchCtx &L, uint32_t kind) {
   return L.stamps != nullptr ? L.stamps + 2u * kind : nullptr;
 }
@@ -105,6 +106,8 @@ cudaError_t configure_tree_kernels();
 
 // Body passes (kernels_body.cu).
 void launch_integrate(const LaunchCtx &L, uint32_t tiles);
+// kNearP2P: exact near-field pair sums of every body into L.near4.
+void launch_near_p2p(const LaunchCtx &L, uint32_t tiles);
 void launch_deposit(const LaunchCtx &L, uint4 *moments, uint32_t tiles);
 // keys/vals of tiles [tile_base, tile_base + tiles), written from index 0.
 // Body ids (caller order) are written too for every scene (fresh_ids 1) or
@@ -174,6 +177,7 @@ void launch_upward(const LaunchCtx &L, uint32_t list_par, uint32_t tasks);
 void launch_m2l(const LaunchCtx &L, uint32_t list_par);
 void launch_l2l_near(const LaunchCtx &L, uint32_t list_par);
 void launch_integrate(const LaunchCtx &L, uint32_t tiles);
+void launch_near_p2p(const LaunchCtx &L, uint32_t tiles);
 void launch_accel(const LaunchCtx &L, const uint32_t *ids, float4 *out, uint32_t tile_base,
                   uint32_t tiles);
 void launch_accel_targets(const LaunchCtx &L, uint32_t scene, uint32_t tile_base, uint32_t tiles,

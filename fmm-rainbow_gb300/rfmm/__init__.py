@@ -86,11 +86,11 @@ class Tuning(C.Structure):
 class Timeline(C.Structure):
     """`rfmm_timeline` (include/rfmm.h): step kernels as they ran inside the graphs."""
 
-    _fields_ = [("steps", C.c_uint32), ("launches", C.c_uint32 * 5), ("busy_ms", C.c_double * 5),
-                ("gap_ms", C.c_double * 5), ("span_ms", C.c_double)]
+    _fields_ = [("steps", C.c_uint32), ("launches", C.c_uint32 * 6), ("busy_ms", C.c_double * 6),
+                ("gap_ms", C.c_double * 6), ("span_ms", C.c_double)]
 
     def as_dict(self):
-        kinds = ("upward", "m2l", "l2l_near", "integrate", "resort")
+        kinds = KERNEL_KINDS
         return {"steps": self.steps, "span_ms": self.span_ms,
                 "kinds": {k: {"launches": self.launches[i], "busy_ms": self.busy_ms[i],
                               "gap_ms": self.gap_ms[i]} for i, k in enumerate(kinds)}}
@@ -208,7 +208,7 @@ SIGNATURES = {
     "rfmm_server_result": (_i, [_vp, C.c_uint64, _vp, _sz]),
     "rfmm_server_get_stats": (_i, [_vp, C.POINTER(ServerStats)]),
 }
-KERNEL_KINDS = ("upward", "m2l", "l2l_near", "integrate", "resort")
+KERNEL_KINDS = ("upward", "m2l", "l2l_near", "integrate", "resort", "near_p2p")
 
 _lib = None
 

@@ -29,6 +29,9 @@ item once, whatever the kernel's layout):
              moment gathered once) + 16 B per leaf (the next deposit)
   resort     72 B per body (particle and id in and out) + 36 B per leaf
              (leaf count read twice, start slot written)
+  near_p2p   (exact near-field mode) flops: 20 per pair interaction, the
+             usual N-body convention; bytes: 16 B position in and 16 B sums
+             out per body
 """
 from __future__ import annotations
 
@@ -49,7 +52,8 @@ def _grid(counts: np.ndarray, l: int) -> np.ndarray:
 
 
 def _box_sum(nonempty: np.ndarray, lo: np.ndarray, hi: np.ndarray) -> np.ndarray:
-    """Sum of `nonempty` over boxes [lo, hi] (inclusive, per axis, clipped).
+    """Sum of a level grid (occupancy or counts) over boxes [lo, hi]
+    (inclusive, per axis, clipped).
 
     lo/hi are (k, 3) arrays of (z, y, x) corners."""
     d = nonempty.shape[0]
@@ -105,6 +109,30 @@ def tree_work(moments: np.ndarray, depth: int) -> dict:
     return {"depth": D, "cells": cells, "leaves": 8 ** D, "parents": parents, "targets": targets,
             "leaf_targets": leaf_targets, "m2l_pairs": m2l_pairs, "near_pairs": near_pairs,
             "live_subtrees": live_sub, "leaves_live": leaves_live, "upper_live": upper_live}
+
+
+def p2p_pairs(moments: np.ndarray, depth: int) -> int:
+    """Pair interactions of one exact near-field step (RFMM_NEAR_P2P): every
+    body pairs with every other body of the 3x3x3 cells around its sample
+    cell, the first level whose cell holds at most 16 bodies (else the leaf)."""
+    counts = np.ascontiguousarray(moments).view(np.uint32).reshape(-1, 4)[:, 0].astype(np.int64)
+    D = depth
+    leaf = _grid(counts, D)
+    lvl = np.full(leaf.shape, D, np.int64)
+    for l in range(D - 1, 0, -1):  # coarser levels overwrite: the first level from the top wins
+        f = 1 << (D - l)
+        g = _grid(counts, l)
+        up = np.repeat(np.repeat(np.repeat(g, f, 0), f, 1), f, 2)
+        lvl = np.where(up <= ADAPTIVE, l, lvl)
+    pairs = 0
+    for l in range(1, D + 1):
+        sel = (leaf > 0) & (lvl == l)
+        if not sel.any():
+            continue
+        cell = np.argwhere(sel) >> (D - l)
+        box = _box_sum(_grid(counts, l), cell - 1, cell + 1)  # bodies of the 3x3x3 block
+        pairs += int((leaf[sel] * (box - 1)).sum())
+    return pairs
 
 
 def phase_work(n: int, w: dict) -> dict:

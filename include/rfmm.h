@@ -134,7 +134,8 @@ int rfmm_digest(rfmm_handle *h, int which, uint32_t *out);
  * harness's phase order (native/main.rs:468): clear, deposit, upward, m2l,
  * downward, near, integrate.  Fused phases report their time in the first
  * phase of the fusion and 0 in the others: clear is folded into upward,
- * downward carries L2L+near, integrate carries the next step's deposit.
+ * downward carries L2L+near, integrate carries the next step's deposit;
+ * in RFMM_NEAR_P2P mode near carries the exact pair sums.
  * deposit is a standalone P2M of the current positions into a scratch tree
  * (in a step the deposit rides on integrate).  The frame advances the
  * simulation by one step. */
@@ -193,7 +194,8 @@ enum rfmm_kernel_kind {
   RFMM_KERNEL_L2L_NEAR = 2,  /* L2L chain + adaptive-leaf near field */
   RFMM_KERNEL_INTEGRATE = 3, /* L2P + self leaf + kick/drift + next deposit */
   RFMM_KERNEL_RESORT = 4,    /* refresh of the resident leaf order */
-  RFMM_KERNEL_KINDS = 5
+  RFMM_KERNEL_NEAR_P2P = 5,  /* RFMM_NEAR_P2P: exact near-field pair sums */
+  RFMM_KERNEL_KINDS = 6
 };
 
 /* Profiling counterpart of rfmm_step: runs `steps` frames with direct

@@ -114,3 +114,25 @@ def test_switching_back_to_exact_restores_bit_parity(rfmm_mod, oracle_mod):
         s.upload(p)
         s.step(3)
         assert np.array_equal(_bits(s.particles()), _bits(st.particles))
+
+
+def test_fast_p2p_accelerations_within_tolerance(rfmm_mod, oracle_mod):
+    """Exact near-field mode under the fast variant: the tiled pair sums
+    against the oracle's, accelerations relative rms <= 1e-4."""
+    O, R = oracle_mod, rfmm_mod
+    from rfmm import scenes
+    n = 100000
+    p = scenes.plummer(n, seed=9)
+    st = O.OracleState(p, O.make_params(n, gravity=1.0, softening=1e-3, dt=5e-4, near_mode=1))
+    st.solve_fields()
+    ref = st.accelerations()
+    with R.Solver(n, R.default_params(gravity=1.0, softening=1e-3, dt=5e-4)) as s:
+        s.set_near_mode(R.NEAR_P2P)
+        s.set_float_mode(R.FLOAT_FAST)
+        s.upload(p)
+        acc = s.accelerations()[:, :3]
+        s.step(3)
+        assert np.isfinite(s.particles()["pos"]).all()
+    ar = _rel_rms(acc, ref)
+    print("fast p2p n=%d: accelerations rel rms %.3g" % (n, ar))
+    assert ar <= ACCEL_RMS_TOL, ar

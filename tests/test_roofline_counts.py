@@ -57,3 +57,34 @@ def test_tree_work_counts_match_reference_loops(oracle_mod):
         assert w["parents"] == int((st.moments["count"][: (8 ** st.params.depth - 1) // 7] > 16).sum())
         work = roofline.phase_work(n, w)
         assert work["m2l"]["flops"] == 51 * m2l and work["integrate"]["bytes"] > 64 * n
+
+
+def test_p2p_pair_count_matches_direct_count(oracle_mod):
+    """Exact near-field pairs: every body against the bodies of the 3x3x3
+    cells around its sample cell, itself excluded."""
+    O = oracle_mod
+    from rfmm import roofline, scenes
+    for kind, n in (("plummer", 20000), ("uniform", 6000)):
+        p = scenes.make(kind, n, 4)
+        st = O.OracleState(p, O.make_params(n, gravity=1.0, softening=1e-3, dt=5e-4))
+        st.solve_fields()
+        D = st.params.depth
+        samples = st.sample_cells().astype(np.int64)  # global cell index per body
+        counts = st.moments["count"].astype(np.int64)
+        off = lambda l: (8 ** l - 1) // 7  # noqa: E731
+        want = 0
+        for g in samples.tolist():
+            l = next(k for k in range(D + 1) if off(k) <= g < off(k + 1))
+            d = 1 << l
+            c = g - off(l)
+            x, y, z = c % d, (c // d) % d, c // (d * d)
+            tot = 0
+            for dz in (-1, 0, 1):
+                for dy in (-1, 0, 1):
+                    for dx in (-1, 0, 1):
+                        X, Y, Z = x + dx, y + dy, z + dz
+                        if 0 <= X < d and 0 <= Y < d and 0 <= Z < d:
+                            tot += int(counts[off(l) + X + d * (Y + d * Z)])
+            want += tot - 1
+        assert want > 0
+        assert roofline.p2p_pairs(st.moments, D) == want, kind
