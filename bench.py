@@ -78,6 +78,8 @@ def parse_args():
                          "the command profilers capture")
     ap.add_argument("--requests", type=int, default=0, help="served: requests per rate point")
     ap.add_argument("--rates", type=float, nargs="*", default=None, help="served: arrival rates /s")
+    ap.add_argument("--no-plain", action="store_true",
+                    help="served: skip the back-to-back plain solves of the request list")
     ap.add_argument("--near", default="reference", choices=["reference", "p2p"],
                     help="near field: the reference's cell monopoles, or exact pair sums")
     ap.add_argument("--float", default="exact", choices=["exact", "fast"],
@@ -751,14 +753,17 @@ def run_gpu_served(args, w):
                       "requests": count, "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
                       "mean_ms": st["mean_ms"], "max_ms": st["max_ms"],
                       "body_steps_per_s": st["body_steps_per_s"], "wall_s": wall,
-                      "slots": st["slots"], "device_bytes": st["device_bytes"]})
+                      "slots": st["slots"], "device_bytes": st["device_bytes"],
+                      "worker": {k: st[k] for k in ("chunks", "mean_active_slots",
+                                                    "pageable_inputs", "worker_gpu_wait_ms",
+                                                    "worker_host_ms")}})
     clocks = clocks_summary(clk)
 
     # The same request list back to back through plain handles: each request
     # gets its own handle (created and destroyed outside the timer), then its
     # upload, steps and download are timed on the host clock.
     plain_s = 0.0
-    for i in range(count):
+    for i in range(count if not args.no_plain else 0):
         s = rfmm.Solver(int(pool.n[i]), params)
         torch.cuda.synchronize()
         t = time.perf_counter()
@@ -767,7 +772,7 @@ def run_gpu_served(args, w):
         s.particles()
         plain_s += time.perf_counter() - t
         s.close()
-    plain_value = body_steps / plain_s
+    plain_value = body_steps / plain_s if plain_s > 0 else None
     top = max(sweep, key=lambda r: r["body_steps_per_s"])
     line = {
         "metric": "body-steps/s", "value": top["body_steps_per_s"], "unit": "body-steps/s",
@@ -785,7 +790,7 @@ def run_gpu_served(args, w):
                                "requests": count,
                                "timer": "host clock around upload + steps + download per request "
                                         "(handle creation outside)"},
-        "served_over_plain": top["body_steps_per_s"] / plain_value,
+        "served_over_plain": top["body_steps_per_s"] / plain_value if plain_value else None,
         "clocks": clocks,
         "e2e": {"value": top["body_steps_per_s"], "unit": "body-steps/s",
                 "h2d_bytes_per_step": int(np.sum(pool.n) * 32 / count),

@@ -324,6 +324,10 @@ Engine::~Engine() {
     if (ev != nullptr) cudaEventDestroy(ev);
   for (void *p : allocations_) cudaFree(p);
   if (h_ctr_ != nullptr) cudaFreeHost(h_ctr_);
+  for (int b = 0; b < 2; b++) {
+    if (list_pin_[b] != nullptr) cudaFreeHost(list_pin_[b]);
+    if (list_ev_[b] != nullptr) cudaEventDestroy(list_ev_[b]);
+  }
   if (own_stream_ != nullptr) cudaStreamDestroy(own_stream_);
 }
 
@@ -528,6 +532,7 @@ LaunchCtx Engine::ctx(uint32_t mpar, uint32_t lpar, uint32_t ppar) const {
   L.ctr = d_ctr_;
   L.tickets = d_tickets_;
   L.tmaps = d_tmaps_;
+  L.sms = (uint32_t)sms_;
   L.body_ctas = body_ctas_;
   L.tree_ctas = tree_ctas_;
   L.m2l_ctas = (uint32_t)sms_ * tuning_.m2l_ctas_per_sm;
@@ -626,6 +631,34 @@ void Engine::enqueue_resort(uint32_t ppar, uint32_t count_par, unsigned long lon
 }
 
 int Engine::rebuild_lists() {
+  if (use_lists_) {
+    if (list_pin_[0] == nullptr) {
+      for (int b = 0; b < 2; b++) {
+        RF_CK(cudaHostAlloc((void **)&list_pin_[b], 4ull * (2ull + tiles_ + tasks_),
+                            cudaHostAllocDefault));
+        RF_CK(cudaEventCreateWithFlags(&list_ev_[b], cudaEventDisableTiming));
+      }
+    }
+    const uint32_t b = list_buf_;
+    list_buf_ ^= 1u;
+    RF_CK(cudaEventSynchronize(list_ev_[b]));  // the last copy out of this block is done
+    uint32_t *blk = list_pin_[b], *tiles = blk + 2, *tasks = blk + 2 + tiles_;
+    uint32_t nt = 0, nk = 0;
+    for (const SceneDesc &d : scenes_) {
+      if (d.n == 0u) continue;
+      for (uint32_t t = 0; t < pad_tiles(d.n); t++) tiles[nt++] = d.tile_off + t;
+      for (uint32_t t = 0; t < (1u << (3u * d.sub_level)); t++) tasks[nk++] = d.task_off + t;
+    }
+    blk[0] = nt;
+    blk[1] = nk;
+    if (nt != 0u)
+      RF_CK(cudaMemcpyAsync(d_tile_list_, tiles, 4ull * nt, cudaMemcpyHostToDevice, stream_));
+    if (nk != 0u)
+      RF_CK(cudaMemcpyAsync(d_task_list_, tasks, 4ull * nk, cudaMemcpyHostToDevice, stream_));
+    RF_CK(cudaMemcpyAsync(&d_ctr_->tiles_active, blk, 8, cudaMemcpyHostToDevice, stream_));
+    RF_CK(cudaEventRecord(list_ev_[b], stream_));
+    return RFMM_OK;
+  }
   tile_list_h_.clear();
   task_list_h_.clear();
   for (const SceneDesc &d : scenes_) {

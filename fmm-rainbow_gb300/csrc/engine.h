@@ -198,6 +198,15 @@ class Engine {
   float4 *d_aux_ = nullptr;
   uint32_t *d_tile_list_ = nullptr, *d_task_list_ = nullptr;
   std::vector<uint32_t> tile_list_h_, task_list_h_;
+  // Serving engines refresh the active lists often and while kernels are
+  // queued: the lists go to the device from two pinned blocks used in turn
+  // ([count of tiles, count of tasks | tiles_ tiles | tasks_ tasks]), each
+  // with an event marking when its last copy finished.  A pageable source
+  // would make the copy wait for the queued kernels once it outgrows the
+  // driver's staging buffer.
+  uint32_t *list_pin_[2] = {nullptr, nullptr};
+  cudaEvent_t list_ev_[2] = {nullptr, nullptr};
+  uint32_t list_buf_ = 0;
   uint32_t *d_choice_ = nullptr;
   float *d_lfield_ = nullptr, *d_fields_ = nullptr;
   WorkItem *d_plist_[2] = {nullptr, nullptr};

@@ -459,37 +459,54 @@ __device__ __forceinline__ void p2p_staged_range(const float4 *__restrict__ pos,
       for (uint32_t k = 0; k < m; k++)
         if (base + k != self) p2p_pair(buf[k], px, py, pz, eps2, sx, sy, sz);
     } else {
+#ifdef RFMM_FAST_FLOAT
+      // Two partial sums (even and odd sources) give each thread two
+      // independent chains; the fast variant does not keep the reference
+      // summation order.
+      float ax = 0.0f, ay = 0.0f, az = 0.0f, bx = 0.0f, by = 0.0f, bz = 0.0f;
+      uint32_t k = 0;
+#pragma unroll 2
+      for (; k + 1u < m; k += 2u) {
+        p2p_pair(buf[k], px, py, pz, eps2, ax, ay, az);
+        p2p_pair(buf[k + 1u], px, py, pz, eps2, bx, by, bz);
+      }
+      if (k < m) p2p_pair(buf[k], px, py, pz, eps2, ax, ay, az);
+      sx = sx + (ax + bx);
+      sy = sy + (ay + by);
+      sz = sz + (az + bz);
+#else
 #pragma unroll 4
       for (uint32_t k = 0; k < m; k++) p2p_pair(buf[k], px, py, pz, eps2, sx, sy, sz);
+#endif
     }
   }
 }
 
-// The 27 cells (level l, around (cx, cy, cz)) in the reference order, each as
-// its slot range [lo, hi) of the leaf-sorted bodies.
-template <typename F>
-__device__ __forceinline__ void for_neighbour_ranges(const SceneDesc &S, const uint32_t *starts,
-                                                     uint32_t l, uint32_t cx, uint32_t cy,
-                                                     uint32_t cz, F &&f) {
+// Slot range [lo, hi) of neighbour j (0..26, in the reference's z-, y-,
+// x-major order) of cell (cx, cy, cz) at level l; false when j lies outside
+// the grid.
+__device__ __forceinline__ bool neighbour_range(const SceneDesc &S, const uint32_t *starts,
+                                                uint32_t l, uint32_t cx, uint32_t cy, uint32_t cz,
+                                                uint32_t j, uint32_t &lo, uint32_t &hi) {
   const int dim = 1 << l;
+  const int nx = (int)cx + (int)(j % 3u) - 1, ny = (int)cy + (int)((j / 3u) % 3u) - 1,
+            nz = (int)cz + (int)(j / 9u) - 1;
+  if (nx < 0 || ny < 0 || nz < 0 || nx >= dim || ny >= dim || nz >= dim) return false;
   const uint32_t sh3 = 3u * (S.depth - l);
-  for (int oz = -1; oz <= 1; oz++) {
-    const int nz = (int)cz + oz;
-    if (nz < 0 || nz >= dim) continue;
-    for (int oy = -1; oy <= 1; oy++) {
-      const int ny = (int)cy + oy;
-      if (ny < 0 || ny >= dim) continue;
-      for (int ox = -1; ox <= 1; ox++) {
-        const int nx = (int)cx + ox;
-        if (nx < 0 || nx >= dim) continue;
-        const uint32_t m = morton3((uint32_t)nx, (uint32_t)ny, (uint32_t)nz);
-        f(__ldg(&starts[S.cell_off + (m << sh3)]), __ldg(&starts[S.cell_off + ((m + 1u) << sh3)]));
-      }
-    }
-  }
+  const uint32_t m = morton3((uint32_t)nx, (uint32_t)ny, (uint32_t)nz);
+  lo = __ldg(&starts[S.cell_off + (m << sh3)]);
+  hi = __ldg(&starts[S.cell_off + ((m + 1u) << sh3)]);
+  return true;
 }
 
-__global__ void __launch_bounds__(256) k_near_p2p(const SceneDesc *__restrict__ scenes,
+struct CtaSync {
+  __device__ __forceinline__ void operator()() const { __syncthreads(); }
+};
+struct WarpSync {
+  __device__ __forceinline__ void operator()() const { __syncwarp(); }
+};
+
+__global__ void __launch_bounds__(256, 4) k_near_p2p(const SceneDesc *__restrict__ scenes,
                                                   const uint32_t *__restrict__ tile_scene,
                                                   const float4 *__restrict__ pos4,
                                                   const uint32_t *__restrict__ starts,
@@ -542,11 +559,12 @@ __global__ void __launch_bounds__(256) k_near_p2p(const SceneDesc *__restrict__ 
     const bool tile_uniform = __syncthreads_and(!active || key == s_cell[0]) != 0;
     if (tile_uniform) {
       // Every thread takes the same branches: tid 0's cell drives the loops.
-      for_neighbour_ranges(S, starts, s_cell[1], s_cell[2], s_cell[3], s_cell[4],
-                           [&](uint32_t lo, uint32_t hi) {
-                             p2p_staged_range<kTile>(pos4, lo, hi, buf, tid, slot, px, py, pz,
-                                                     eps2, sx, sy, sz, [] { __syncthreads(); });
-                           });
+      for (uint32_t j = 0; j < 27u; j++) {
+        uint32_t lo, hi;
+        if (neighbour_range(S, starts, s_cell[1], s_cell[2], s_cell[3], s_cell[4], j, lo, hi))
+          p2p_staged_range<kTile>(pos4, lo, hi, buf, tid, slot, px, py, pz, eps2, sx, sy, sz,
+                                  CtaSync());
+      }
     } else {
       // Warps whose active bodies share a cell stage their own 32-source slice.
       const uint32_t amask = __ballot_sync(0xFFFFFFFFu, active);
@@ -561,10 +579,12 @@ __global__ void __launch_bounds__(256) k_near_p2p(const SceneDesc *__restrict__ 
         const uint32_t wy = __shfl_sync(0xFFFFFFFFu, ly >> csh, lead);
         const uint32_t wz = __shfl_sync(0xFFFFFFFFu, lz >> csh, lead);
         float4 *wbuf = buf + 32u * warp;
-        for_neighbour_ranges(S, starts, wl, wx, wy, wz, [&](uint32_t lo, uint32_t hi) {
-          p2p_staged_range<32u>(pos4, lo, hi, wbuf, lane, slot, px, py, pz, eps2, sx, sy, sz,
-                                [] { __syncwarp(); });
-        });
+        for (uint32_t j = 0; j < 27u; j++) {
+          uint32_t lo, hi;
+          if (neighbour_range(S, starts, wl, wx, wy, wz, j, lo, hi))
+            p2p_staged_range<32u>(pos4, lo, hi, wbuf, lane, slot, px, py, pz, eps2, sx, sy, sz,
+                                  WarpSync());
+        }
       } else if (active) {
         const P2PView V{pos4, starts, slot};
         float sp;
@@ -949,8 +969,21 @@ void launch_integrate(const LaunchCtx &L, uint32_t tiles) {
                      (const float4 *)L.near4, stamp_rec(L, 3u));
 }
 
+// The P2P grid: one wave of this kernel's resident CTAs (its register
+// budget allows fewer per SM than integrate's), at most one per tile.
+static uint32_t near_p2p_grid(const LaunchCtx &L, uint32_t tiles) {
+  static const uint32_t per_sm = [] {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_near_p2p, kTile, 0) != cudaSuccess || n < 1)
+      n = 1;
+    return (uint32_t)n;
+  }();
+  const uint32_t grid = (L.sms ? L.sms : 1u) * per_sm;
+  return tiles < grid ? tiles : grid;
+}
+
 void launch_near_p2p(const LaunchCtx &L, uint32_t tiles) {
-  launch_step_kernel(L, k_near_p2p, dim3(body_grid(L, tiles)), dim3(kTile), 0, L.scenes,
+  launch_step_kernel(L, k_near_p2p, dim3(near_p2p_grid(L, tiles)), dim3(kTile), 0, L.scenes,
                      L.tile_scene, (const float4 *)L.pos4, (const uint32_t *)L.starts_out,
                      (const uint4 *)L.mom, (const uint32_t *)L.choice, tiles, L.tile_list,
                      (const Counters *)L.ctr, L.near4, stamp_rec(L, 5u));

@@ -47,6 +47,7 @@ struct LaunchCtx {
   Counters *ctr;
   uint32_t *tickets;
   const CUtensorMap *tmaps;    // 8 per scene (levels 0..7; 3..6 used)
+  uint32_t sms;                // multiprocessors of the device
   uint32_t body_ctas;          // persistent grid of the body passes (resident CTAs)
   uint32_t tree_ctas;          // persistent grid of the upward pass
   uint32_t m2l_ctas;           // persistent grid of the M2L pass

@@ -194,6 +194,9 @@ class Server {
   std::vector<double> latencies_ms_;
   double first_submit_ = 0, last_done_ = 0, body_steps_ = 0;
   uint64_t submitted_ = 0, completed_ = 0;
+  // worker counters (written by the worker thread under m_)
+  uint64_t chunks_ = 0, pageable_inputs_ = 0;
+  double active_sum_ = 0, wait_s_ = 0, host_s_ = 0;
 };
 
 int Server::create(const rfmm_server_config &cfg, Server **out) {
@@ -308,7 +311,8 @@ int Server::submit(const void *host, uint32_t n, const rfmm_params *p, uint32_t 
     return RFMM_ERR_BUDGET;
   }
   r->in_ring = in_ring_.alloc(32ull * n);
-  if (r->in_ring == nullptr) r->input.resize(32ull * n);
+  const bool pageable = r->in_ring == nullptr;
+  if (pageable) r->input.resize(32ull * n);
   std::memcpy(r->in_ring != nullptr ? r->in_ring : r->input.data(), host, 32ull * n);
   std::lock_guard<std::mutex> lk(m_);
   if (failure_ != RFMM_OK) {
@@ -317,6 +321,7 @@ int Server::submit(const void *host, uint32_t n, const rfmm_params *p, uint32_t 
     return failure_;
   }
   r->id = next_id_++;
+  if (pageable) pageable_inputs_++;
   r->t_arrival = std::isnan(arrival_s) ? t_entry : arrival_s;
   if (submitted_ == 0 || r->t_arrival < first_submit_) first_submit_ = r->t_arrival;
   submitted_++;
@@ -391,6 +396,8 @@ void Server::worker_loop() {
       to_activate.assign(staged_fifo_.begin(), staged_fifo_.end());
       staged_fifo_.clear();
     }
+    const double t_host0 = now_s();
+    double t_wait = 0.0;
     int st = RFMM_OK;
     for (int s : to_activate) {
       Request *r = slots_[s].req;
@@ -413,7 +420,12 @@ void Server::worker_loop() {
     if (active.empty()) continue;
     // Bounded run-ahead: wait for the chunk enqueued kRunAhead chunks ago.
     cudaEvent_t &slot_ev = ahead[chunks % kRunAhead];
-    if (chunks >= (uint64_t)kRunAhead) cudaEventSynchronize(slot_ev);
+    if (chunks >= (uint64_t)kRunAhead) {
+      const double w0 = now_s();
+      cudaEventSynchronize(slot_ev);
+      t_wait = now_s() - w0;
+    }
+    const size_t n_active = active.size();
     uint32_t chunk = max_chunk_;
     for (int s : active) chunk = std::min(chunk, slots_[s].req->left);
     if (st == RFMM_OK) st = E_->step(chunk);
@@ -434,9 +446,13 @@ void Server::worker_loop() {
       drain_fifo_.push_back(s);
     }
     if (!finished.empty() && st == RFMM_OK) st = E_->refresh_lists();
-    if (st != RFMM_OK) {
+    {
       std::lock_guard<std::mutex> lk(m_);
-      failure_ = st;
+      if (st != RFMM_OK) failure_ = st;
+      chunks_++;
+      active_sum_ += (double)n_active;
+      wait_s_ += t_wait;
+      host_s_ += now_s() - t_host0 - t_wait;
     }
     if (!finished.empty()) cv_.notify_all();
   }
@@ -548,6 +564,11 @@ int Server::stats(rfmm_server_stats *out) {
   }
   if (last_done_ > first_submit_) out->body_steps_per_s = body_steps_ / (last_done_ - first_submit_);
   out->body_steps = body_steps_;
+  out->chunks = chunks_;
+  out->mean_active_slots = chunks_ ? active_sum_ / (double)chunks_ : 0.0;
+  out->pageable_inputs = pageable_inputs_;
+  out->worker_gpu_wait_ms = 1e3 * wait_s_;
+  out->worker_host_ms = 1e3 * host_s_;
   return failure_;
 }
 

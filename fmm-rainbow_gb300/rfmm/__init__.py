@@ -68,7 +68,10 @@ class ServerStats(C.Structure):
                 ("in_flight", C.c_uint64), ("slots", C.c_uint32), ("slot_capacity", C.c_uint32),
                 ("device_bytes", C.c_uint64), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
                 ("mean_ms", C.c_double), ("max_ms", C.c_double),
-                ("body_steps_per_s", C.c_double), ("body_steps", C.c_double)]
+                ("body_steps_per_s", C.c_double), ("body_steps", C.c_double),
+                ("chunks", C.c_uint64), ("mean_active_slots", C.c_double),
+                ("pageable_inputs", C.c_uint64), ("worker_gpu_wait_ms", C.c_double),
+                ("worker_host_ms", C.c_double)]
 
 
 class Tuning(C.Structure):

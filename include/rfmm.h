@@ -384,6 +384,12 @@ typedef struct rfmm_server_stats {
   double p50_ms, p99_ms, mean_ms, max_ms; /* arrival -> result in host memory */
   double body_steps_per_s;                /* completed work / (last done - first arrival) */
   double body_steps;
+  uint64_t chunks;                        /* batched step chunks run */
+  double mean_active_slots;               /* occupied slots per chunk, on average */
+  uint64_t pageable_inputs;               /* requests whose input missed the pinned ring */
+  double worker_gpu_wait_ms;              /* worker time waiting for the GPU (run-ahead bound) */
+  double worker_host_ms;                  /* worker time admitting, refreshing lists, enqueuing
+                                           * steps and retiring slots */
 } rfmm_server_stats;
 
 enum rfmm_request_state { RFMM_REQ_QUEUED = 0, RFMM_REQ_RUNNING = 1, RFMM_REQ_DONE = 2, RFMM_REQ_FAILED = 3 };
