@@ -683,7 +683,7 @@ def run_gpu_served(args, w):
     params = rfmm.default_params(gravity=w["G"], softening=w["eps"], dt=w["dt"])
     rates = args.rates or w["rates"]
     producers, collectors = 8, 4
-    staging = 8 << 30  # pinned host staging of the server (inputs 6 GiB, results 2 GiB)
+    staging = 24 << 30  # pinned host staging of the server (inputs 18 GiB, results 6 GiB)
     body_steps = pool.body_steps()
 
     # Warm-up: module load and graph captures on a small server.
@@ -756,7 +756,8 @@ def run_gpu_served(args, w):
                       "slots": st["slots"], "device_bytes": st["device_bytes"],
                       "worker": {k: st[k] for k in ("chunks", "mean_active_slots",
                                                     "pageable_inputs", "worker_gpu_wait_ms",
-                                                    "worker_host_ms")}})
+                                                    "worker_admit_ms", "worker_lists_ms",
+                                                    "worker_step_ms", "worker_retire_ms")}})
     clocks = clocks_summary(clk)
 
     # The same request list back to back through plain handles: each request

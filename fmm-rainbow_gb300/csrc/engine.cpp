@@ -3,6 +3,7 @@
 #include "rfmm_math.h"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -641,7 +642,11 @@ int Engine::rebuild_lists() {
     }
     const uint32_t b = list_buf_;
     list_buf_ ^= 1u;
-    RF_CK(cudaEventSynchronize(list_ev_[b]));  // the last copy out of this block is done
+    {
+      const auto w0 = std::chrono::steady_clock::now();
+      RF_CK(cudaEventSynchronize(list_ev_[b]));  // the last copy out of this block is done
+      list_wait_s_ += std::chrono::duration<double>(std::chrono::steady_clock::now() - w0).count();
+    }
     uint32_t *blk = list_pin_[b], *tiles = blk + 2, *tasks = blk + 2 + tiles_;
     uint32_t nt = 0, nk = 0;
     for (const SceneDesc &d : scenes_) {

@@ -86,6 +86,8 @@ class Engine {
   // range (slot_scratch), then the slot is emptied.
   int retire(uint32_t scene, bool lists = true);
   int refresh_lists() { return rebuild_lists(); }
+  // Seconds refresh_lists spent waiting for a pinned list block's last copy.
+  double list_wait_seconds() const { return list_wait_s_; }
   float4 *slot_bodies(uint32_t scene) const { return d_part_[pcur_] + 2ull * scenes_[scene].body_off; }
   float4 *slot_scratch(uint32_t scene) const {
     return d_part_[pcur_ ^ 1u] + 2ull * scenes_[scene].body_off;
@@ -207,6 +209,7 @@ class Engine {
   uint32_t *list_pin_[2] = {nullptr, nullptr};
   cudaEvent_t list_ev_[2] = {nullptr, nullptr};
   uint32_t list_buf_ = 0;
+  double list_wait_s_ = 0.0;
   uint32_t *d_choice_ = nullptr;
   float *d_lfield_ = nullptr, *d_fields_ = nullptr;
   WorkItem *d_plist_[2] = {nullptr, nullptr};

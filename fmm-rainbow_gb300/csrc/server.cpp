@@ -196,7 +196,7 @@ class Server {
   uint64_t submitted_ = 0, completed_ = 0;
   // worker counters (written by the worker thread under m_)
   uint64_t chunks_ = 0, pageable_inputs_ = 0;
-  double active_sum_ = 0, wait_s_ = 0, host_s_ = 0;
+  double active_sum_ = 0, wait_s_ = 0, admit_s_ = 0, lists_s_ = 0, step_s_ = 0, retire_s_ = 0;
 };
 
 int Server::create(const rfmm_server_config &cfg, Server **out) {
@@ -384,6 +384,7 @@ void Server::worker_loop() {
   cudaEvent_t ahead[kRunAhead] = {};
   for (auto &ev : ahead) cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
   uint64_t chunks = 0;
+  bool lists_stale = false;  // slots retired since the last list refresh
   for (;;) {
     std::vector<int> to_activate;
     {
@@ -396,8 +397,9 @@ void Server::worker_loop() {
       to_activate.assign(staged_fifo_.begin(), staged_fifo_.end());
       staged_fifo_.clear();
     }
-    const double t_host0 = now_s();
-    double t_wait = 0.0;
+    // Admissions; then one refresh of the active lists covers them and the
+    // retirements of the previous iteration.
+    double t0 = now_s();
     int st = RFMM_OK;
     for (int s : to_activate) {
       Request *r = slots_[s].req;
@@ -416,28 +418,40 @@ void Server::worker_loop() {
         active.push_back(s);
       }
     }
-    if (!to_activate.empty() && st == RFMM_OK) st = E_->refresh_lists();
-    if (active.empty()) continue;
+    double t1 = now_s();
+    const double list_wait0 = E_->list_wait_seconds();
+    if ((lists_stale || !to_activate.empty()) && st == RFMM_OK) {
+      st = E_->refresh_lists();
+      lists_stale = false;
+    }
+    double t2 = now_s();
+    const double list_wait = E_->list_wait_seconds() - list_wait0;
+    if (active.empty()) {
+      std::lock_guard<std::mutex> lk(m_);
+      admit_s_ += t1 - t0;
+      lists_s_ += t2 - t1 - list_wait;
+      wait_s_ += list_wait;
+      continue;
+    }
     // Bounded run-ahead: wait for the chunk enqueued kRunAhead chunks ago.
     cudaEvent_t &slot_ev = ahead[chunks % kRunAhead];
-    if (chunks >= (uint64_t)kRunAhead) {
-      const double w0 = now_s();
-      cudaEventSynchronize(slot_ev);
-      t_wait = now_s() - w0;
-    }
+    if (chunks >= (uint64_t)kRunAhead) cudaEventSynchronize(slot_ev);
+    const double t3 = now_s();
     const size_t n_active = active.size();
     uint32_t chunk = max_chunk_;
     for (int s : active) chunk = std::min(chunk, slots_[s].req->left);
     if (st == RFMM_OK) st = E_->step(chunk);
     if (st == RFMM_OK) st = cuda_status(cudaEventRecord(slot_ev, E_->stream()));
     chunks++;
+    const double t4 = now_s();
     std::vector<int> finished;
     for (int s : active) {
       slots_[s].req->left -= chunk;
       if (slots_[s].req->left == 0u) finished.push_back(s);
     }
     for (int s : finished) {
-      // Unpermute into scratch and empty the slot (lists refreshed below).
+      // Unpermute into scratch and empty the slot; the lists are refreshed
+      // before the next step.
       if (st == RFMM_OK) st = E_->retire((uint32_t)s, false);
       if (st == RFMM_OK) st = cuda_status(cudaEventRecord(slots_[s].ready, E_->stream()));
       active.erase(std::find(active.begin(), active.end(), s));
@@ -445,14 +459,18 @@ void Server::worker_loop() {
       slots_[s].state = kDraining;
       drain_fifo_.push_back(s);
     }
-    if (!finished.empty() && st == RFMM_OK) st = E_->refresh_lists();
+    if (!finished.empty()) lists_stale = true;
+    const double t5 = now_s();
     {
       std::lock_guard<std::mutex> lk(m_);
       if (st != RFMM_OK) failure_ = st;
       chunks_++;
       active_sum_ += (double)n_active;
-      wait_s_ += t_wait;
-      host_s_ += now_s() - t_host0 - t_wait;
+      admit_s_ += t1 - t0;
+      lists_s_ += t2 - t1 - list_wait;
+      wait_s_ += list_wait + (t3 - t2);
+      step_s_ += t4 - t3;
+      retire_s_ += t5 - t4;
     }
     if (!finished.empty()) cv_.notify_all();
   }
@@ -568,7 +586,10 @@ int Server::stats(rfmm_server_stats *out) {
   out->mean_active_slots = chunks_ ? active_sum_ / (double)chunks_ : 0.0;
   out->pageable_inputs = pageable_inputs_;
   out->worker_gpu_wait_ms = 1e3 * wait_s_;
-  out->worker_host_ms = 1e3 * host_s_;
+  out->worker_admit_ms = 1e3 * admit_s_;
+  out->worker_lists_ms = 1e3 * lists_s_;
+  out->worker_step_ms = 1e3 * step_s_;
+  out->worker_retire_ms = 1e3 * retire_s_;
   return failure_;
 }
 

@@ -71,7 +71,8 @@ class ServerStats(C.Structure):
                 ("body_steps_per_s", C.c_double), ("body_steps", C.c_double),
                 ("chunks", C.c_uint64), ("mean_active_slots", C.c_double),
                 ("pageable_inputs", C.c_uint64), ("worker_gpu_wait_ms", C.c_double),
-                ("worker_host_ms", C.c_double)]
+                ("worker_admit_ms", C.c_double), ("worker_lists_ms", C.c_double),
+                ("worker_step_ms", C.c_double), ("worker_retire_ms", C.c_double)]
 
 
 class Tuning(C.Structure):

@@ -387,9 +387,10 @@ typedef struct rfmm_server_stats {
   uint64_t chunks;                        /* batched step chunks run */
   double mean_active_slots;               /* occupied slots per chunk, on average */
   uint64_t pageable_inputs;               /* requests whose input missed the pinned ring */
-  double worker_gpu_wait_ms;              /* worker time waiting for the GPU (run-ahead bound) */
-  double worker_host_ms;                  /* worker time admitting, refreshing lists, enqueuing
-                                           * steps and retiring slots */
+  /* Where the worker thread's time went: waiting for the GPU (the run-ahead
+   * bound and list-buffer reuse), admitting slots (sort + deposit enqueue),
+   * rebuilding the active lists, enqueuing steps, retiring finished slots. */
+  double worker_gpu_wait_ms, worker_admit_ms, worker_lists_ms, worker_step_ms, worker_retire_ms;
 } rfmm_server_stats;
 
 enum rfmm_request_state { RFMM_REQ_QUEUED = 0, RFMM_REQ_RUNNING = 1, RFMM_REQ_DONE = 2, RFMM_REQ_FAILED = 3 };
