@@ -214,7 +214,6 @@ int Engine::create(const std::vector<SceneSpec> &specs, Engine **out) {
   A((void **)&E->d_fields_, 48 * C);
   A((void **)&E->d_ctr_, sizeof(Counters));
   A((void **)&E->d_tickets_, 4 * kTicketStride * specs.size());
-  A((void **)&E->d_top_acc_, 16ull * kTopCells * specs.size());
   A((void **)&E->d_tmaps_, sizeof(CUtensorMap) * 8 * specs.size());
   A((void **)&E->sort_.hist, 4 * 256 * (size_t)sort_tiles(E->slots_));
   A((void **)&E->sort_.totals, 4 * 256);
@@ -279,8 +278,6 @@ int Engine::create(const std::vector<SceneSpec> &specs, Engine **out) {
   if (e == cudaSuccess) e = cudaMemsetAsync(E->d_ctr_, 0, sizeof(Counters), E->stream_);
   if (e == cudaSuccess)
     e = cudaMemsetAsync(E->d_tickets_, 0, 4 * kTicketStride * specs.size(), E->stream_);
-  if (e == cudaSuccess)
-    e = cudaMemsetAsync(E->d_top_acc_, 0, 16ull * kTopCells * specs.size(), E->stream_);
   if (e != cudaSuccess) {
     delete E;
     return cuda_status(e);
@@ -535,7 +532,6 @@ LaunchCtx Engine::ctx(uint32_t mpar, uint32_t lpar, uint32_t ppar) const {
   L.plist_cap = plist_cap_;
   L.ctr = d_ctr_;
   L.tickets = d_tickets_;
-  L.top_acc = d_top_acc_;
   L.tmaps = d_tmaps_;
   L.sms = (uint32_t)sms_;
   L.body_ctas = body_ctas_;
@@ -699,7 +695,6 @@ int Engine::commit_scene(uint32_t scene) {
   RF_CK(cudaMemsetAsync(d_mom_[mcur_ ^ 1u] + d.cell_off, 0, 16ull * d.cells, stream_));
   RF_CK(cudaMemsetAsync(d_src_ + d.cell_off, 0, 16ull * d.cells, stream_));
   RF_CK(cudaMemsetAsync(d_aux_ + d.cell_off, 0, 16ull * d.cells, stream_));
-  RF_CK(cudaMemsetAsync(d_top_acc_ + kTopCells * scene, 0, 16ull * kTopCells, stream_));
   launch_gather(L, sort_.vals[r], d_part_[pcur_], d_ids_[pcur_], d_part_[pcur_ ^ 1u],
                 d_ids_[pcur_ ^ 1u], d_mom_[mcur_], tiles, d.tile_off);
   RF_CK(cudaGetLastError());
@@ -783,7 +778,6 @@ int Engine::commit() {
   RF_CK(cudaMemsetAsync(d_mom_[mcur_ ^ 1u], 0, 16ull * cells_, stream_));
   RF_CK(cudaMemsetAsync(d_src_, 0, 16ull * cells_, stream_));
   RF_CK(cudaMemsetAsync(d_aux_, 0, 16ull * cells_, stream_));
-  RF_CK(cudaMemsetAsync(d_top_acc_, 0, 16ull * kTopCells * scenes_.size(), stream_));
   launch_gather(L, sort_.vals[r], d_part_[pcur_], d_ids_[pcur_], d_part_[pcur_ ^ 1u],
                 d_ids_[pcur_ ^ 1u], d_mom_[mcur_], tiles_, 0u, d_pos4_);
   launches_ += radix_sort_kernels();

@@ -216,7 +216,6 @@ class Engine {
   Counters *h_ctr_ = nullptr;  // pinned host copy of the counters (status reads)
   Counters *d_ctr_ = nullptr;
   uint32_t *d_tickets_ = nullptr;
-  uint4 *d_top_acc_ = nullptr;  // kTopCells per scene: upward's top-level accumulator
   CUtensorMap *d_tmaps_ = nullptr;
   SortScratch sort_{};
   std::vector<void *> allocations_;

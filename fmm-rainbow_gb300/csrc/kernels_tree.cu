@@ -9,10 +9,9 @@
 //
 // GB300 structure:
 //   k_upward     one 256-thread CTA per 8x8x8-leaf subtree reduces four levels
-//                in shared memory, adds its root into the scene's top-cell
-//                accumulator and takes a completion ticket as soon as its
-//                root is known; the last CTA of a scene writes the top cells
-//                (already summed) and their records.  It also writes each cell's source record (centre
+//                in shared memory and takes a completion ticket as soon as
+//                its root is known; the last CTA of a scene finishes the top
+//                levels.  It also writes each cell's source record (centre
 //                of mass, G*m), appends every parent with more than 16 bodies
 //                to the work list, zeroes the leaf level the next integrate
 //                deposits into, and resolves each leaf's sample cell; a few
@@ -88,8 +87,7 @@ __device__ __forceinline__ void upward_task(
     uint4 *__restrict__ mom_next, float4 *__restrict__ src, float4 *__restrict__ aux,
     uint32_t *__restrict__ choice, WorkItem *__restrict__ plist, uint32_t plist_cap,
     Counters *__restrict__ ctr, uint32_t list_par, uint32_t *__restrict__ tickets, uint4 *s0,
-    uint4 *s1, uint4 *s2, uint4 *__restrict__ top_acc, WorkItem *s_items, uint32_t &s_nitems,
-    uint32_t &s_base,
+    uint4 *s1, uint4 *s2, uint4 *s_top, WorkItem *s_items, uint32_t &s_nitems, uint32_t &s_base,
     uint32_t &s_last) {
   const uint32_t tid = threadIdx.x;
   const uint32_t D = S.depth, r = S.sub_level;  // r = D - 3
@@ -142,20 +140,8 @@ __device__ __forceinline__ void upward_task(
       uint4 acc = make_uint4(0u, 0u, 0u, 0u);
       for (uint32_t k = 0; k < 8u; k++) acc = add_moment(acc, s2[k]);
       s2[8] = acc;
+      // The level-r cell the last CTA reads.
       mom[S.cell_off + level_offset_d(r) + lin3(sx, sy, sz, 1u << r)] = acc;
-      // The root's sums go into its ancestors at levels r-1 .. 0 in the
-      // scene's top-cell accumulator (integer adds modulo 2^32: the order
-      // between subtrees does not matter); the completion ticket below
-      // releases them to the scene's last CTA.
-      for (uint32_t l = r; l-- > 0u;) {
-        const uint32_t sh = r - l;
-        uint32_t *a = reinterpret_cast<uint32_t *>(
-            top_acc + kTopCells * scene + level_offset_d(l) + lin3_lv(sx >> sh, sy >> sh, sz >> sh, l));
-        atomicAdd(a + 0, acc.x);
-        atomicAdd(a + 1, acc.y);
-        atomicAdd(a + 2, acc.z);
-        atomicAdd(a + 3, acc.w);
-      }
     }
   }
 
@@ -232,13 +218,25 @@ __device__ __forceinline__ void upward_task(
   }
 
   if (s_last) {
-    // Every live subtree has added its root into the accumulator before its
-    // ticket: the top cells are final.  Their moments and records in one pass
-    // (at most 73 cells), and the accumulator is cleared for the next launch.
+    // Level r has at most 512 cells: stage it (written by other CTAs) via L2.
+    const uint32_t nr = 1u << (3u * r);
+    for (uint32_t i = tid; i < nr; i += blockDim.x)
+      s0[i] = __ldcg(&mom[S.cell_off + level_offset_d(r) + i]);
+    __syncthreads();
+    // Sums of levels r-1 .. 0 into s_top (level l at level_offset(l)), then
+    // their records in one pass.
+    for (int l = (int)r - 1; l >= 0; l--) {
+      const uint32_t nl = 1u << (3u * l);
+      if (tid < nl) {
+        uint32_t x, y, z;
+        cell_coords_lv(tid, (uint32_t)l, x, y, z);
+        const uint4 *child = l + 1 == (int)r ? s0 : s_top + level_offset_d((uint32_t)l + 1u);
+        s_top[level_offset_d((uint32_t)l) + tid] = sum_children(child, x, y, z, 2u << l);
+      }
+      __syncthreads();
+    }
     if (tid < level_offset_d(r)) {  // every cell of levels 0 .. r-1
-      uint4 *ta = top_acc + kTopCells * scene + tid;
-      const uint4 acc = __ldcg(ta);
-      *ta = make_uint4(0u, 0u, 0u, 0u);
+      const uint4 acc = s_top[tid];
       store_cell(S, tid, acc, mom, src, aux);
       if ((int32_t)acc.x > (int32_t)kAdaptive) s_items[atomicAdd(&s_nitems, 1u)] = {scene, tid};
     }
@@ -275,11 +273,11 @@ __global__ void __launch_bounds__(256) k_upward(const SceneDesc *__restrict__ sc
                                                 const WorkItem *__restrict__ plist_prev,
                                                 Counters *__restrict__ ctr, uint32_t list_par,
                                                 uint32_t *__restrict__ tickets, uint32_t clear_ctas,
-                                                uint4 *__restrict__ top_acc,
                                                 unsigned long long *__restrict__ stamp) {
   __shared__ uint4 s0[512];
   __shared__ uint4 s1[64];
   __shared__ uint4 s2[9];     // level D-2, then the subtree root
+  __shared__ uint4 s_top[73];  // levels 0 .. r-1 of the last CTA (r <= 3)
   __shared__ WorkItem s_items[160];  // a subtree's 73 cells + the top levels' 73
   __shared__ uint32_t s_nitems, s_base, s_last;
   __shared__ SceneDesc sS;
@@ -338,7 +336,7 @@ __global__ void __launch_bounds__(256) k_upward(const SceneDesc *__restrict__ sc
       load_scene(sS, scenes, scene);
     }
     upward_task(sS, scene, task - sS.task_off, mom, mom_next, src, aux, choice, plist, plist_cap,
-                ctr, list_par, tickets, s0, s1, s2, top_acc, s_items, s_nitems, s_base, s_last);
+                ctr, list_par, tickets, s0, s1, s2, s_top, s_items, s_nitems, s_base, s_last);
   }
   stamp_end(stamp);
   grid_dependents_may_launch();
@@ -776,7 +774,7 @@ void launch_upward(const LaunchCtx &L, uint32_t list_par, uint32_t tasks) {
   launch_step_kernel(L, k_upward, dim3(grid + clear), dim3(256), 0, L.scenes, L.task_scene,
                      L.task_list, tasks, L.mom, L.mom_next, L.src, L.aux, L.choice, L.fields,
                      L.plist, L.plist_cap, L.plist_prev, L.ctr, list_par, L.tickets, clear,
-                     L.top_acc, stamp_rec(L, 0u));
+                     stamp_rec(L, 0u));
 }
 
 size_t m2l_smem_bytes(bool compact) {

@@ -54,7 +54,6 @@ struct Scratch {
   alignas(16) SceneDesc scene;
   alignas(16) Counters ctr;
   alignas(16) uint32_t tickets[kTicketStride];
-  alignas(16) uint4 top_acc[kTopCells];        // upward's top-level accumulator
   alignas(16) uint32_t tile_scene[kMaxTiles];  // one scene: all zero
   alignas(16) uint32_t task_scene[kMaxTasks];  // one scene: all zero
   alignas(16) float4 part[2 * kMaxBodies];     // padded copy of the caller's bodies
@@ -214,7 +213,6 @@ extern "C" int rfmm_solve_fields_noalloc(const void *device_particles, uint32_t 
   e = cudaMemcpyAsync(&S->scene, &d, sizeof(d), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(&S->ctr, 0, sizeof(Counters), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(S->tickets, 0, sizeof(S->tickets), s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(S->top_acc, 0, sizeof(S->top_acc), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(S->tile_scene, 0, sizeof(S->tile_scene), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(S->task_scene, 0, sizeof(S->task_scene), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(device_moments, 0, 16ull * d.cells, s);
@@ -245,7 +243,6 @@ extern "C" int rfmm_solve_fields_noalloc(const void *device_particles, uint32_t 
   L.plist_cap = kMaxParents;
   L.ctr = &S->ctr;
   L.tickets = S->tickets;
-  L.top_acc = S->top_acc;
   L.tmaps = S->tmaps;
   L.body_ctas = st.body_ctas;
   L.tree_ctas = (uint32_t)st.sms * 6u;

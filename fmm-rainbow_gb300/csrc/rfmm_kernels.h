@@ -46,7 +46,6 @@ struct LaunchCtx {
   uint32_t plist_cap;
   Counters *ctr;
   uint32_t *tickets;
-  uint4 *top_acc;              // kTopCells per scene, zero between upward launches
   const CUtensorMap *tmaps;    // 8 per scene (levels 0..7; 3..6 used)
   uint32_t sms;                // multiprocessors of the device
   uint32_t body_ctas;          // persistent grid of the body passes (resident CTAs)

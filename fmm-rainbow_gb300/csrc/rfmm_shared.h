@@ -20,10 +20,6 @@ constexpr uint32_t kTile = 256u;
 constexpr uint32_t kTicketGroup = 64u;
 constexpr uint32_t kTicketStride = 16u;  // 1 + up to 8 groups (512 subtrees at depth 6)
 
-// Cells above the 8x8x8-leaf subtrees (levels 0 .. depth-4; at most 73 for
-// depth 6): per scene, an accumulator the live subtrees add their roots into.
-constexpr uint32_t kTopCells = 73u;
-
 constexpr uint32_t kNearReference = 0u;
 constexpr uint32_t kNearP2P = 1u;
 

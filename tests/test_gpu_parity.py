@@ -189,12 +189,17 @@ def test_golden_digests_on_gpu(rfmm_mod, oracle_mod):
     import make_golden
     R, O = rfmm_mod, oracle_mod
     gold = json.load(open(os.path.join(here, "golden", "oracle_digests.json")))
-    checked = 0
+    checked, galaxies, skipped = 0, 0, []
     for name, g in sorted(gold.items()):
         galaxy = g["kind"] == "galaxy"
+        galaxies += galaxy
         p = None if galaxy else make_golden.scene(g["kind"], g["n"], g["seed"])
         if not galaxy and O.fnv1a(p) != g["input_particles"]:
-            continue  # this platform's numpy scene generator differs in the last bits
+            # This platform's numpy scene generator differs in the last bits:
+            # the frozen digests do not apply to these inputs (the live
+            # oracle comparisons in this file still cover them).
+            skipped.append(name)
+            continue
         prm = R.default_params(gravity=g["gravity"], softening=g["softening"], dt=g["dt"])
         with R.Solver(g["n"], prm) as s:
             if galaxy:  # seeded on the GPU
@@ -212,7 +217,11 @@ def test_golden_digests_on_gpu(rfmm_mod, oracle_mod):
             assert s.digest(R.BUF_MOMENTS) == g["step_moments"], name
             assert s.digest(R.BUF_FIELDS) == g["step_fields"], name
         checked += 1
-    assert checked >= 1
+    if skipped:
+        import warnings
+        warnings.warn("golden entries with platform-dependent inputs not checked: %s" % skipped)
+    # The GPU-seeded galaxies do not depend on the host's numpy: always checked.
+    assert galaxies >= 1 and checked >= galaxies, (checked, galaxies, skipped)
 
 
 def test_tuning_never_changes_results(rfmm_mod, oracle_mod):
