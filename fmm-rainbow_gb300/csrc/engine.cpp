@@ -329,6 +329,8 @@ Engine::~Engine() {
     if (list_pin_[b] != nullptr) cudaFreeHost(list_pin_[b]);
     if (list_ev_[b] != nullptr) cudaEventDestroy(list_ev_[b]);
   }
+  if (map_pin_ != nullptr) cudaFreeHost(map_pin_);
+  if (map_ev_ != nullptr) cudaEventDestroy(map_ev_);
   if (own_stream_ != nullptr) cudaStreamDestroy(own_stream_);
 }
 
@@ -707,8 +709,7 @@ int Engine::commit_scene(uint32_t scene) {
   return RFMM_OK;
 }
 
-int Engine::activate(uint32_t scene, uint32_t n, const rfmm_params &p, const void *src,
-                     cudaMemcpyKind kind, bool lists) {
+int Engine::slot_desc(uint32_t scene, uint32_t n, const rfmm_params &p) {
   if (scene >= scenes_.size() || n == 0u) return RFMM_ERR_INVALID;
   SceneDesc &d = scenes_[scene];
   if (d.n != 0u) return RFMM_ERR_STATE;
@@ -731,6 +732,14 @@ int Engine::activate(uint32_t scene, uint32_t n, const rfmm_params &p, const voi
     d.control_axis_mode[k] = p.control_axis_mode[k];
   }
   RF_CK(cudaMemcpyAsync(d_scenes_ + scene, &d, sizeof(SceneDesc), cudaMemcpyHostToDevice, stream_));
+  return RFMM_OK;
+}
+
+int Engine::activate(uint32_t scene, uint32_t n, const rfmm_params &p, const void *src,
+                     cudaMemcpyKind kind, bool lists) {
+  const int sd = slot_desc(scene, n, p);
+  if (sd != RFMM_OK) return sd;
+  const SceneDesc &d = scenes_[scene];
   if (src != nullptr)  // null: the caller already staged the bodies at slot_bodies(scene)
     RF_CK(cudaMemcpyAsync(d_part_[pcur_] + 2ull * d.body_off, src, 32ull * n, kind, stream_));
   launch_iota(stream_, d_ids_[pcur_] + d.body_off, pad_tiles(n) * kTile);
@@ -741,6 +750,75 @@ int Engine::activate(uint32_t scene, uint32_t n, const rfmm_params &p, const voi
   uploaded_[scene] = true;
   committed_ = true;
   return lists ? rebuild_lists() : RFMM_OK;
+}
+
+int Engine::activate_many(const std::vector<Admission> &admissions) {
+  if (admissions.empty()) return RFMM_OK;
+  if (admissions.size() == 1u) {
+    const Admission &a = admissions[0];
+    return activate(a.scene, a.n, a.params, nullptr, cudaMemcpyDeviceToDevice, false);
+  }
+  // Ascending slot order: the sort (scene rank above the Morton code) returns
+  // the slots' keys in the same order, so sorted position i belongs to map
+  // tile i / 256.
+  std::vector<Admission> adm(admissions);
+  std::sort(adm.begin(), adm.end(),
+            [](const Admission &x, const Admission &y) { return x.scene < y.scene; });
+  for (size_t i = 1; i < adm.size(); i++)
+    if (adm[i].scene == adm[i - 1].scene) return RFMM_ERR_INVALID;
+  for (const Admission &a : adm) {  // validate all before changing any slot
+    if (a.scene >= scenes_.size() || a.n == 0u) return RFMM_ERR_INVALID;
+    const SceneDesc &d = scenes_[a.scene];
+    if (d.n != 0u) return RFMM_ERR_STATE;
+    const uint32_t depth = a.params.depth ? a.params.depth : depth_for_particles(a.n);
+    if (a.n > d.tile_cap * kTile || depth < 4u || depth > d.max_depth) return RFMM_ERR_BUDGET;
+  }
+  for (const Admission &a : adm) {
+    const int sd = slot_desc(a.scene, a.n, a.params);
+    if (sd != RFMM_OK) return sd;
+  }
+  if (map_pin_ == nullptr) {
+    RF_CK(cudaHostAlloc((void **)&map_pin_, 4ull * tiles_, cudaHostAllocDefault));
+    RF_CK(cudaEventCreateWithFlags(&map_ev_, cudaEventDisableTiming));
+    const int st = alloc((void **)&d_map_, 4ull * tiles_);
+    if (st != RFMM_OK) return st;
+  }
+  RF_CK(cudaEventSynchronize(map_ev_));  // the previous map copy is done with the block
+  uint32_t total = 0;
+  for (const Admission &a : adm) {
+    const SceneDesc &d = scenes_[a.scene];
+    for (uint32_t t = 0; t < pad_tiles(d.n); t++) map_pin_[total++] = d.tile_off + t;
+  }
+  RF_CK(cudaMemcpyAsync(d_map_, map_pin_, 4ull * total, cudaMemcpyHostToDevice, stream_));
+  RF_CK(cudaEventRecord(map_ev_, stream_));
+  LaunchCtx L = ctx(mcur_, lpar_, pcur_);
+  // Keys of every admitted slot (numbering its bodies in caller order), one
+  // sort, cleared trees, one gather with the leaf deposit, bodies back into
+  // the current buffer.
+  launch_keys(L, sort_.keys[0], sort_.vals[0], d_ids_[pcur_], 1, total, 0u, nullptr, d_map_);
+  const int r = radix_sort(stream_, sort_, total * kTile, key_bits_);
+  for (const Admission &a : adm) {
+    const SceneDesc &d = scenes_[a.scene];
+    RF_CK(cudaMemsetAsync(d_mom_[mcur_] + d.cell_off, 0, 16ull * d.cells, stream_));
+    RF_CK(cudaMemsetAsync(d_mom_[mcur_ ^ 1u] + d.cell_off, 0, 16ull * d.cells, stream_));
+    RF_CK(cudaMemsetAsync(d_src_ + d.cell_off, 0, 16ull * d.cells, stream_));
+    RF_CK(cudaMemsetAsync(d_aux_ + d.cell_off, 0, 16ull * d.cells, stream_));
+  }
+  launch_gather(L, sort_.vals[r], d_part_[pcur_], d_ids_[pcur_], d_part_[pcur_ ^ 1u],
+                d_ids_[pcur_ ^ 1u], d_mom_[mcur_], total, 0u, nullptr, d_map_);
+  RF_CK(cudaGetLastError());
+  for (const Admission &a : adm) {
+    const SceneDesc &d = scenes_[a.scene];
+    const uint32_t tiles = pad_tiles(d.n);
+    RF_CK(cudaMemcpyAsync(d_part_[pcur_] + 2ull * d.body_off, d_part_[pcur_ ^ 1u] + 2ull * d.body_off,
+                          32ull * tiles * kTile, cudaMemcpyDeviceToDevice, stream_));
+    RF_CK(cudaMemcpyAsync(d_ids_[pcur_] + d.body_off, d_ids_[pcur_ ^ 1u] + d.body_off,
+                          4ull * tiles * kTile, cudaMemcpyDeviceToDevice, stream_));
+    uploaded_[a.scene] = true;
+  }
+  launches_ += 2u + 3u * ((key_bits_ + 7u) / 8u);
+  committed_ = true;
+  return RFMM_OK;
 }
 
 int Engine::retire(uint32_t scene, bool lists) {

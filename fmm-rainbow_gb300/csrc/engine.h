@@ -86,6 +86,15 @@ class Engine {
   // range (slot_scratch), then the slot is emptied.
   int retire(uint32_t scene, bool lists = true);
   int refresh_lists() { return rebuild_lists(); }
+  // Serving: several requests into empty slots at once (bodies already staged
+  // at slot_bodies): one key pass, one radix sort and one gather with deposit
+  // for all of them (their keys concatenated in slot order), instead of a
+  // sort per slot.  Lists are left for refresh_lists().
+  struct Admission {
+    uint32_t scene, n;
+    rfmm_params params;
+  };
+  int activate_many(const std::vector<Admission> &admissions);
   // Seconds refresh_lists spent waiting for a pinned list block's last copy.
   double list_wait_seconds() const { return list_wait_s_; }
   float4 *slot_bodies(uint32_t scene) const { return d_part_[pcur_] + 2ull * scenes_[scene].body_off; }
@@ -156,6 +165,10 @@ class Engine {
   uint32_t *d_starts_ = nullptr;  // per-leaf start slots (leaf sorts)
   int launch_chunk(uint32_t len, bool sort_at_end);
   int commit_scene(uint32_t scene);
+  int slot_desc(uint32_t scene, uint32_t n, const rfmm_params &p);  // fill a free slot's descriptor
+  uint32_t *map_pin_ = nullptr;   // activate_many: pinned tile map (tiles_ entries)
+  uint32_t *d_map_ = nullptr;     // its device copy
+  cudaEvent_t map_ev_ = nullptr;  // the last copy out of map_pin_
   int rebuild_lists();
   int check_device_error();
 

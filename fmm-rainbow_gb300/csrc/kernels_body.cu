@@ -730,8 +730,9 @@ __global__ void __launch_bounds__(256) k_keys(const SceneDesc *__restrict__ scen
                                               uint32_t *__restrict__ keys, uint32_t *__restrict__ vals,
                                               uint32_t *__restrict__ ids, int fresh_ids,
                                               uint32_t tile_base,
-                                              const __grid_constant__ SceneMask fresh) {
-  const uint32_t tile = tile_base + blockIdx.x;
+                                              const __grid_constant__ SceneMask fresh,
+                                              const uint32_t *__restrict__ tile_map) {
+  const uint32_t tile = tile_map != nullptr ? tile_map[blockIdx.x] : tile_base + blockIdx.x;
   const uint32_t sc = tile_scene[tile];
   const SceneDesc &S = scenes[sc];
   const uint32_t slot = tile * kTile + threadIdx.x;
@@ -770,11 +771,14 @@ __global__ void __launch_bounds__(256) k_gather(const SceneDesc *__restrict__ sc
                                                 float4 *__restrict__ part_out,
                                                 uint32_t *__restrict__ ids_out,
                                                 uint4 *__restrict__ deposit_into, uint32_t tiles,
-                                                uint32_t tile_base, float4 *__restrict__ pos_out) {
+                                                uint32_t tile_base, float4 *__restrict__ pos_out,
+                                                const uint32_t *__restrict__ tile_map) {
   __shared__ DepositTable T;
   __shared__ SceneDesc S;
   // Slots [tile_base * 256, (tile_base + tiles) * 256) are permuted among
-  // themselves; perm is relative to tile_base and holds absolute slots.
+  // themselves; perm is relative to tile_base and holds absolute slots.  With
+  // a tile map, output tile i is tile_map[i] and each scene's tiles are
+  // permuted among themselves.
   const uint32_t lo = tile_base * kTile, hi = (tile_base + tiles) * kTile;
   uint32_t t0 = blockIdx.x, t1 = blockIdx.x + 1u;
   if (deposit_into != nullptr) {
@@ -783,10 +787,12 @@ __global__ void __launch_bounds__(256) k_gather(const SceneDesc *__restrict__ sc
   }
   uint32_t cur = 0xFFFFFFFFu;
   for (uint32_t i = t0; i < t1; i++) {
-    const uint32_t tile = tile_base + i;
+    const uint32_t tile = tile_map != nullptr ? tile_map[i] : tile_base + i;
     const uint32_t slot = tile * kTile + threadIdx.x;
     uint32_t from = perm[i * kTile + threadIdx.x];
-    if (from < lo || from >= hi) from = slot;  // defensive: a permutation never leaves the range
+    // Defensive: a permutation never leaves its range (or its scene).
+    if (tile_map != nullptr ? tile_scene[from / kTile] != tile_scene[tile] : (from < lo || from >= hi))
+      from = slot;
     const float4 p0 = part_in[2u * from], p1 = part_in[2u * from + 1u];
     part_out[2u * slot] = p0;
     part_out[2u * slot + 1u] = p1;
@@ -995,18 +1001,19 @@ void launch_deposit(const LaunchCtx &L, uint4 *moments, uint32_t tiles) {
 }
 
 void launch_keys(const LaunchCtx &L, uint32_t *keys, uint32_t *vals, uint32_t *ids, int fresh_ids,
-                 uint32_t tiles, uint32_t tile_base, const SceneMask *fresh) {
+                 uint32_t tiles, uint32_t tile_base, const SceneMask *fresh,
+                 const uint32_t *tile_map) {
   static const SceneMask kNone{};
   k_keys<<<tiles, kTile, 0, L.stream>>>(L.scenes, L.tile_scene, L.part, keys, vals, ids, fresh_ids,
-                                        tile_base, fresh != nullptr ? *fresh : kNone);
+                                        tile_base, fresh != nullptr ? *fresh : kNone, tile_map);
 }
 
 void launch_gather(const LaunchCtx &L, const uint32_t *perm, const float4 *part_in,
                    const uint32_t *ids_in, float4 *part_out, uint32_t *ids_out, uint4 *deposit_into,
-                   uint32_t tiles, uint32_t tile_base, float4 *pos_out) {
+                   uint32_t tiles, uint32_t tile_base, float4 *pos_out, const uint32_t *tile_map) {
   const uint32_t grid = deposit_into != nullptr ? body_grid(L, tiles) : tiles;
   k_gather<<<grid, kTile, 0, L.stream>>>(L.scenes, L.tile_scene, perm, part_in, ids_in, part_out,
-                                         ids_out, deposit_into, tiles, tile_base, pos_out);
+                                         ids_out, deposit_into, tiles, tile_base, pos_out, tile_map);
 }
 
 // Per-leaf body ranges of the leaf-sorted scenes (kNearP2P): entry m of a

@@ -113,13 +113,18 @@ void launch_deposit(const LaunchCtx &L, uint4 *moments, uint32_t tiles);
 // keys/vals of tiles [tile_base, tile_base + tiles), written from index 0.
 // Body ids (caller order) are written too for every scene (fresh_ids 1) or
 // for the scenes set in *fresh (fresh_ids 2).
+// With `tile_map` (device, `tiles` entries) the tiles are tile_map[0 ..]
+// instead of [tile_base, tile_base + tiles).
 void launch_keys(const LaunchCtx &L, uint32_t *keys, uint32_t *vals, uint32_t *ids, int fresh_ids,
-                 uint32_t tiles, uint32_t tile_base, const SceneMask *fresh = nullptr);
-// Permute the bodies of tiles [tile_base, tile_base + tiles) (perm from index 0).
+                 uint32_t tiles, uint32_t tile_base, const SceneMask *fresh = nullptr,
+                 const uint32_t *tile_map = nullptr);
+// Permute the bodies of tiles [tile_base, tile_base + tiles) (perm from index 0),
+// or of the tiles tile_map[0 ..] (each scene's tiles among themselves).
 // With `pos_out`, also writes each permuted body's position float4 there.
 void launch_gather(const LaunchCtx &L, const uint32_t *perm, const float4 *part_in,
                    const uint32_t *ids_in, float4 *part_out, uint32_t *ids_out, uint4 *deposit_into,
-                   uint32_t tiles, uint32_t tile_base, float4 *pos_out = nullptr);
+                   uint32_t tiles, uint32_t tile_base, float4 *pos_out = nullptr,
+                   const uint32_t *tile_map = nullptr);
 // Leaf start tables of every kNearP2P scene from the sorted keys.
 void launch_leaf_starts(const LaunchCtx &L, const uint32_t *sorted_keys, uint32_t scenes);
 void launch_unpermute(const LaunchCtx &L, const uint32_t *ids, float4 *out, uint32_t tile_base,

@@ -401,21 +401,26 @@ void Server::worker_loop() {
     // retirements of the previous iteration.
     double t0 = now_s();
     int st = RFMM_OK;
-    for (int s : to_activate) {
-      Request *r = slots_[s].req;
-      st = E_->activate((uint32_t)s, r->n, r->params, nullptr, cudaMemcpyDeviceToDevice, false);
+    if (!to_activate.empty()) {
+      // Every staged slot admitted with one sort.
+      std::vector<Engine::Admission> adm;
+      for (int s : to_activate) adm.push_back({(uint32_t)s, slots_[s].req->n, slots_[s].req->params});
+      st = E_->activate_many(adm);
       std::lock_guard<std::mutex> lk(m_);
-      if (st != RFMM_OK) {
-        r->state = kFailed;
-        r->status = st;
-        slots_[s].state = kFree;
-        slots_[s].req = nullptr;
-        failure_ = st;
-      } else {
-        slots_[s].state = kActive;
-        r->state = kRunning;
-        r->t_admit = now_s();
-        active.push_back(s);
+      for (int s : to_activate) {
+        Request *r = slots_[s].req;
+        if (st != RFMM_OK) {
+          r->state = kFailed;
+          r->status = st;
+          slots_[s].state = kFree;
+          slots_[s].req = nullptr;
+          failure_ = st;
+        } else {
+          slots_[s].state = kActive;
+          r->state = kRunning;
+          r->t_admit = now_s();
+          active.push_back(s);
+        }
       }
     }
     double t1 = now_s();
