@@ -757,7 +757,8 @@ def run_gpu_served(args, w):
                       "worker": {k: st[k] for k in ("chunks", "mean_active_slots",
                                                     "pageable_inputs", "worker_gpu_wait_ms",
                                                     "worker_admit_ms", "worker_lists_ms",
-                                                    "worker_step_ms", "worker_retire_ms")}})
+                                                    "worker_step_ms", "worker_retire_ms",
+                                                    "gpu_step_ms", "gpu_between_ms")}})
     clocks = clocks_summary(clk)
 
     # The same request list back to back through plain handles: each request

@@ -199,6 +199,7 @@ int Engine::create(const std::vector<SceneSpec> &specs, Engine **out) {
   A((void **)&E->d_task_scene_, 4 * E->tasks_);
   A((void **)&E->d_tile_list_, 4 * E->tiles_);
   A((void **)&E->d_task_list_, 4 * E->tasks_);
+  A((void **)&E->d_scene_list_, 4 * specs.size());
   for (int b = 0; b < 2; b++) {
     A((void **)&E->d_part_[b], 32 * S);
     A((void **)&E->d_ids_[b], 4 * S);
@@ -248,12 +249,17 @@ int Engine::create(const std::vector<SceneSpec> &specs, Engine **out) {
     t.l2l_ctas_per_sm = 5;
     t.integrate_ctas_per_sm = E->body_limit_;
     t.integrate_dynamic = 0;
-    t.resort_interval = E->use_lists_ ? 0u : 16u;  // slots are sorted when they are filled
+    t.resort_interval = 16u;
     t.graph_steps = 16;
     t.pdl = 1;
     // The compacting M2L variant evaluates only the contributing stencil
     // slots; measured faster for one scene and for many.
     t.m2l_compact = 1u;
+    // Warp-per-subtree and lane-per-target paths when the work lists are
+    // long (many scenes), the CTA- and warp-per-item paths otherwise.
+    t.m2l_lanes = 2u;
+    t.l2l_lanes = 2u;
+    t.upward_warps = 2u;
     if (e == cudaSuccess) e = E->set_tuning(t) == RFMM_OK ? cudaSuccess : cudaErrorInvalidValue;
   }
   if (e == cudaSuccess)
@@ -329,8 +335,14 @@ Engine::~Engine() {
     if (list_pin_[b] != nullptr) cudaFreeHost(list_pin_[b]);
     if (list_ev_[b] != nullptr) cudaEventDestroy(list_ev_[b]);
   }
-  if (map_pin_ != nullptr) cudaFreeHost(map_pin_);
-  if (map_ev_ != nullptr) cudaEventDestroy(map_ev_);
+  for (int b = 0; b < 2; b++) {
+    if (scene_pin_[b] != nullptr) cudaFreeHost(scene_pin_[b]);
+    if (scene_ev_[b] != nullptr) cudaEventDestroy(scene_ev_[b]);
+    for (MapBlock *m : {&admit_map_, &retire_map_}) {
+      if (m->pin[b] != nullptr) cudaFreeHost(m->pin[b]);
+      if (m->ev[b] != nullptr) cudaEventDestroy(m->ev[b]);
+    }
+  }
   if (own_stream_ != nullptr) cudaStreamDestroy(own_stream_);
 }
 
@@ -436,7 +448,8 @@ int Engine::set_tuning(const rfmm_tuning &t) {
   if (t.upward_ctas_per_sm < 1u || t.upward_ctas_per_sm > 16u || t.m2l_ctas_per_sm < 1u ||
       t.m2l_ctas_per_sm > 6u || t.l2l_ctas_per_sm < 1u || t.l2l_ctas_per_sm > 8u ||
       t.integrate_ctas_per_sm < 1u || t.integrate_ctas_per_sm > body_limit_ || t.graph_steps < 1u ||
-      t.graph_steps > 64u || t.integrate_dynamic > 1u || t.pdl > 1u || t.m2l_compact > 1u)
+      t.graph_steps > 64u || t.integrate_dynamic > 1u || t.pdl > 1u || t.m2l_compact > 1u ||
+      t.m2l_lanes > 2u || t.l2l_lanes > 2u || t.upward_warps > 2u)
     return RFMM_ERR_INVALID;
   clear_graphs();  // captured launch shapes change
   tuning_ = t;
@@ -475,7 +488,7 @@ int Engine::autotune(uint32_t steps_per_trial, rfmm_tuning *best) {
   int st = trial(cur, &cur_ms);
   // Coordinate descent, two sweeps over the knobs.
   for (int sweep = 0; sweep < 2 && st == RFMM_OK; sweep++) {
-    for (int knob = 0; knob < 9 && st == RFMM_OK; knob++) {
+    for (int knob = 0; knob < 12 && st == RFMM_OK; knob++) {
       std::vector<uint32_t> values;
       switch (knob) {
         case 0: values = {2, 4, 6, 8}; break;
@@ -486,15 +499,19 @@ int Engine::autotune(uint32_t steps_per_trial, rfmm_tuning *best) {
         case 5: values = {0, 1}; break;
         case 6: values = {4, 8, 16, 32}; break;
         case 7:
-          if (!use_lists_) values = {8, 16, 32, 64};  // serving slots are sorted on admission
+          values = {8, 16, 32, 64};
           break;
         case 8: values = {0, 1}; break;
+        case 9: values = {0, 1, 2}; break;
+        case 10: values = {0, 1, 2}; break;
+        case 11: values = {0, 1, 2}; break;
       }
       for (uint32_t v : values) {
         rfmm_tuning t = cur;
-        uint32_t *field[9] = {&t.upward_ctas_per_sm, &t.m2l_ctas_per_sm, &t.l2l_ctas_per_sm,
-                              &t.integrate_ctas_per_sm, &t.integrate_dynamic, &t.pdl,
-                              &t.graph_steps, &t.resort_interval, &t.m2l_compact};
+        uint32_t *field[12] = {&t.upward_ctas_per_sm, &t.m2l_ctas_per_sm, &t.l2l_ctas_per_sm,
+                               &t.integrate_ctas_per_sm, &t.integrate_dynamic, &t.pdl,
+                               &t.graph_steps, &t.resort_interval, &t.m2l_compact,
+                               &t.m2l_lanes, &t.l2l_lanes, &t.upward_warps};
         if (*field[knob] == v) continue;
         *field[knob] = v;
         float ms = 0.0f;
@@ -542,8 +559,12 @@ LaunchCtx Engine::ctx(uint32_t mpar, uint32_t lpar, uint32_t ppar) const {
   L.l2l_ctas = (uint32_t)sms_ * tuning_.l2l_ctas_per_sm;
   L.integrate_dynamic = tuning_.integrate_dynamic != 0u;
   L.m2l_compact = tuning_.m2l_compact != 0u;
+  L.m2l_lanes = tuning_.m2l_lanes;
+  L.l2l_lanes = tuning_.l2l_lanes;
+  L.upward_warps = tuning_.upward_warps;
   L.tile_list = use_lists_ ? d_tile_list_ : nullptr;
   L.task_list = use_lists_ ? d_task_list_ : nullptr;
+  L.scene_list = use_lists_ ? d_scene_list_ : nullptr;
   L.pdl = pdl_;
   L.p2p = near_mode_ == kNearP2P;
   L.pos4 = d_pos4_;
@@ -637,7 +658,7 @@ int Engine::rebuild_lists() {
   if (use_lists_) {
     if (list_pin_[0] == nullptr) {
       for (int b = 0; b < 2; b++) {
-        RF_CK(cudaHostAlloc((void **)&list_pin_[b], 4ull * (2ull + tiles_ + tasks_),
+        RF_CK(cudaHostAlloc((void **)&list_pin_[b], 4ull * (3ull + tiles_ + tasks_ + scenes_.size()),
                             cudaHostAllocDefault));
         RF_CK(cudaEventCreateWithFlags(&list_ev_[b], cudaEventDisableTiming));
       }
@@ -649,36 +670,49 @@ int Engine::rebuild_lists() {
       RF_CK(cudaEventSynchronize(list_ev_[b]));  // the last copy out of this block is done
       list_wait_s_ += std::chrono::duration<double>(std::chrono::steady_clock::now() - w0).count();
     }
-    uint32_t *blk = list_pin_[b], *tiles = blk + 2, *tasks = blk + 2 + tiles_;
-    uint32_t nt = 0, nk = 0;
-    for (const SceneDesc &d : scenes_) {
+    uint32_t *blk = list_pin_[b], *tiles = blk + 3, *tasks = blk + 3 + tiles_,
+             *sl = blk + 3 + tiles_ + tasks_;
+    uint32_t nt = 0, nk = 0, ns = 0;
+    for (uint32_t i = 0; i < scenes_.size(); i++) {
+      const SceneDesc &d = scenes_[i];
       if (d.n == 0u) continue;
       for (uint32_t t = 0; t < pad_tiles(d.n); t++) tiles[nt++] = d.tile_off + t;
       for (uint32_t t = 0; t < (1u << (3u * d.sub_level)); t++) tasks[nk++] = d.task_off + t;
+      sl[ns++] = i;
     }
     blk[0] = nt;
     blk[1] = nk;
+    blk[2] = ns;
     if (nt != 0u)
       RF_CK(cudaMemcpyAsync(d_tile_list_, tiles, 4ull * nt, cudaMemcpyHostToDevice, stream_));
     if (nk != 0u)
       RF_CK(cudaMemcpyAsync(d_task_list_, tasks, 4ull * nk, cudaMemcpyHostToDevice, stream_));
-    RF_CK(cudaMemcpyAsync(&d_ctr_->tiles_active, blk, 8, cudaMemcpyHostToDevice, stream_));
+    if (ns != 0u)
+      RF_CK(cudaMemcpyAsync(d_scene_list_, sl, 4ull * ns, cudaMemcpyHostToDevice, stream_));
+    RF_CK(cudaMemcpyAsync(&d_ctr_->tiles_active, blk, 12, cudaMemcpyHostToDevice, stream_));
     RF_CK(cudaEventRecord(list_ev_[b], stream_));
     return RFMM_OK;
   }
   tile_list_h_.clear();
   task_list_h_.clear();
-  for (const SceneDesc &d : scenes_) {
+  scene_list_h_.clear();
+  for (uint32_t i = 0; i < scenes_.size(); i++) {
+    const SceneDesc &d = scenes_[i];
     if (d.n == 0u) continue;
     for (uint32_t t = 0; t < pad_tiles(d.n); t++) tile_list_h_.push_back(d.tile_off + t);
     for (uint32_t t = 0; t < (1u << (3u * d.sub_level)); t++) task_list_h_.push_back(d.task_off + t);
+    scene_list_h_.push_back(i);
   }
-  const uint32_t counts[2] = {(uint32_t)tile_list_h_.size(), (uint32_t)task_list_h_.size()};
+  const uint32_t counts[3] = {(uint32_t)tile_list_h_.size(), (uint32_t)task_list_h_.size(),
+                              (uint32_t)scene_list_h_.size()};
   if (!tile_list_h_.empty())
     RF_CK(cudaMemcpyAsync(d_tile_list_, tile_list_h_.data(), 4 * tile_list_h_.size(),
                           cudaMemcpyHostToDevice, stream_));
   if (!task_list_h_.empty())
     RF_CK(cudaMemcpyAsync(d_task_list_, task_list_h_.data(), 4 * task_list_h_.size(),
+                          cudaMemcpyHostToDevice, stream_));
+  if (!scene_list_h_.empty())
+    RF_CK(cudaMemcpyAsync(d_scene_list_, scene_list_h_.data(), 4 * scene_list_h_.size(),
                           cudaMemcpyHostToDevice, stream_));
   RF_CK(cudaMemcpyAsync(&d_ctr_->tiles_active, counts, sizeof(counts), cudaMemcpyHostToDevice,
                         stream_));
@@ -731,33 +765,55 @@ int Engine::slot_desc(uint32_t scene, uint32_t n, const rfmm_params &p) {
     d.control_point[k] = p.control_point[k];
     d.control_axis_mode[k] = p.control_axis_mode[k];
   }
-  RF_CK(cudaMemcpyAsync(d_scenes_ + scene, &d, sizeof(SceneDesc), cudaMemcpyHostToDevice, stream_));
+  scenes_dirty_ = true;
   return RFMM_OK;
 }
 
-int Engine::activate(uint32_t scene, uint32_t n, const rfmm_params &p, const void *src,
-                     cudaMemcpyKind kind, bool lists) {
-  const int sd = slot_desc(scene, n, p);
-  if (sd != RFMM_OK) return sd;
-  const SceneDesc &d = scenes_[scene];
-  if (src != nullptr)  // null: the caller already staged the bodies at slot_bodies(scene)
-    RF_CK(cudaMemcpyAsync(d_part_[pcur_] + 2ull * d.body_off, src, 32ull * n, kind, stream_));
-  launch_iota(stream_, d_ids_[pcur_] + d.body_off, pad_tiles(n) * kTile);
-  RF_CK(cudaGetLastError());
-  launches_ += 1;
-  const int st = commit_scene(scene);
-  if (st != RFMM_OK) return st;
-  uploaded_[scene] = true;
-  committed_ = true;
-  return lists ? rebuild_lists() : RFMM_OK;
+int Engine::flush_scenes() {
+  if (!scenes_dirty_) return RFMM_OK;
+  if (scene_pin_[0] == nullptr) {
+    for (int b = 0; b < 2; b++) {
+      RF_CK(cudaHostAlloc((void **)&scene_pin_[b], sizeof(SceneDesc) * scenes_.size(), cudaHostAllocDefault));
+      RF_CK(cudaEventCreateWithFlags(&scene_ev_[b], cudaEventDisableTiming));
+    }
+  }
+  const uint32_t b = scene_buf_;
+  scene_buf_ ^= 1u;
+  RF_CK(cudaEventSynchronize(scene_ev_[b]));  // the block's last copy is done
+  std::memcpy(scene_pin_[b], scenes_.data(), sizeof(SceneDesc) * scenes_.size());
+  RF_CK(cudaMemcpyAsync(d_scenes_, scene_pin_[b], sizeof(SceneDesc) * scenes_.size(),
+                        cudaMemcpyHostToDevice, stream_));
+  RF_CK(cudaEventRecord(scene_ev_[b], stream_));
+  scenes_dirty_ = false;
+  return RFMM_OK;
+}
+
+int Engine::upload_map(MapBlock &m, const std::vector<uint32_t> &scenes, uint32_t *count) {
+  if (m.pin[0] == nullptr) {
+    for (int b = 0; b < 2; b++) {
+      RF_CK(cudaHostAlloc((void **)&m.pin[b], 4ull * tiles_, cudaHostAllocDefault));
+      RF_CK(cudaEventCreateWithFlags(&m.ev[b], cudaEventDisableTiming));
+    }
+    const int st = alloc((void **)&m.dev, 4ull * tiles_);
+    if (st != RFMM_OK) return st;
+  }
+  const uint32_t b = m.next;
+  m.next ^= 1u;
+  RF_CK(cudaEventSynchronize(m.ev[b]));  // the block's last copy is done
+  uint32_t total = 0;
+  for (uint32_t sc : scenes) {
+    const SceneDesc &d = scenes_[sc];
+    for (uint32_t t = 0; t < pad_tiles(d.n); t++) m.pin[b][total++] = d.tile_off + t;
+  }
+  // The previous use of m.dev is earlier on the same stream.
+  RF_CK(cudaMemcpyAsync(m.dev, m.pin[b], 4ull * total, cudaMemcpyHostToDevice, stream_));
+  RF_CK(cudaEventRecord(m.ev[b], stream_));
+  *count = total;
+  return RFMM_OK;
 }
 
 int Engine::activate_many(const std::vector<Admission> &admissions) {
   if (admissions.empty()) return RFMM_OK;
-  if (admissions.size() == 1u) {
-    const Admission &a = admissions[0];
-    return activate(a.scene, a.n, a.params, nullptr, cudaMemcpyDeviceToDevice, false);
-  }
   // Ascending slot order: the sort (scene rank above the Morton code) returns
   // the slots' keys in the same order, so sorted position i belongs to map
   // tile i / 256.
@@ -767,76 +823,65 @@ int Engine::activate_many(const std::vector<Admission> &admissions) {
   for (size_t i = 1; i < adm.size(); i++)
     if (adm[i].scene == adm[i - 1].scene) return RFMM_ERR_INVALID;
   for (const Admission &a : adm) {  // validate all before changing any slot
-    if (a.scene >= scenes_.size() || a.n == 0u) return RFMM_ERR_INVALID;
+    if (a.scene >= scenes_.size() || a.n == 0u || a.buffer > 1u) return RFMM_ERR_INVALID;
     const SceneDesc &d = scenes_[a.scene];
     if (d.n != 0u) return RFMM_ERR_STATE;
     const uint32_t depth = a.params.depth ? a.params.depth : depth_for_particles(a.n);
     if (a.n > d.tile_cap * kTile || depth < 4u || depth > d.max_depth) return RFMM_ERR_BUDGET;
   }
+  std::vector<uint32_t> slots;
+  SceneMask which{};
   for (const Admission &a : adm) {
     const int sd = slot_desc(a.scene, a.n, a.params);
     if (sd != RFMM_OK) return sd;
+    slots.push_back(a.scene);
+    which.bits[a.scene >> 5] |= 1u << (a.scene & 31u);
   }
-  if (map_pin_ == nullptr) {
-    RF_CK(cudaHostAlloc((void **)&map_pin_, 4ull * tiles_, cudaHostAllocDefault));
-    RF_CK(cudaEventCreateWithFlags(&map_ev_, cudaEventDisableTiming));
-    const int st = alloc((void **)&d_map_, 4ull * tiles_);
-    if (st != RFMM_OK) return st;
-  }
-  RF_CK(cudaEventSynchronize(map_ev_));  // the previous map copy is done with the block
+  int st = flush_scenes();
+  if (st != RFMM_OK) return st;
+  const uint32_t cur = pcur_.load(), scr = cur ^ 1u;
+  for (const Admission &a : adm)
+    if (a.buffer != scr)  // staged before a resort flipped the buffers
+      RF_CK(cudaMemcpyAsync(slot_bodies(a.scene, scr), slot_bodies(a.scene, a.buffer), 32ull * a.n,
+                            cudaMemcpyDeviceToDevice, stream_));
   uint32_t total = 0;
-  for (const Admission &a : adm) {
-    const SceneDesc &d = scenes_[a.scene];
-    for (uint32_t t = 0; t < pad_tiles(d.n); t++) map_pin_[total++] = d.tile_off + t;
-  }
-  RF_CK(cudaMemcpyAsync(d_map_, map_pin_, 4ull * total, cudaMemcpyHostToDevice, stream_));
-  RF_CK(cudaEventRecord(map_ev_, stream_));
-  LaunchCtx L = ctx(mcur_, lpar_, pcur_);
-  // Keys of every admitted slot (numbering its bodies in caller order), one
-  // sort, cleared trees, one gather with the leaf deposit, bodies back into
-  // the current buffer.
-  launch_keys(L, sort_.keys[0], sort_.vals[0], d_ids_[pcur_], 1, total, 0u, nullptr, d_map_);
+  st = upload_map(admit_map_, slots, &total);
+  if (st != RFMM_OK) return st;
+  // Keys of the staged bodies (numbering them in caller order), one sort,
+  // cleared trees, one gather with the leaf deposit into the current buffer.
+  LaunchCtx L = ctx(mcur_, lpar_, scr);
+  launch_keys(L, sort_.keys[0], sort_.vals[0], d_ids_[scr], 1, total, 0u, nullptr, admit_map_.dev);
   const int r = radix_sort(stream_, sort_, total * kTile, key_bits_);
-  for (const Admission &a : adm) {
-    const SceneDesc &d = scenes_[a.scene];
-    RF_CK(cudaMemsetAsync(d_mom_[mcur_] + d.cell_off, 0, 16ull * d.cells, stream_));
-    RF_CK(cudaMemsetAsync(d_mom_[mcur_ ^ 1u] + d.cell_off, 0, 16ull * d.cells, stream_));
-    RF_CK(cudaMemsetAsync(d_src_ + d.cell_off, 0, 16ull * d.cells, stream_));
-    RF_CK(cudaMemsetAsync(d_aux_ + d.cell_off, 0, 16ull * d.cells, stream_));
-  }
-  launch_gather(L, sort_.vals[r], d_part_[pcur_], d_ids_[pcur_], d_part_[pcur_ ^ 1u],
-                d_ids_[pcur_ ^ 1u], d_mom_[mcur_], total, 0u, nullptr, d_map_);
+  launch_clear_scenes(L, (uint32_t)scenes_.size(), which, d_mom_[mcur_], d_mom_[mcur_ ^ 1u], d_src_, d_aux_);
+  launch_gather(L, sort_.vals[r], d_part_[scr], d_ids_[scr], d_part_[cur], d_ids_[cur], d_mom_[mcur_],
+                total, 0u, nullptr, admit_map_.dev);
   RF_CK(cudaGetLastError());
-  for (const Admission &a : adm) {
-    const SceneDesc &d = scenes_[a.scene];
-    const uint32_t tiles = pad_tiles(d.n);
-    RF_CK(cudaMemcpyAsync(d_part_[pcur_] + 2ull * d.body_off, d_part_[pcur_ ^ 1u] + 2ull * d.body_off,
-                          32ull * tiles * kTile, cudaMemcpyDeviceToDevice, stream_));
-    RF_CK(cudaMemcpyAsync(d_ids_[pcur_] + d.body_off, d_ids_[pcur_ ^ 1u] + d.body_off,
-                          4ull * tiles * kTile, cudaMemcpyDeviceToDevice, stream_));
-    uploaded_[a.scene] = true;
-  }
-  launches_ += 2u + 3u * ((key_bits_ + 7u) / 8u);
+  for (uint32_t sc : slots) uploaded_[sc] = true;
+  launches_ += 3u + 3u * ((key_bits_ + 7u) / 8u);
   committed_ = true;
   return RFMM_OK;
 }
 
-int Engine::retire(uint32_t scene, bool lists) {
-  if (scene >= scenes_.size() || scenes_[scene].n == 0u) return RFMM_ERR_INVALID;
-  const SceneDesc &d = scenes_[scene];
-  LaunchCtx L = ctx(mcur_, lpar_, pcur_);
-  launch_unpermute(L, d_ids_[pcur_], d_part_[pcur_ ^ 1u], d.tile_off, pad_tiles(d.n));
+int Engine::retire_many(const std::vector<uint32_t> &slots) {
+  if (slots.empty()) return RFMM_OK;
+  for (uint32_t sc : slots)
+    if (sc >= scenes_.size() || scenes_[sc].n == 0u) return RFMM_ERR_INVALID;
+  uint32_t total = 0;
+  int st = upload_map(retire_map_, slots, &total);
+  if (st != RFMM_OK) return st;
+  const uint32_t cur = pcur_.load();
+  LaunchCtx L = ctx(mcur_, lpar_, cur);
+  launch_unpermute(L, d_ids_[cur], d_part_[cur ^ 1u], 0u, total, retire_map_.dev);
   RF_CK(cudaGetLastError());
   launches_ += 1;
-  return deactivate(scene, lists);
+  for (uint32_t sc : slots) scenes_[sc].n = 0u;
+  scenes_dirty_ = true;
+  return RFMM_OK;
 }
 
-int Engine::deactivate(uint32_t scene, bool lists) {
-  if (scene >= scenes_.size()) return RFMM_ERR_INVALID;
-  SceneDesc &d = scenes_[scene];
-  d.n = 0u;
-  RF_CK(cudaMemcpyAsync(d_scenes_ + scene, &d, sizeof(SceneDesc), cudaMemcpyHostToDevice, stream_));
-  return lists ? rebuild_lists() : RFMM_OK;
+int Engine::refresh_lists() {
+  const int st = flush_scenes();
+  return st != RFMM_OK ? st : rebuild_lists();
 }
 
 int Engine::commit() {
@@ -939,7 +984,7 @@ int Engine::solve_fields() {
 }
 
 int Engine::launch_chunk(uint32_t len, bool sort_at_end) {
-  const auto key = std::make_tuple(len, mcur_, lpar_, pcur_, sort_at_end);
+  const auto key = std::make_tuple(len, mcur_, lpar_, pcur_.load(), sort_at_end);
   auto it = graphs_.find(key);
   if (it == graphs_.end()) {
     // Timeline: this graph's records, cleared by its first node.

@@ -8,6 +8,7 @@
 #pragma once
 
 #include <cstdint>
+#include <atomic>
 #include <map>
 #include <tuple>
 #include <vector>
@@ -75,32 +76,38 @@ class Engine {
   int solve_fields();
   int step(uint32_t steps);
 
-  // Serving slots: put `n` bodies with `params` into an empty slot (sorted
-  // and deposited on the spot, other scenes untouched) or empty it again.
-  // With lists = false the active tile/task lists are left for one
-  // refresh_lists() after several slot changes.
-  int activate(uint32_t scene, uint32_t n, const rfmm_params &params, const void *src,
-               cudaMemcpyKind kind, bool lists = true);
-  int deactivate(uint32_t scene, bool lists = true);
-  // Bodies of a finished slot back to the caller's order in the scratch
-  // range (slot_scratch), then the slot is emptied.
-  int retire(uint32_t scene, bool lists = true);
-  int refresh_lists() { return rebuild_lists(); }
-  // Serving: several requests into empty slots at once (bodies already staged
-  // at slot_bodies): one key pass, one radix sort and one gather with deposit
-  // for all of them (their keys concatenated in slot order), instead of a
-  // sort per slot.  Lists are left for refresh_lists().
+  // Serving slots.  Requests are staged into empty slots of the scratch
+  // particle buffer (slot_bodies(slot, scratch_buffer()) as read at staging
+  // time) and admitted together: one scene-table copy, one key pass, one
+  // radix sort, one tree clear and one gather with deposit into the current
+  // buffer for all of them (their keys concatenated in slot order); a slot
+  // staged before a resort flipped the buffers is copied across first.
+  // Lists are left for refresh_lists().
   struct Admission {
     uint32_t scene, n;
     rfmm_params params;
+    uint32_t buffer;  // particle buffer the bodies were staged in
   };
   int activate_many(const std::vector<Admission> &admissions);
+  // Finished slots: their bodies back to caller order in their scratch-buffer
+  // range (one launch for all), then the slots are emptied; the emptied
+  // descriptors reach the device with the next refresh_lists() or admission,
+  // which must come before the next step.
+  int retire_many(const std::vector<uint32_t> &slots);
+  int refresh_lists();
   // Seconds refresh_lists spent waiting for a pinned list block's last copy.
   double list_wait_seconds() const { return list_wait_s_; }
-  float4 *slot_bodies(uint32_t scene) const { return d_part_[pcur_] + 2ull * scenes_[scene].body_off; }
-  float4 *slot_scratch(uint32_t scene) const {
-    return d_part_[pcur_ ^ 1u] + 2ull * scenes_[scene].body_off;
+  // Serving: a slot's bodies in particle buffer `buffer`.  Stage-in writes
+  // an empty slot in scratch_buffer() as read at the time (a resort may flip
+  // the buffers before admission, which then copies the slot across); a
+  // retired slot's result lies in scratch_buffer() as read right after
+  // retire_many().  Kernels never touch an inactive slot's range in either
+  // buffer.
+  float4 *slot_bodies(uint32_t scene, uint32_t buffer) const {
+    return d_part_[buffer] + 2ull * scenes_[scene].body_off;
   }
+  uint32_t particle_buffer() const { return pcur_.load(); }
+  uint32_t scratch_buffer() const { return pcur_.load() ^ 1u; }
   uint32_t capacity(uint32_t scene) const { return scenes_[scene].tile_cap * kTile; }
   bool active(uint32_t scene) const { return scenes_[scene].n != 0u; }
   int sync();
@@ -165,10 +172,26 @@ class Engine {
   uint32_t *d_starts_ = nullptr;  // per-leaf start slots (leaf sorts)
   int launch_chunk(uint32_t len, bool sort_at_end);
   int commit_scene(uint32_t scene);
-  int slot_desc(uint32_t scene, uint32_t n, const rfmm_params &p);  // fill a free slot's descriptor
-  uint32_t *map_pin_ = nullptr;   // activate_many: pinned tile map (tiles_ entries)
-  uint32_t *d_map_ = nullptr;     // its device copy
-  cudaEvent_t map_ev_ = nullptr;  // the last copy out of map_pin_
+  int slot_desc(uint32_t scene, uint32_t n, const rfmm_params &p);  // fill a free slot's descriptor (host)
+  // Serving: the host scene table goes to the device whole (from two pinned
+  // blocks used in turn) when slot changes made it stale.
+  int flush_scenes();
+  bool scenes_dirty_ = false;
+  SceneDesc *scene_pin_[2] = {nullptr, nullptr};
+  cudaEvent_t scene_ev_[2] = {nullptr, nullptr};
+  uint32_t scene_buf_ = 0;
+  // Tile maps of admissions and retirements: pinned blocks used in turn, each
+  // with an event marking its last copy, and their device copies.
+  struct MapBlock {
+    uint32_t *pin[2] = {nullptr, nullptr};
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    uint32_t *dev = nullptr;
+    uint32_t next = 0;
+  };
+  MapBlock admit_map_, retire_map_;
+  // Copies `tiles` of `scenes` (each slot's padded tiles, in order) into the
+  // map's next pinned block and to the device; returns the tile count.
+  int upload_map(MapBlock &m, const std::vector<uint32_t> &scenes, uint32_t *count);
   int rebuild_lists();
   int check_device_error();
 
@@ -211,11 +234,11 @@ class Engine {
   int diag_prepare(uint32_t scene, size_t doubles, bool all_bodies);
   float4 *d_src_ = nullptr;
   float4 *d_aux_ = nullptr;
-  uint32_t *d_tile_list_ = nullptr, *d_task_list_ = nullptr;
-  std::vector<uint32_t> tile_list_h_, task_list_h_;
+  uint32_t *d_tile_list_ = nullptr, *d_task_list_ = nullptr, *d_scene_list_ = nullptr;
+  std::vector<uint32_t> tile_list_h_, task_list_h_, scene_list_h_;
   // Serving engines refresh the active lists often and while kernels are
   // queued: the lists go to the device from two pinned blocks used in turn
-  // ([count of tiles, count of tasks | tiles_ tiles | tasks_ tasks]), each
+  // ([counts of tiles, tasks, scenes | tiles_ tiles | tasks_ tasks | scenes]), each
   // with an event marking when its last copy finished.  A pageable source
   // would make the copy wait for the queued kernels once it outgrows the
   // driver's staging buffer.
@@ -235,7 +258,9 @@ class Engine {
   size_t device_bytes_ = 0;
 
   // Host-side sequencing state.
-  uint32_t pcur_ = 0;    // particle buffer holding the resident bodies
+  // Particle buffer holding the resident bodies; flipped by the thread that
+  // enqueues work, read by serving stage-in threads (particle_buffer()).
+  std::atomic<uint32_t> pcur_{0};
   uint32_t mcur_ = 0;    // moment buffer whose leaf level holds the current deposit
   uint32_t lpar_ = 0;    // parent list to write next
   int tree_buf_ = -1;    // moment buffer holding the last complete tree

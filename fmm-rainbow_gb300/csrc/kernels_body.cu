@@ -827,8 +827,9 @@ __global__ void __launch_bounds__(256) k_unpermute(const SceneDesc *__restrict__
                                                    const uint32_t *__restrict__ tile_scene,
                                                    const float4 *__restrict__ part,
                                                    const uint32_t *__restrict__ ids,
-                                                   float4 *__restrict__ out, uint32_t tile_base) {
-  const uint32_t tile = tile_base + blockIdx.x;
+                                                   float4 *__restrict__ out, uint32_t tile_base,
+                                                   const uint32_t *__restrict__ tile_map) {
+  const uint32_t tile = tile_map != nullptr ? tile_map[blockIdx.x] : tile_base + blockIdx.x;
   const SceneDesc &S = scenes[tile_scene[tile]];
   const uint32_t slot = tile * kTile + threadIdx.x;
   if (slot - S.body_off >= S.n) return;
@@ -1047,8 +1048,37 @@ void launch_leaf_starts(const LaunchCtx &L, const uint32_t *sorted_keys, uint32_
 }
 
 void launch_unpermute(const LaunchCtx &L, const uint32_t *ids, float4 *out, uint32_t tile_base,
-                      uint32_t tiles) {
-  k_unpermute<<<tiles, kTile, 0, L.stream>>>(L.scenes, L.tile_scene, L.part, ids, out, tile_base);
+                      uint32_t tiles, const uint32_t *tile_map) {
+  k_unpermute<<<tiles, kTile, 0, L.stream>>>(L.scenes, L.tile_scene, L.part, ids, out, tile_base,
+                                             tile_map);
+}
+
+// Zero the moments (both buffers), sources and records of every cell of the
+// scenes set in `which` (a rebuilt scene starts from cleared trees: the
+// upward pass skips subtrees that are empty in both moment buffers).  Every
+// CTA takes a share of each scene's cells.
+__global__ void __launch_bounds__(256) k_clear_scenes(const SceneDesc *__restrict__ scenes, uint32_t nscenes,
+                                                      const __grid_constant__ SceneMask which,
+                                                      uint4 *__restrict__ mom0, uint4 *__restrict__ mom1,
+                                                      float4 *__restrict__ src, float4 *__restrict__ aux) {
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t w = 0; w < (nscenes + 31u) / 32u; w++) {
+    for (uint32_t bits = which.bits[w]; bits != 0u; bits &= bits - 1u) {
+      const SceneDesc &S = scenes[32u * w + (uint32_t)(__ffs(bits) - 1)];
+      for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < S.cells; c += stride) {
+        const uint32_t i = S.cell_off + c;
+        mom0[i] = make_uint4(0u, 0u, 0u, 0u);
+        mom1[i] = make_uint4(0u, 0u, 0u, 0u);
+        src[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        aux[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      }
+    }
+  }
+}
+
+void launch_clear_scenes(const LaunchCtx &L, uint32_t nscenes, const SceneMask &which, uint4 *mom0,
+                         uint4 *mom1, float4 *src, float4 *aux) {
+  k_clear_scenes<<<4u * L.sms, 256, 0, L.stream>>>(L.scenes, nscenes, which, mom0, mom1, src, aux);
 }
 
 void launch_initialize(const LaunchCtx &L, float4 *part_out, uint32_t tile_base, uint32_t tiles) {

@@ -28,6 +28,11 @@
 //                from the M2L results of the target's ancestors (so levels
 //                need no ordering), then adaptive leaves add their 26 near
 //                terms in loop order.
+//   k_upward_warps, and the lane paths of k_m2l and k_l2l_near
+//                the same passes with one warp per subtree and one lane per
+//                target (its sums in its own registers, in the same order):
+//                fewer instructions and barriers per term, for work lists
+//                long enough to fill the GPU (many scenes).
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -257,11 +262,280 @@ __device__ __forceinline__ void upward_task(
   __syncthreads();
 }
 
+// The clearing CTAs of the upward pass: each warp takes 32 of the previous
+// step's listed parents at a time (one per lane), then clears their 8
+// children's 48-byte fields with one 16-byte store per lane (fields are zero
+// off the M2L path).
+__device__ __forceinline__ void clear_previous_fields(const SceneDesc *__restrict__ scenes,
+                                                      float *__restrict__ fields,
+                                                      const WorkItem *__restrict__ plist_prev,
+                                                      Counters *__restrict__ ctr, uint32_t list_par,
+                                                      uint32_t plist_cap, uint32_t clear_ctas,
+                                                      unsigned long long *__restrict__ stamp) {
+  const uint32_t tid = threadIdx.x;
+  grid_dependency_wait();  // the previous integrate read the fields
+  stamp_begin(stamp);
+  if (blockIdx.x == 0 && tid == 0) ctr->tile_cursor = 0u;  // for this step's integrate
+  const uint32_t prev_n = min(ctr->parents[list_par ^ 1u], plist_cap);
+  const uint32_t wpb = blockDim.x >> 5, lane = tid & 31u;
+  const uint32_t ch = lane / 3u, part = lane % 3u;  // lanes 0..23: child, float4 of its field
+  const uint32_t choff_x = ch & 1u, choff_y = (ch >> 1) & 1u, choff_z = ch >> 2;
+  for (uint32_t i0 = (blockIdx.x * wpb + (tid >> 5)) * 32u; i0 < prev_n; i0 += clear_ctas * wpb * 32u) {
+    uint32_t base = 0u, dim = 0u;
+    if (i0 + lane < prev_n) {
+      const WorkItem w = plist_prev[i0 + lane];
+      const uint32_t lp = w.cell == 0u ? 0u : level_of_d(w.cell);
+      uint32_t px, py, pz;
+      cell_coords_lv(w.cell - level_offset_d(lp), lp, px, py, pz);
+      dim = 2u << lp;
+      base = scenes[w.scene].cell_off + level_offset_d(lp + 1u) + lin3(2u * px, 2u * py, 2u * pz, dim);
+    }
+    const uint32_t nb = min(32u, prev_n - i0);
+    for (uint32_t j = 0; j < nb; j++) {
+      const uint32_t b = __shfl_sync(0xFFFFFFFFu, base, j), d = __shfl_sync(0xFFFFFFFFu, dim, j);
+      if (lane < 24u) {
+        const uint32_t c = b + choff_x + d * (choff_y + d * choff_z);
+        reinterpret_cast<float4 *>(fields)[(size_t)c * 3u + part] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    }
+  }
+  stamp_end(stamp);
+  grid_dependents_may_launch();
+}
+
+// ----------------------------------------------------------- upward, warps
+//
+// One warp per 8x8x8-leaf subtree.  Lane L owns the subtree's level D-1
+// cells 2L and 2L+1 in Morton order, so lanes 4p .. 4p+3 hold the eight
+// children of level D-2 cell p: each lane sums its cells' leaves itself and
+// two rounds of shuffles give the level D-2 cells, three more the root.  No
+// CTA barrier is taken and a CTA works on eight subtrees at once.  Lane 0
+// writes the root and takes the completion tickets; the scene's last warp
+// reduces levels r-1 .. 0 the same way from the level-r cells.  All sums are
+// integers modulo 2^32, so the order of addition does not matter.
+
+// Block coordinates of Morton index m over s levels (x in the lowest bit).
+__device__ __forceinline__ void morton_xyz(uint32_t m, uint32_t s, uint32_t &x, uint32_t &y, uint32_t &z) {
+  x = y = z = 0u;
+#pragma unroll
+  for (uint32_t b = 0; b < 3u; b++) {
+    if (b < s) {
+      x |= ((m >> (3u * b)) & 1u) << b;
+      y |= ((m >> (3u * b + 1u)) & 1u) << b;
+      z |= ((m >> (3u * b + 2u)) & 1u) << b;
+    }
+  }
+}
+
+__device__ __forceinline__ uint4 shfl_xor_add(uint4 v, uint32_t mask) {
+  return add_moment(v, make_uint4(__shfl_xor_sync(0xFFFFFFFFu, v.x, mask),
+                                  __shfl_xor_sync(0xFFFFFFFFu, v.y, mask),
+                                  __shfl_xor_sync(0xFFFFFFFFu, v.z, mask),
+                                  __shfl_xor_sync(0xFFFFFFFFu, v.w, mask)));
+}
+
+// Lists up to four candidate cells per lane (count > 16, wgsl:472-476) with
+// one atomic for the warp.
+__device__ __forceinline__ void warp_list_parents(uint32_t scene, const uint32_t cell[4],
+                                                  const bool want[4], WorkItem *__restrict__ plist,
+                                                  uint32_t plist_cap, Counters *__restrict__ ctr,
+                                                  uint32_t list_par) {
+  const uint32_t lane = threadIdx.x & 31u, below = (1u << lane) - 1u;
+  uint32_t ball[4], total = 0u;
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    ball[i] = __ballot_sync(0xFFFFFFFFu, want[i]);
+    total += __popc(ball[i]);
+  }
+  if (total == 0u) return;
+  uint32_t base = 0u;
+  if (lane == 0u) {
+    base = atomicAdd(&ctr->parents[list_par], total);
+    if (base + total > plist_cap) atomicCAS(&ctr->error, 0u, (uint32_t)kDevErrListOverflow);
+  }
+  base = __shfl_sync(0xFFFFFFFFu, base, 0);
+  uint32_t before = 0u;
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const uint32_t at = base + before + __popc(ball[i] & below);
+    if (want[i] && at < plist_cap) plist[at] = WorkItem{scene, cell[i]};
+    before += __popc(ball[i]);
+  }
+}
+
+__device__ __forceinline__ bool above_capacity(uint32_t count) {
+  return (int32_t)count > (int32_t)kAdaptive;
+}
+
+__device__ __forceinline__ void upward_warp_task(
+    const SceneDesc &S, uint32_t scene, uint32_t sub, uint4 *__restrict__ mom,
+    uint4 *__restrict__ mom_next, float4 *__restrict__ src, float4 *__restrict__ aux,
+    uint32_t *__restrict__ choice, WorkItem *__restrict__ plist, uint32_t plist_cap,
+    Counters *__restrict__ ctr, uint32_t list_par, uint32_t *__restrict__ tickets) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t D = S.depth, r = S.sub_level;  // r = D - 3
+  uint32_t sx, sy, sz;
+  cell_coords_lv(sub, r, sx, sy, sz);
+  const uint32_t leaf_base = S.cell_off + level_offset_d(D);
+  // This lane's two level D-1 cells: block coordinates 0..3 per axis.
+  uint32_t ux[2], uy[2], uz[2];
+  uint4 c1[2];
+  uint32_t seen = 0u;
+#pragma unroll
+  for (uint32_t j = 0; j < 2u; j++) {
+    morton_xyz(2u * lane + j, 2u, ux[j], uy[j], uz[j]);
+    uint4 acc = make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+    for (uint32_t k = 0; k < 8u; k++) {
+      const uint4 m = mom[leaf_base + lin3_lv(8u * sx + 2u * ux[j] + (k & 1u), 8u * sy + 2u * uy[j] + ((k >> 1) & 1u),
+                                              8u * sz + 2u * uz[j] + (k >> 2), D)];
+      seen |= m.x;
+      acc = add_moment(acc, m);
+    }
+    c1[j] = acc;
+  }
+  // The subtree root in both moment buffers (see upward_task for why a
+  // subtree empty in all of these has nothing to write).
+  const uint32_t rcell = level_offset_d(r) + lin3_lv(sx, sy, sz, r);
+  if (lane == 0u) seen |= mom[S.cell_off + rcell].x | mom_next[S.cell_off + rcell].x;
+  const bool live = __any_sync(0xFFFFFFFFu, seen != 0u);
+  uint4 c2 = make_uint4(0u, 0u, 0u, 0u), root = c2;
+  if (live) {
+    c2 = shfl_xor_add(shfl_xor_add(add_moment(c1[0], c1[1]), 1u), 2u);  // level D-2 cell lane >> 2
+    root = shfl_xor_add(shfl_xor_add(shfl_xor_add(c2, 4u), 8u), 16u);
+    if (lane == 0u) mom[S.cell_off + rcell] = root;
+  }
+  uint32_t last = 0u;
+  if (lane == 0u) {
+    const uint32_t ntasks = 1u << (3u * r);
+    const uint32_t ngroups = (ntasks + kTicketGroup - 1u) / kTicketGroup;
+    const uint32_t group = sub / kTicketGroup;
+    const uint32_t gsize = min(kTicketGroup, ntasks - group * kTicketGroup);
+    uint32_t *t = tickets + scene * kTicketStride;
+    const uint32_t g_old = live ? atomic_add_acq_rel(&t[1u + group], 1u) : atomicAdd(&t[1u + group], 1u);
+    if (g_old == gsize - 1u) {  // last subtree of its group
+      if (!live) __threadfence();
+      t[1u + group] = 0u;
+      if (atomic_add_acq_rel(&t[0], 1u) == ngroups - 1u) {  // last group of the scene
+        t[0] = 0u;
+        last = 1u;
+      }
+    }
+  }
+  last = __shfl_sync(0xFFFFFFFFu, last, 0);
+
+  if (live) {
+    const uint32_t p = lane >> 2;  // this lane's level D-2 cell (Morton)
+    uint32_t px, py, pz;
+    morton_xyz(p, 1u, px, py, pz);
+    uint32_t cell[4];
+    bool want[4];
+#pragma unroll
+    for (uint32_t j = 0; j < 2u; j++) {
+      // Leaves: source records and the cleared next-deposit leaf (the leaf
+      // moments are read again, from L1).
+#pragma unroll 1
+      for (uint32_t k = 0; k < 8u; k++) {
+        const uint32_t leaf = leaf_base + lin3_lv(8u * sx + 2u * ux[j] + (k & 1u),
+                                                  8u * sy + 2u * uy[j] + ((k >> 1) & 1u),
+                                                  8u * sz + 2u * uz[j] + (k >> 2), D);
+        const uint4 m = mom[leaf];
+        src[leaf] = make_source(m, S.scale, S.gravity, S.n_f);
+        aux[leaf] = make_aux(m.x, S.gravity, S.n_f);
+        mom_next[leaf] = make_uint4(0u, 0u, 0u, 0u);
+        // Sample cell of the leaf: inside the subtree when its root holds
+        // more than 16 bodies (the first of levels D-2, D-1 with count <= 16,
+        // else the leaf), else unresolved.
+        uint32_t v = kChoiceUnresolved;
+        if (above_capacity(root.x)) {
+          if (!above_capacity(c2.x)) {
+            v = ((D - 2u) << 28) | (level_offset_d(D - 2u) + lin3_lv(2u * sx + px, 2u * sy + py, 2u * sz + pz, D - 2u));
+          } else if (!above_capacity(c1[j].x)) {
+            v = ((D - 1u) << 28) |
+                (level_offset_d(D - 1u) + lin3_lv(4u * sx + ux[j], 4u * sy + uy[j], 4u * sz + uz[j], D - 1u));
+          } else {
+            v = (D << 28) | (leaf - S.cell_off);
+          }
+        }
+        choice[leaf] = v;
+      }
+      // The level D-1 cell.
+      cell[j] = level_offset_d(D - 1u) + lin3_lv(4u * sx + ux[j], 4u * sy + uy[j], 4u * sz + uz[j], D - 1u);
+      store_cell(S, cell[j], c1[j], mom, src, aux);
+      want[j] = above_capacity(c1[j].x);
+    }
+    cell[2] = level_offset_d(D - 2u) + lin3_lv(2u * sx + px, 2u * sy + py, 2u * sz + pz, D - 2u);
+    want[2] = (lane & 3u) == 0u && above_capacity(c2.x);
+    if ((lane & 3u) == 0u) store_cell(S, cell[2], c2, mom, src, aux);
+    cell[3] = rcell;
+    want[3] = lane == 0u && above_capacity(root.x);
+    if (lane == 0u) store_cell(S, rcell, root, mom, src, aux);
+    warp_list_parents(scene, cell, want, plist, plist_cap, ctr, list_par);
+  }
+
+  if (last) {
+    // Levels r-1 .. 0 from the level-r cells (written by other warps; their
+    // tickets released those writes to lane 0's acquire).
+    __syncwarp();
+    __threadfence();
+    const uint32_t rbase = S.cell_off + level_offset_d(r);
+    uint4 a = make_uint4(0u, 0u, 0u, 0u), b = a;  // level-2 cells 2L, 2L+1 (r >= 2) or level 1 (r == 1)
+    uint32_t ax[2], ay[2], az[2];
+#pragma unroll
+    for (uint32_t j = 0; j < 2u; j++) morton_xyz(2u * lane + j, 2u, ax[j], ay[j], az[j]);
+    if (r == 3u) {
+#pragma unroll
+      for (uint32_t j = 0; j < 2u; j++) {
+        uint4 acc = make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+        for (uint32_t k = 0; k < 8u; k++)
+          acc = add_moment(acc, __ldcg(&mom[rbase + lin3_lv(2u * ax[j] + (k & 1u), 2u * ay[j] + ((k >> 1) & 1u),
+                                                            2u * az[j] + (k >> 2), 3u)]));
+        if (j == 0u) a = acc; else b = acc;
+      }
+    } else if (r == 2u) {
+      a = __ldcg(&mom[rbase + lin3_lv(ax[0], ay[0], az[0], 2u)]);
+      b = __ldcg(&mom[rbase + lin3_lv(ax[1], ay[1], az[1], 2u)]);
+    } else if (lane < 8u) {
+      uint32_t x, y, z;
+      morton_xyz(lane, 1u, x, y, z);
+      a = __ldcg(&mom[rbase + lin3_lv(x, y, z, 1u)]);
+    }
+    const uint4 l1 = shfl_xor_add(shfl_xor_add(add_moment(a, b), 1u), 2u);  // level-1 cell lane >> 2 (r >= 2)
+    const uint4 l0 = r >= 2u ? shfl_xor_add(shfl_xor_add(shfl_xor_add(l1, 4u), 8u), 16u)
+                             : shfl_xor_add(shfl_xor_add(shfl_xor_add(a, 1u), 2u), 4u);
+    uint32_t cell[4] = {0u, 0u, 0u, 0u};
+    bool want[4] = {false, false, false, false};
+    if (r == 3u) {
+#pragma unroll
+      for (uint32_t j = 0; j < 2u; j++) {
+        cell[j] = level_offset_d(2u) + lin3_lv(ax[j], ay[j], az[j], 2u);
+        const uint4 v = j == 0u ? a : b;
+        store_cell(S, cell[j], v, mom, src, aux);
+        want[j] = above_capacity(v.x);
+      }
+    }
+    if (r >= 2u && (lane & 3u) == 0u) {
+      uint32_t x, y, z;
+      morton_xyz(lane >> 2, 1u, x, y, z);
+      cell[2] = level_offset_d(1u) + lin3_lv(x, y, z, 1u);
+      store_cell(S, cell[2], l1, mom, src, aux);
+      want[2] = above_capacity(l1.x);
+    }
+    if (lane == 0u) {
+      cell[3] = 0u;
+      store_cell(S, 0u, l0, mom, src, aux);
+      want[3] = above_capacity(l0.x);
+    }
+    warp_list_parents(scene, cell, want, plist, plist_cap, ctr, list_par);
+  }
+}
+
 // Persistent upward pass over the active subtree tasks (task_list, or every
 // task when null).  The first `clear_ctas` CTAs only clear the fields of the
 // previous step's targets (children of its listed parents; fields are zero
 // off the M2L path), so the subtree CTAs start their reductions at once.
-__global__ void __launch_bounds__(256) k_upward(const SceneDesc *__restrict__ scenes,
+__global__ void __launch_bounds__(256, 4) k_upward(const SceneDesc *__restrict__ scenes,
                                                 const uint32_t *__restrict__ task_scene,
                                                 const uint32_t *__restrict__ task_list,
                                                 uint32_t ntasks_all,
@@ -273,6 +547,7 @@ __global__ void __launch_bounds__(256) k_upward(const SceneDesc *__restrict__ sc
                                                 const WorkItem *__restrict__ plist_prev,
                                                 Counters *__restrict__ ctr, uint32_t list_par,
                                                 uint32_t *__restrict__ tickets, uint32_t clear_ctas,
+                                                uint32_t warp_min,
                                                 unsigned long long *__restrict__ stamp) {
   __shared__ uint4 s0[512];
   __shared__ uint4 s1[64];
@@ -281,38 +556,8 @@ __global__ void __launch_bounds__(256) k_upward(const SceneDesc *__restrict__ sc
   __shared__ WorkItem s_items[160];  // a subtree's 73 cells + the top levels' 73
   __shared__ uint32_t s_nitems, s_base, s_last;
   __shared__ SceneDesc sS;
-  const uint32_t tid = threadIdx.x;
   if (blockIdx.x < clear_ctas) {
-    grid_dependency_wait();  // the previous integrate read the fields
-    stamp_begin(stamp);
-    if (blockIdx.x == 0 && tid == 0) ctr->tile_cursor = 0u;  // for this step's integrate
-    // Each warp takes 32 listed parents at a time (one per lane), then clears
-    // their 8 children's 48-byte fields with one 16-byte store per lane.
-    const uint32_t prev_n = min(ctr->parents[list_par ^ 1u], plist_cap);
-    const uint32_t wpb = blockDim.x >> 5, lane = tid & 31u;
-    const uint32_t ch = lane / 3u, part = lane % 3u;  // lanes 0..23: child, float4 of its field
-    const uint32_t choff_x = ch & 1u, choff_y = (ch >> 1) & 1u, choff_z = ch >> 2;
-    for (uint32_t i0 = (blockIdx.x * wpb + (tid >> 5)) * 32u; i0 < prev_n; i0 += clear_ctas * wpb * 32u) {
-      uint32_t base = 0u, dim = 0u;
-      if (i0 + lane < prev_n) {
-        const WorkItem w = plist_prev[i0 + lane];
-        const uint32_t lp = w.cell == 0u ? 0u : level_of_d(w.cell);
-        uint32_t px, py, pz;
-        cell_coords_lv(w.cell - level_offset_d(lp), lp, px, py, pz);
-        dim = 2u << lp;
-        base = scenes[w.scene].cell_off + level_offset_d(lp + 1u) + lin3(2u * px, 2u * py, 2u * pz, dim);
-      }
-      const uint32_t nb = min(32u, prev_n - i0);
-      for (uint32_t j = 0; j < nb; j++) {
-        const uint32_t b = __shfl_sync(0xFFFFFFFFu, base, j), d = __shfl_sync(0xFFFFFFFFu, dim, j);
-        if (lane < 24u) {
-          const uint32_t c = b + choff_x + d * (choff_y + d * choff_z);
-          reinterpret_cast<float4 *>(fields)[(size_t)c * 3u + part] = make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-      }
-    }
-    stamp_end(stamp);
-    grid_dependents_may_launch();
+    clear_previous_fields(scenes, fields, plist_prev, ctr, list_par, plist_cap, clear_ctas, stamp);
     return;
   }
 
@@ -321,6 +566,21 @@ __global__ void __launch_bounds__(256) k_upward(const SceneDesc *__restrict__ sc
   // before waiting for that kernel.
   const uint32_t cta = blockIdx.x - clear_ctas, ncta = gridDim.x - clear_ctas;
   const uint32_t ntasks = task_list != nullptr ? min(ctr->tasks_active, ntasks_all) : ntasks_all;
+  if (ntasks >= warp_min) {  // grid-uniform: one warp per subtree
+    const uint32_t wpb = blockDim.x >> 5, warp = threadIdx.x >> 5;
+    grid_dependency_wait();  // the previous integrate deposited into mom_next
+    stamp_begin(stamp);
+    for (uint32_t it = cta + ncta * warp; it < ntasks; it += ncta * wpb) {
+      const uint32_t task = task_list != nullptr ? task_list[it] : it;
+      const uint32_t scene = task_scene[task];
+      const SceneDesc &S = scenes[scene];
+      upward_warp_task(S, scene, task - S.task_off, mom, mom_next, src, aux, choice, plist, plist_cap,
+                       ctr, list_par, tickets);
+    }
+    stamp_end(stamp);
+    grid_dependents_may_launch();
+    return;
+  }
   uint32_t task = 0u, scene = 0u;
   if (cta < ntasks) {
     task = task_list != nullptr ? task_list[cta] : cta;
@@ -433,16 +693,89 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, i
       : "memory");
 }
 
+// M2L with one lane per target (long parent lists): warp w of the pass takes
+// listed parents 4w .. 4w+3, lane 8q + c handles child c of parent q, and
+// the lane adds the terms of its contributing stencil slots to its own ten
+// sums in the reference's loop order (no partial sum crosses lanes).  Source
+// cells are read through L1: the 8 lanes of a parent read the same cell, so
+// a warp requests at most 4 addresses per slot.  `slots` holds, per slot in
+// loop order, the cell's offset in the 6x6x6 block (3 bits per axis) and the
+// children it is adjacent to (bits 9..16).
+__device__ __forceinline__ uint32_t m2l_slot_entry(uint32_t k) {
+  const uint32_t info = m2l_slot_info(k), t = info & 0xFFu;
+  return (t % 6u) | (((t / 6u) % 6u) << 3) | ((t / 36u) << 6) | ((info >> 8) << 9);
+}
+
+__device__ __forceinline__ void m2l_lanes_pass(const SceneDesc *__restrict__ scenes,
+                                               const WorkItem *__restrict__ plist, uint32_t count,
+                                               const uint4 *__restrict__ mom,
+                                               const float4 *__restrict__ src,
+                                               float *__restrict__ lfield,
+                                               const uint32_t *__restrict__ slots) {
+  const uint32_t lane = threadIdx.x & 31u, q = lane >> 3, c = lane & 7u;
+  const uint32_t groups = (count + 3u) / 4u, stride = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t g = blockIdx.x + gridDim.x * (threadIdx.x >> 5); g < groups; g += stride) {
+    const uint32_t item = 4u * g + q;
+    const bool valid = item < count;
+    const WorkItem w = valid ? plist[item] : WorkItem{0u, 0u};
+    const SceneDesc &S = scenes[w.scene];
+    const uint32_t lp = w.cell == 0u ? 0u : level_of_d(w.cell);
+    const uint32_t l = lp + 1u, dim = 2u << lp;
+    uint32_t upx, upy, upz;
+    cell_coords_lv(w.cell - level_offset_d(lp), lp, upx, upy, upz);
+    const int bx = 2 * (int)upx - 2, by = 2 * (int)upy - 2, bz = 2 * (int)upz - 2;
+    const uint32_t lvl_base = S.cell_off + level_offset_d(l);
+    const uint32_t tx = 2u * upx + (c & 1u), ty = 2u * upy + ((c >> 1) & 1u), tz = 2u * upz + (c >> 2);
+    const uint32_t target = lvl_base + lin3(tx, ty, tz, dim);
+    const bool live = valid && mom[target].x != 0u;  // empty children are not targets
+    const float ctx = cell_center_lv(tx, l), cty = cell_center_lv(ty, l), ctz = cell_center_lv(tz, l);
+    const float eps = (0.06f * kHalf) * pow2_neg(l);  // wgsl:507
+    float acc[10];
+#pragma unroll
+    for (int k = 0; k < 10; k++) acc[k] = 0.0f;
+    if (__any_sync(0xFFFFFFFFu, live)) {
+      // Slot k + 1's source is requested while slot k is evaluated.
+      auto fetch = [&](uint32_t k, float4 &sv) {
+        const uint32_t e = slots[k];
+        const int x = bx + (int)(e & 7u), y = by + (int)((e >> 3) & 7u), z = bz + (int)((e >> 6) & 7u);
+        sv = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (live && !((e >> (9u + c)) & 1u) && (uint32_t)x < dim && (uint32_t)y < dim && (uint32_t)z < dim)
+          sv = __ldg(&src[lvl_base + lin3((uint32_t)x, (uint32_t)y, (uint32_t)z, dim)]);
+      };
+      float4 next;
+      fetch(0u, next);
+      for (uint32_t k = 0; k < kTileCells; k++) {
+        const float4 sv = next;
+        if (k + 1u < kTileCells) fetch(k + 1u, next);
+        if (sv.w != 0.0f) {  // excluded, absent and empty slots all read w = 0
+          float out[10];
+          pair_field_d(sv, ctx, cty, ctz, eps, out);
+#pragma unroll
+          for (int m = 0; m < 10; m++) acc[m] = acc[m] + out[m];
+        }
+      }
+    }
+    if (live) {
+      float4 *fp = reinterpret_cast<float4 *>(lfield + (size_t)target * 12u);
+      fp[0] = make_float4(acc[0], acc[1], acc[2], acc[3]);
+      fp[1] = make_float4(acc[4], acc[5], acc[6], acc[7]);
+      fp[2] = make_float4(acc[8], acc[9], 0.0f, 0.0f);
+    }
+  }
+}
+
 template <bool kCompact>
-__global__ void __launch_bounds__(256) k_m2l(const SceneDesc *__restrict__ scenes,
+__global__ void __launch_bounds__(256, 6) k_m2l(const SceneDesc *__restrict__ scenes,
                                              const WorkItem *__restrict__ plist, uint32_t plist_cap,
                                              Counters *__restrict__ ctr, uint32_t list_par,
                                              const uint4 *__restrict__ mom,
                                              const float4 *__restrict__ src,
                                              float *__restrict__ lfield,
                                              const CUtensorMap *__restrict__ tmaps,
+                                             uint32_t lane_min,
                                              unsigned long long *__restrict__ stamp) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ uint32_t s_slots[kTileCells];  // the lane path's slot table
   // The TMA destination must be 128-byte aligned: align the carve-out by hand
   // (the launch reserves 128 spare bytes).
   const uint32_t pad = (128u - (smem_u32(smem_raw) & 127u)) & 127u;
@@ -454,12 +787,21 @@ __global__ void __launch_bounds__(256) k_m2l(const SceneDesc *__restrict__ scene
     sh.stop = 0u;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  for (uint32_t k = tid; k < kTileCells; k += blockDim.x) sh.slot_info[k] = m2l_slot_info(k);
+  for (uint32_t k = tid; k < kTileCells; k += blockDim.x) {
+    sh.slot_info[k] = m2l_slot_info(k);
+    s_slots[k] = m2l_slot_entry(k);
+  }
   grid_dependency_wait();  // the upward pass built the tree and the parent list
   stamp_begin(stamp);
   const uint32_t count = min(ctr->parents[list_par], plist_cap);
   if (blockIdx.x == 0 && tid == 0) ctr->parents[list_par ^ 1u] = 0u;  // reset for the next step
   __syncthreads();
+  if (count >= lane_min) {  // grid-uniform
+    m2l_lanes_pass(scenes, plist, count, mom, src, lfield, s_slots);
+    stamp_end(stamp);
+    grid_dependents_may_launch();
+    return;
+  }
   uint32_t phase = 0u;
 
   for (uint32_t item = blockIdx.x; item < count; item += gridDim.x) {
@@ -620,6 +962,96 @@ __global__ void __launch_bounds__(256) k_m2l(const SceneDesc *__restrict__ scene
   grid_dependents_may_launch();
 }
 
+// --------------------------------------------------- L2L + near, lanes
+//
+// One lane per target (long parent lists): lane t of the pass takes child
+// t & 7 of listed parent t >> 3 and carries all twelve field components
+// itself, so the top-down chain needs no shuffles and the 26 near terms are
+// added by the lane that forms them, in the same order as the warp path (an
+// absent or empty neighbour adds nothing: the running field is never -0, so
+// adding +0 would not change it).  Global warp w is warp w / gridDim.x of CTA
+// w % gridDim.x, so the list spreads over every multiprocessor.
+__device__ __forceinline__ void l2l_lanes_pass(const SceneDesc *__restrict__ scenes,
+                                               const WorkItem *__restrict__ plist, uint32_t count,
+                                               const uint4 *__restrict__ mom,
+                                               const float4 *__restrict__ src,
+                                               const float *__restrict__ lfield,
+                                               float *__restrict__ fields) {
+  const uint32_t lanes = 8u * count;
+  const uint32_t stride = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t gw = blockIdx.x + gridDim.x * (threadIdx.x >> 5u); 32u * gw < lanes; gw += stride) {
+    const uint32_t t = 32u * gw + (threadIdx.x & 31u);
+    if (t >= lanes) continue;
+    const WorkItem w = plist[t >> 3];
+    const SceneDesc &S = scenes[w.scene];
+    const uint32_t lp = w.cell == 0u ? 0u : level_of_d(w.cell);
+    const uint32_t l = lp + 1u, dim = 2u << lp;
+    uint32_t upx, upy, upz;
+    cell_coords_lv(w.cell - level_offset_d(lp), lp, upx, upy, upz);
+    const uint32_t ch = t & 7u;
+    const uint32_t tx = 2u * upx + (ch & 1u), ty = 2u * upy + ((ch >> 1) & 1u), tz = 2u * upz + (ch >> 2);
+    const uint32_t lvl_base = S.cell_off + level_offset_d(l);
+    const uint32_t target = lvl_base + lin3(tx, ty, tz, dim);
+    const uint32_t tcount = mom[target].x;
+    if (tcount == 0u) continue;
+
+    // f_a = m2l(a) + inherited(f_{a-1}) from the root field 0 (wgsl:574-611).
+    float f[10];
+#pragma unroll
+    for (int k = 0; k < 10; k++) f[k] = 0.0f;
+#pragma unroll
+    for (uint32_t a = 1u; a <= 6u; a++) {
+      if (a <= l) {
+        const uint32_t sh_ = l - a;
+        const uint32_t ax = tx >> sh_, ay = ty >> sh_, az = tz >> sh_;
+        const float4 *gp = reinterpret_cast<const float4 *>(
+            lfield + (size_t)(S.cell_off + level_offset_d(a) + lin3_lv(ax, ay, az, a)) * 12u);
+        const float4 g0 = __ldg(gp), g1 = __ldg(gp + 1), g2 = __ldg(gp + 2);
+        const float dx = cell_center_lv(ax, a) - cell_center_lv(ax >> 1, a - 1u);
+        const float dy = cell_center_lv(ay, a) - cell_center_lv(ay >> 1, a - 1u);
+        const float dz = cell_center_lv(az, a) - cell_center_lv(az >> 1, a - 1u);
+        // a += J . delta, phi -= a . delta, J unchanged (wgsl:603-609).
+        const float tax = (f[4] * dx + f[5] * dy) + f[6] * dz;
+        const float tay = (f[5] * dx + f[7] * dy) + f[8] * dz;
+        const float taz = (f[6] * dx + f[8] * dy) + f[9] * dz;
+        const float tph = (f[0] * dx + f[1] * dy) + f[2] * dz;
+        f[0] = g0.x + (f[0] + tax);
+        f[1] = g0.y + (f[1] + tay);
+        f[2] = g0.z + (f[2] + taz);
+        f[3] = g0.w + (f[3] + (-tph));
+        f[4] = g1.x + f[4];
+        f[5] = g1.y + f[5];
+        f[6] = g1.z + f[6];
+        f[7] = g1.w + f[7];
+        f[8] = g2.x + f[8];
+        f[9] = g2.y + f[9];
+      }
+    }
+
+    const bool leaf = tcount <= kAdaptive || l == S.depth;  // wgsl:537-541
+    if (leaf && S.near_mode == kNearReference) {
+      const float ctx = cell_center_lv(tx, l), cty = cell_center_lv(ty, l), ctz = cell_center_lv(tz, l);
+      const float near_eps = fmaxf(S.softening, (0.72f * kHalf) * pow2_neg(l));
+      for (uint32_t j = 0; j < 27u; j++) {
+        if (j == 13u) continue;  // the target itself
+        const int sx = (int)tx + (int)(j % 3u) - 1, sy = (int)ty + (int)((j / 3u) % 3u) - 1,
+                  sz = (int)tz + (int)(j / 9u) - 1;
+        if (sx < 0 || sy < 0 || sz < 0 || sx >= (int)dim || sy >= (int)dim || sz >= (int)dim) continue;
+        const float4 s = __ldg(&src[lvl_base + lin3((uint32_t)sx, (uint32_t)sy, (uint32_t)sz, dim)]);
+        if (s.w == 0.0f) continue;
+        float out[10];
+        pair_field_d(s, ctx, cty, ctz, near_eps, out);
+#pragma unroll
+        for (int k = 0; k < 10; k++) f[k] = f[k] + out[k];
+      }
+    }
+    float4 *fp = reinterpret_cast<float4 *>(fields + (size_t)target * 12u);
+    fp[0] = make_float4(f[0], f[1], f[2], f[3]);
+    fp[1] = make_float4(f[4], f[5], f[6], f[7]);
+    fp[2] = make_float4(f[8], f[9], 0.0f, 0.0f);
+  }
+}
+
 // ------------------------------------------------------------ L2L + near
 
 struct L2LShared {
@@ -635,6 +1067,7 @@ __global__ void __launch_bounds__(256) k_l2l_near(const SceneDesc *__restrict__ 
                                                   const float4 *__restrict__ src,
                                                   const float *__restrict__ lfield,
                                                   float *__restrict__ fields,
+                                                  uint32_t lane_min,
                                                   unsigned long long *__restrict__ stamp) {
   __shared__ L2LShared sh;
   const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
@@ -654,6 +1087,12 @@ __global__ void __launch_bounds__(256) k_l2l_near(const SceneDesc *__restrict__ 
   const uint32_t sc = lane < 4u ? (kSrcC >> (4u * lane)) & 15u : lane;
   const uint32_t sd = lane < 4u ? (kSrcD >> (4u * lane)) & 15u : lane;
   __syncthreads();
+  if (count >= lane_min) {  // grid-uniform
+    l2l_lanes_pass(scenes, plist, count, mom, src, lfield, fields);
+    stamp_end(stamp);
+    grid_dependents_may_launch();
+    return;
+  }
   for (uint32_t item = blockIdx.x; item < count; item += gridDim.x) {
     const WorkItem w = plist[item];
     const SceneDesc &S = scenes[w.scene];
@@ -765,6 +1204,18 @@ void launch_wait_check(cudaStream_t stream, uint32_t polls, uint32_t *status) {
 
 // --------------------------------------------------------------- launches
 
+// Work-list lengths from which the warp-per-subtree and lane-per-target
+// paths run, per tuning value (0: never, 1: always, 2: from the measured
+// crossovers: subtree tasks for the upward pass, listed parents for M2L and
+// L2L + near).
+constexpr uint32_t kNever = 0xFFFFFFFFu;
+constexpr uint32_t kUpwardWarpAuto = 4096u;
+constexpr uint32_t kM2LLaneAuto = 16384u;
+constexpr uint32_t kL2LLaneAuto = 2048u;
+static uint32_t lane_min(uint32_t mode, uint32_t automatic) {
+  return mode == 0u ? kNever : (mode == 1u ? 0u : automatic);
+}
+
 void launch_upward(const LaunchCtx &L, uint32_t list_par, uint32_t tasks) {
   const uint32_t grid = tasks < L.tree_ctas ? tasks : L.tree_ctas;
   // Clearing CTAs: one pass of 32 parents per warp covers 8 * 32 * clear_ctas
@@ -774,7 +1225,7 @@ void launch_upward(const LaunchCtx &L, uint32_t list_par, uint32_t tasks) {
   launch_step_kernel(L, k_upward, dim3(grid + clear), dim3(256), 0, L.scenes, L.task_scene,
                      L.task_list, tasks, L.mom, L.mom_next, L.src, L.aux, L.choice, L.fields,
                      L.plist, L.plist_cap, L.plist_prev, L.ctr, list_par, L.tickets, clear,
-                     stamp_rec(L, 0u));
+                     lane_min(L.upward_warps, kUpwardWarpAuto), stamp_rec(L, 0u));
 }
 
 size_t m2l_smem_bytes(bool compact) {
@@ -785,13 +1236,15 @@ void launch_m2l(const LaunchCtx &L, uint32_t list_par) {
   launch_step_kernel(L, L.m2l_compact ? k_m2l<true> : k_m2l<false>, dim3(L.m2l_ctas), dim3(256),
                      m2l_smem_bytes(L.m2l_compact), L.scenes,
                      (const WorkItem *)L.plist, L.plist_cap, L.ctr, list_par, (const uint4 *)L.mom,
-                     (const float4 *)L.src, L.lfield, L.tmaps, stamp_rec(L, 1u));
+                     (const float4 *)L.src, L.lfield, L.tmaps, lane_min(L.m2l_lanes, kM2LLaneAuto),
+                     stamp_rec(L, 1u));
 }
 
 void launch_l2l_near(const LaunchCtx &L, uint32_t list_par) {
   launch_step_kernel(L, k_l2l_near, dim3(L.l2l_ctas), dim3(256), 0, L.scenes, (const WorkItem *)L.plist,
                      L.plist_cap, (const Counters *)L.ctr, list_par, (const uint4 *)L.mom,
-                     (const float4 *)L.src, (const float *)L.lfield, L.fields, stamp_rec(L, 2u));
+                     (const float4 *)L.src, (const float *)L.lfield, L.fields,
+                     lane_min(L.l2l_lanes, kL2LLaneAuto), stamp_rec(L, 2u));
 }
 
 cudaError_t configure_tree_kernels() {

@@ -54,8 +54,12 @@ struct LaunchCtx {
   uint32_t l2l_ctas;           // persistent grid of the L2L + near pass
   bool integrate_dynamic;      // integrate CTAs grab tiles from a counter
   bool m2l_compact;            // M2L variant that lists contributing slots first
+  uint32_t m2l_lanes;          // M2L with one lane per target: 0 never, 1 always, 2 long lists
+  uint32_t l2l_lanes;          // L2L + near with one lane per target: the same
+  uint32_t upward_warps;       // upward with one warp (not one CTA) per subtree: the same
   const uint32_t *tile_list;   // active body tiles (null: every tile)
   const uint32_t *task_list;   // active upward tasks (null: every task)
+  const uint32_t *scene_list;  // active scenes (null: every scene)
   bool pdl;                    // launch step kernels with programmatic stream serialization
   bool p2p;                    // near field by exact pair sums (every scene in kNearP2P)
   float4 *pos4;                // leaf-sorted position snapshot (kNearP2P)
@@ -127,8 +131,13 @@ void launch_gather(const LaunchCtx &L, const uint32_t *perm, const float4 *part_
                    const uint32_t *tile_map = nullptr);
 // Leaf start tables of every kNearP2P scene from the sorted keys.
 void launch_leaf_starts(const LaunchCtx &L, const uint32_t *sorted_keys, uint32_t scenes);
+// Bodies of tiles [tile_base, tile_base + tiles) (or tile_map[0 ..]) back to
+// caller order: out[body_off + id] = part[slot].
 void launch_unpermute(const LaunchCtx &L, const uint32_t *ids, float4 *out, uint32_t tile_base,
-                      uint32_t tiles);
+                      uint32_t tiles, const uint32_t *tile_map = nullptr);
+// Cleared moments (both buffers), sources and records of the scenes in `which`.
+void launch_clear_scenes(const LaunchCtx &L, uint32_t nscenes, const SceneMask &which, uint4 *mom0,
+                         uint4 *mom1, float4 *src, float4 *aux);
 void launch_initialize(const LaunchCtx &L, float4 *part_out, uint32_t tile_base, uint32_t tiles);
 // Bodies of the scenes whose tiles are [tile_base, tile_base + tiles) copied
 // from src.p[scene - scene_base] (caller order, 16-byte aligned) into their slots.

@@ -152,6 +152,7 @@ struct Slot {
   SlotState state = kFree;
   Request *req = nullptr;
   cudaEvent_t ready = nullptr;  // staged input on the device / result in scratch
+  uint32_t buffer = 0;          // engine particle buffer holding the staged input / the result
 };
 
 }  // namespace
@@ -197,6 +198,7 @@ class Server {
   // worker counters (written by the worker thread under m_)
   uint64_t chunks_ = 0, pageable_inputs_ = 0;
   double active_sum_ = 0, wait_s_ = 0, admit_s_ = 0, lists_s_ = 0, step_s_ = 0, retire_s_ = 0;
+  double gpu_step_ms_ = 0, gpu_between_ms_ = 0;
 };
 
 int Server::create(const rfmm_server_config &cfg, Server **out) {
@@ -352,7 +354,12 @@ void Server::stage_loop(int k) {
       slots_[s].req = r;
       r->slot = s;
     }
-    float4 *dst = E_->slot_bodies((uint32_t)s);
+    // The engine's scratch particle buffer as of now (admission gathers from
+    // it into the current one; a resort that flips the buffers before
+    // admission makes the admission copy the slot across).
+    const uint32_t buf = E_->scratch_buffer();
+    slots_[s].buffer = buf;
+    float4 *dst = E_->slot_bodies((uint32_t)s, buf);
     cudaError_t e = cudaMemcpyAsync(dst, r->in(), 32ull * r->n, cudaMemcpyHostToDevice, copy_in_[k]);
     if (e == cudaSuccess) e = cudaEventRecord(slots_[s].ready, copy_in_[k]);
     if (e == cudaSuccess) e = cudaEventSynchronize(slots_[s].ready);
@@ -383,6 +390,36 @@ void Server::worker_loop() {
   std::vector<int> active;
   cudaEvent_t ahead[kRunAhead] = {};
   for (auto &ev : ahead) cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+  // Timing events around each chunk's step graph: chunk c uses entry
+  // c % kTimed; chunk c - kTimed + 1 is read back (long complete: the worker
+  // stays kRunAhead chunks ahead) just before entry c % kTimed, which holds
+  // its predecessor's end, is reused.
+  constexpr uint64_t kTimed = 8;
+  cudaEvent_t t_begin[kTimed] = {}, t_end[kTimed] = {};
+  for (uint64_t i = 0; i < kTimed; i++) {
+    cudaEventCreate(&t_begin[i]);
+    cudaEventCreate(&t_end[i]);
+  }
+  auto harvest = [&](uint64_t c) {  // c = the chunk about to be enqueued
+    if (c + 1 < kTimed) return;
+    const uint64_t j = (c + 1) % kTimed, pred = c % kTimed;
+    float step_ms = 0.0f, between_ms = 0.0f;
+    if (cudaEventSynchronize(t_end[j]) != cudaSuccess ||
+        cudaEventElapsedTime(&step_ms, t_begin[j], t_end[j]) != cudaSuccess)
+      return;
+    const bool has_pred = c >= kTimed;  // chunk c - kTimed exists
+    if (has_pred && cudaEventElapsedTime(&between_ms, t_end[pred], t_begin[j]) != cudaSuccess) between_ms = 0.0f;
+    std::lock_guard<std::mutex> lk(m_);
+    gpu_step_ms_ += step_ms;
+    gpu_between_ms_ += between_ms;
+  };
+  auto destroy_events = [&] {
+    for (auto &ev : ahead) cudaEventDestroy(ev);
+    for (uint64_t i = 0; i < kTimed; i++) {
+      cudaEventDestroy(t_begin[i]);
+      cudaEventDestroy(t_end[i]);
+    }
+  };
   uint64_t chunks = 0;
   bool lists_stale = false;  // slots retired since the last list refresh
   for (;;) {
@@ -391,7 +428,7 @@ void Server::worker_loop() {
       std::unique_lock<std::mutex> lk(m_);
       cv_.wait(lk, [&] { return stop_ || !staged_fifo_.empty() || !active.empty(); });
       if (stop_) {
-        for (auto &ev : ahead) cudaEventDestroy(ev);
+        destroy_events();
         return;
       }
       to_activate.assign(staged_fifo_.begin(), staged_fifo_.end());
@@ -404,7 +441,8 @@ void Server::worker_loop() {
     if (!to_activate.empty()) {
       // Every staged slot admitted with one sort.
       std::vector<Engine::Admission> adm;
-      for (int s : to_activate) adm.push_back({(uint32_t)s, slots_[s].req->n, slots_[s].req->params});
+      for (int s : to_activate)
+        adm.push_back({(uint32_t)s, slots_[s].req->n, slots_[s].req->params, slots_[s].buffer});
       st = E_->activate_many(adm);
       std::lock_guard<std::mutex> lk(m_);
       for (int s : to_activate) {
@@ -445,7 +483,10 @@ void Server::worker_loop() {
     const size_t n_active = active.size();
     uint32_t chunk = max_chunk_;
     for (int s : active) chunk = std::min(chunk, slots_[s].req->left);
+    harvest(chunks);
+    if (st == RFMM_OK) st = cuda_status(cudaEventRecord(t_begin[chunks % kTimed], E_->stream()));
     if (st == RFMM_OK) st = E_->step(chunk);
+    if (st == RFMM_OK) st = cuda_status(cudaEventRecord(t_end[chunks % kTimed], E_->stream()));
     if (st == RFMM_OK) st = cuda_status(cudaEventRecord(slot_ev, E_->stream()));
     chunks++;
     const double t4 = now_s();
@@ -454,15 +495,23 @@ void Server::worker_loop() {
       slots_[s].req->left -= chunk;
       if (slots_[s].req->left == 0u) finished.push_back(s);
     }
-    for (int s : finished) {
-      // Unpermute into scratch and empty the slot; the lists are refreshed
-      // before the next step.
-      if (st == RFMM_OK) st = E_->retire((uint32_t)s, false);
-      if (st == RFMM_OK) st = cuda_status(cudaEventRecord(slots_[s].ready, E_->stream()));
-      active.erase(std::find(active.begin(), active.end(), s));
+    if (!finished.empty()) {
+      // One unpermute into the scratch buffer for every finished slot; the
+      // emptied slots reach the device with the next admission or list
+      // refresh, before the next step.
+      std::vector<uint32_t> done(finished.begin(), finished.end());
+      if (st == RFMM_OK) st = E_->retire_many(done);
+      const uint32_t out_buf = E_->scratch_buffer();
+      for (int s : finished) {
+        slots_[s].buffer = out_buf;
+        if (st == RFMM_OK) st = cuda_status(cudaEventRecord(slots_[s].ready, E_->stream()));
+        active.erase(std::find(active.begin(), active.end(), s));
+      }
       std::lock_guard<std::mutex> lk(m_);
-      slots_[s].state = kDraining;
-      drain_fifo_.push_back(s);
+      for (int s : finished) {
+        slots_[s].state = kDraining;
+        drain_fifo_.push_back(s);
+      }
     }
     if (!finished.empty()) lists_stale = true;
     const double t5 = now_s();
@@ -497,7 +546,7 @@ void Server::drain_loop() {
     if (r->out_ring == nullptr) r->output.resize(32ull * r->n);
     cudaError_t e = cudaStreamWaitEvent(copy_out_, slots_[s].ready, 0);
     if (e == cudaSuccess)
-      e = cudaMemcpyAsync(r->out(), E_->slot_scratch((uint32_t)s), 32ull * r->n,
+      e = cudaMemcpyAsync(r->out(), E_->slot_bodies((uint32_t)s, slots_[s].buffer), 32ull * r->n,
                           cudaMemcpyDeviceToHost, copy_out_);
     if (e == cudaSuccess) e = cudaStreamSynchronize(copy_out_);
     std::lock_guard<std::mutex> lk(m_);
@@ -595,6 +644,8 @@ int Server::stats(rfmm_server_stats *out) {
   out->worker_lists_ms = 1e3 * lists_s_;
   out->worker_step_ms = 1e3 * step_s_;
   out->worker_retire_ms = 1e3 * retire_s_;
+  out->gpu_step_ms = gpu_step_ms_;
+  out->gpu_between_ms = gpu_between_ms_;
   return failure_;
 }
 

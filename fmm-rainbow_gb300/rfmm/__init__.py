@@ -72,7 +72,8 @@ class ServerStats(C.Structure):
                 ("chunks", C.c_uint64), ("mean_active_slots", C.c_double),
                 ("pageable_inputs", C.c_uint64), ("worker_gpu_wait_ms", C.c_double),
                 ("worker_admit_ms", C.c_double), ("worker_lists_ms", C.c_double),
-                ("worker_step_ms", C.c_double), ("worker_retire_ms", C.c_double)]
+                ("worker_step_ms", C.c_double), ("worker_retire_ms", C.c_double),
+                ("gpu_step_ms", C.c_double), ("gpu_between_ms", C.c_double)]
 
 
 class Tuning(C.Structure):
@@ -81,7 +82,8 @@ class Tuning(C.Structure):
     _fields_ = [("upward_ctas_per_sm", C.c_uint32), ("m2l_ctas_per_sm", C.c_uint32),
                 ("l2l_ctas_per_sm", C.c_uint32), ("integrate_ctas_per_sm", C.c_uint32),
                 ("integrate_dynamic", C.c_uint32), ("resort_interval", C.c_uint32),
-                ("graph_steps", C.c_uint32), ("pdl", C.c_uint32), ("m2l_compact", C.c_uint32)]
+                ("graph_steps", C.c_uint32), ("pdl", C.c_uint32), ("m2l_compact", C.c_uint32),
+                ("m2l_lanes", C.c_uint32), ("l2l_lanes", C.c_uint32), ("upward_warps", C.c_uint32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -297,6 +297,12 @@ typedef struct rfmm_tuning {
   uint32_t pdl;                   /* programmatic dependent launch between step kernels */
   uint32_t m2l_compact;           /* 1 (default): M2L lists each child's contributing slots
                                    * first; 0: every stencil slot, in chunks */
+  uint32_t m2l_lanes;             /* M2L with one lane per target, four parents per warp:
+                                   * 0 never, 1 always, 2 when the parent list is long */
+  uint32_t l2l_lanes;             /* L2L + near with one lane per target (else one warp):
+                                   * 0 never, 1 always, 2 when the parent list is long */
+  uint32_t upward_warps;          /* upward pass with one warp (else one CTA) per subtree:
+                                   * 0 never, 1 always, 2 when there are many subtrees */
 } rfmm_tuning;
 
 int rfmm_get_tuning(rfmm_handle *h, rfmm_tuning *out);
@@ -391,6 +397,11 @@ typedef struct rfmm_server_stats {
    * bound and list-buffer reuse), admitting slots (sort + deposit enqueue),
    * rebuilding the active lists, enqueuing steps, retiring finished slots. */
   double worker_gpu_wait_ms, worker_admit_ms, worker_lists_ms, worker_step_ms, worker_retire_ms;
+  /* Device time of the batched step chunks, and from the end of one chunk to
+   * the start of the next (admissions, list copies, retirements, and any
+   * time the GPU waited for the worker), from events around every chunk
+   * (all but the last few chunks). */
+  double gpu_step_ms, gpu_between_ms;
 } rfmm_server_stats;
 
 enum rfmm_request_state { RFMM_REQ_QUEUED = 0, RFMM_REQ_RUNNING = 1, RFMM_REQ_DONE = 2, RFMM_REQ_FAILED = 3 };

@@ -18,7 +18,10 @@ def _mixed_scenes():
     return [scenes.make(kind, n, 100 + i) for i, (kind, n) in enumerate(specs)]
 
 
-def test_batch_matches_oracle_per_scene(rfmm_mod, oracle_mod):
+@pytest.mark.parametrize("tree", ["warps", "lanes"])
+def test_batch_matches_oracle_per_scene(rfmm_mod, oracle_mod, tree):
+    """Both tree-kernel variants (one CTA or one warp per subtree, one warp or
+    one lane per target)."""
     O, R = oracle_mod, rfmm_mod
     ps = _mixed_scenes()
     g = [1.0, 0.5, 1.0, 1.0, 2.0, 1.0, 0.8, 1.0, 1.0, 1.2]
@@ -27,6 +30,9 @@ def test_batch_matches_oracle_per_scene(rfmm_mod, oracle_mod):
     with R.Batch([len(p) for p in ps], params) as b:
         depths = {pl[0] for pl in b.plans}
         assert depths == {4, 5, 6}
+        t = b.tuning()
+        t.m2l_lanes = t.l2l_lanes = t.upward_warps = int(tree == "lanes")
+        b.set_tuning(t)
         b.set_resort_interval(2)
         for i, p in enumerate(ps):
             b.upload(i, p)

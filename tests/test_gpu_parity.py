@@ -234,7 +234,11 @@ def test_tuning_never_changes_results(rfmm_mod, oracle_mod):
     st.step(6)
     variants = [dict(), dict(integrate_dynamic=1, graph_steps=4, pdl=0, m2l_compact=1),
                 dict(upward_ctas_per_sm=2, m2l_ctas_per_sm=1, l2l_ctas_per_sm=1,
-                     integrate_ctas_per_sm=1, resort_interval=3, graph_steps=1)]
+                     integrate_ctas_per_sm=1, resort_interval=3, graph_steps=1),
+                dict(m2l_lanes=1, l2l_lanes=1, upward_warps=1),
+                dict(m2l_lanes=0, l2l_lanes=0, upward_warps=0),
+                dict(m2l_lanes=2, l2l_lanes=2, upward_warps=1),
+                dict(m2l_lanes=1, l2l_lanes=1, m2l_ctas_per_sm=1, l2l_ctas_per_sm=1, pdl=0)]
     for v in variants:
         with _solver(R, n) as s:
             t = s.tuning()

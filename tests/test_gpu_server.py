@@ -67,3 +67,34 @@ def test_server_rejects_oversize_request(rfmm_mod):
         rid = srv.submit(scenes.uniform(4096, seed=1), 2)
         srv.wait(rid)
         assert srv.result(rid).shape == (4096,)
+
+
+def test_served_resorts_keep_results(rfmm_mod):
+    """Requests long enough that the engine re-sorts its active slots (every
+    16 steps) while they run, and requests staged before a re-sort flips the
+    particle buffers but admitted after it: each result still equals the
+    plain solve alone."""
+    R = rfmm_mod
+    from rfmm import scenes
+    rng = np.random.default_rng(77)
+    reqs = []
+    for i in range(16):
+        n = int(np.exp(rng.uniform(np.log(2000), np.log(90000))))
+        reqs.append((scenes.make(["plummer", "clusters4", "uniform"][i % 3], n, 800 + i),
+                     int(rng.integers(17, 46))))
+    prm = R.default_params(gravity=1.0, softening=1e-3, dt=5e-4)
+    with R.Server(max_bodies=131072, memory_budget_bytes=2 << 30, max_slots=4,
+                  max_chunk_steps=5) as srv:
+        ids = []
+        for p, steps in reqs:
+            ids.append(srv.submit(p, steps, prm))
+            time.sleep(0.001)
+        got = []
+        for rid in ids:
+            srv.wait(rid, 120000)
+            got.append(srv.result(rid))
+    for (p, steps), g in zip(reqs, got):
+        with R.Solver(len(p), prm) as s:
+            s.upload(p)
+            s.step(steps)
+            assert np.array_equal(_bits(g), _bits(s.particles())), (len(p), steps)
