@@ -78,6 +78,8 @@ def parse_args():
                          "the command profilers capture")
     ap.add_argument("--requests", type=int, default=0, help="served: requests per rate point")
     ap.add_argument("--rates", type=float, nargs="*", default=None, help="served: arrival rates /s")
+    ap.add_argument("--served-timeline", action="store_true",
+                    help="served: record the step kernels' in-graph timeline per rate point")
     ap.add_argument("--no-plain", action="store_true",
                     help="served: skip the back-to-back plain solves of the request list")
     ap.add_argument("--near", default="reference", choices=["reference", "p2p"],
@@ -685,10 +687,11 @@ def run_gpu_served(args, w):
     producers, collectors = 8, 4
     staging = 24 << 30  # pinned host staging of the server (inputs 18 GiB, results 6 GiB)
     body_steps = pool.body_steps()
+    fmode = rfmm.FLOAT_FAST if args.float == "fast" else rfmm.FLOAT_EXACT
 
     # Warm-up: module load and graph captures on a small server.
     warm = rfmm.Server(max_bodies=w["n_max"], memory_budget_bytes=2 << 30, max_slots=2,
-                       max_chunk_steps=4)
+                       max_chunk_steps=4, float_mode=fmode)
     for i in range(min(3, count)):
         rid = warm.submit(pool.bodies(i), int(pool.steps[i]), params)
         warm.wait(rid, 600000)
@@ -699,7 +702,8 @@ def run_gpu_served(args, w):
     clk = None
     for ri, rate in enumerate(rates):
         srv = rfmm.Server(max_bodies=w["n_max"], memory_budget_bytes=w["budget"],
-                          max_chunk_steps=4, staging_bytes=staging)
+                          max_chunk_steps=4, staging_bytes=staging, float_mode=fmode,
+                          timeline=args.served_timeline)
         arrivals = np.cumsum(np.random.default_rng(w["seed"] + ri).exponential(1.0 / rate, count))
         ids = [None] * count
         actual = np.zeros(count)
@@ -743,6 +747,7 @@ def run_gpu_served(args, w):
             raise errors[0]
         wall = time.perf_counter() - t0
         st = srv.stats()
+        tl = srv.timeline() if args.served_timeline else None
         srv.close()
         lag = (actual - (t0 + arrivals)) * 1e3
         sweep.append({"offered_rate_per_s": rate,
@@ -759,6 +764,12 @@ def run_gpu_served(args, w):
                                                     "worker_admit_ms", "worker_lists_ms",
                                                     "worker_step_ms", "worker_retire_ms",
                                                     "gpu_step_ms", "gpu_between_ms")}})
+        if tl is not None:
+            sweep[-1]["timeline"] = {
+                "note": "most recent run of each captured step graph",
+                "steps": tl["steps"], "span_ms_per_step": tl["span_ms"] / max(tl["steps"], 1),
+                "busy_ms_per_launch": {k: v["busy_ms"] / v["launches"]
+                                       for k, v in tl["kinds"].items() if v["launches"]}}
     clocks = clocks_summary(clk)
 
     # The same request list back to back through plain handles: each request
@@ -767,6 +778,7 @@ def run_gpu_served(args, w):
     plain_s = 0.0
     for i in range(count if not args.no_plain else 0):
         s = rfmm.Solver(int(pool.n[i]), params)
+        s.set_float_mode(fmode)
         torch.cuda.synchronize()
         t = time.perf_counter()
         s.upload(pool.bodies(i))
@@ -782,6 +794,7 @@ def run_gpu_served(args, w):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded, numpy PCG64): " + w["desc"],
         "config": {"workload": args.workload, "form": "served (continuous batching)",
+                   "float_mode": args.float,
                    "requests_per_rate": count, "body_steps_per_rate": body_steps,
                    "memory_budget_bytes": w["budget"], "slot_capacity": w["n_max"],
                    "producer_threads": producers, "collector_threads": collectors,

@@ -562,6 +562,7 @@ LaunchCtx Engine::ctx(uint32_t mpar, uint32_t lpar, uint32_t ppar) const {
   L.m2l_lanes = tuning_.m2l_lanes;
   L.l2l_lanes = tuning_.l2l_lanes;
   L.upward_warps = tuning_.upward_warps;
+  L.many_scenes = scenes_.size() > 1u;
   L.tile_list = use_lists_ ? d_tile_list_ : nullptr;
   L.task_list = use_lists_ ? d_task_list_ : nullptr;
   L.scene_list = use_lists_ ? d_scene_list_ : nullptr;
@@ -984,7 +985,36 @@ int Engine::solve_fields() {
 }
 
 int Engine::launch_chunk(uint32_t len, bool sort_at_end) {
-  const auto key = std::make_tuple(len, mcur_, lpar_, pcur_.load(), sort_at_end);
+  Graph *g = nullptr;
+  const int st = capture_chunk(len, mcur_, lpar_, pcur_.load(), sort_at_end, &g);
+  if (st != RFMM_OK) return st;
+  RF_CK(cudaGraphLaunch(g->exec, stream_));
+  launches_ += g->kernels;
+  const uint32_t flip = len & 1u;
+  tree_buf_ = (int)(mcur_ ^ ((len - 1u) & 1u));
+  mcur_ ^= flip;
+  lpar_ ^= flip;
+  if (sort_at_end) pcur_ ^= 1u;
+  return RFMM_OK;
+}
+
+int Engine::prepare_graphs(uint32_t max_len) {
+  if (max_len == 0u || max_len > tuning_.graph_steps) return RFMM_ERR_INVALID;
+  for (uint32_t len = 1; len <= max_len; len++)
+    for (uint32_t m = 0; m < 2u; m++)
+      for (uint32_t l = 0; l < 2u; l++)
+        for (uint32_t p = 0; p < 2u; p++)
+          for (int sort = 0; sort < (resort_interval_ > 0 ? 2 : 1); sort++) {
+            Graph *g = nullptr;
+            const int st = capture_chunk(len, m, l, p, sort != 0, &g);
+            if (st != RFMM_OK) return st;
+          }
+  return RFMM_OK;
+}
+
+int Engine::capture_chunk(uint32_t len, uint32_t mcur, uint32_t lpar, uint32_t pcur, bool sort_at_end,
+                          Graph **out) {
+  const auto key = std::make_tuple(len, mcur, lpar, pcur, sort_at_end);
   auto it = graphs_.find(key);
   if (it == graphs_.end()) {
     // Timeline: this graph's records, cleared by its first node.
@@ -1000,10 +1030,10 @@ int Engine::launch_chunk(uint32_t len, bool sort_at_end) {
     if (rec != nullptr)
       cudaMemsetAsync(rec, 0, 8ull * kStampSteps * kStampWordsPerStep, stream_);
     for (uint32_t j = 0; j < len; j++)
-      enqueue_step(mcur_ ^ (j & 1u), lpar_ ^ (j & 1u), pcur_,
+      enqueue_step(mcur ^ (j & 1u), lpar ^ (j & 1u), pcur,
                    rec != nullptr ? rec + (size_t)j * kStampWordsPerStep : nullptr);
     if (sort_at_end)
-      enqueue_resort(pcur_, mcur_ ^ (len & 1u),
+      enqueue_resort(pcur, mcur ^ (len & 1u),
                      rec != nullptr ? rec + (size_t)(len - 1u) * kStampWordsPerStep : nullptr);
     cudaError_t e = cudaStreamEndCapture(stream_, &g);
     if (e != cudaSuccess) {
@@ -1017,13 +1047,7 @@ int Engine::launch_chunk(uint32_t len, bool sort_at_end) {
     const uint32_t kernels = len * kernels_per_step() + (sort_at_end ? resort_kernels() : 0u);
     it = graphs_.emplace(key, Graph{exec, kernels, len, sort_at_end, region}).first;
   }
-  RF_CK(cudaGraphLaunch(it->second.exec, stream_));
-  launches_ += it->second.kernels;
-  const uint32_t flip = len & 1u;
-  tree_buf_ = (int)(mcur_ ^ ((len - 1u) & 1u));
-  mcur_ ^= flip;
-  lpar_ ^= flip;
-  if (sort_at_end) pcur_ ^= 1u;
+  *out = &it->second;
   return RFMM_OK;
 }
 

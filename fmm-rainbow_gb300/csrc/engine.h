@@ -95,6 +95,9 @@ class Engine {
   // which must come before the next step.
   int retire_many(const std::vector<uint32_t> &slots);
   int refresh_lists();
+  // Captures the step graphs of every chunk length up to max_len and every
+  // buffer parity ahead of time (serving: no capture while requests wait).
+  int prepare_graphs(uint32_t max_len);
   // Seconds refresh_lists spent waiting for a pinned list block's last copy.
   double list_wait_seconds() const { return list_wait_s_; }
   // Serving: a slot's bodies in particle buffer `buffer`.  Stage-in writes
@@ -285,6 +288,9 @@ class Engine {
   uint32_t stamp_regions_used_ = 0;
   unsigned long long *d_stamps_ = nullptr;
   std::map<std::tuple<uint32_t, uint32_t, uint32_t, uint32_t, bool>, Graph> graphs_;
+  // The step graph of `len` steps from the given buffer parities (captured
+  // and instantiated on first use).
+  int capture_chunk(uint32_t len, uint32_t mcur, uint32_t lpar, uint32_t pcur, bool sort_at_end, Graph **out);
   uint64_t launches_ = 0;  // kernels this engine has launched (graph nodes included)
   uint32_t resort_kernels() const { return 4u; }
   cudaEvent_t ev_[8] = {};

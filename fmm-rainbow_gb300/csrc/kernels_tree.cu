@@ -37,6 +37,7 @@
 #include <cuda_runtime.h>
 
 #include <type_traits>
+#include <utility>
 
 #include "rfmm_device.cuh"
 #include "rfmm_kernels.h"
@@ -535,6 +536,7 @@ __device__ __forceinline__ void upward_warp_task(
 // task when null).  The first `clear_ctas` CTAs only clear the fields of the
 // previous step's targets (children of its listed parents; fields are zero
 // off the M2L path), so the subtree CTAs start their reductions at once.
+template <bool kWide>
 __global__ void __launch_bounds__(256, 4) k_upward(const SceneDesc *__restrict__ scenes,
                                                 const uint32_t *__restrict__ task_scene,
                                                 const uint32_t *__restrict__ task_list,
@@ -566,7 +568,7 @@ __global__ void __launch_bounds__(256, 4) k_upward(const SceneDesc *__restrict__
   // before waiting for that kernel.
   const uint32_t cta = blockIdx.x - clear_ctas, ncta = gridDim.x - clear_ctas;
   const uint32_t ntasks = task_list != nullptr ? min(ctr->tasks_active, ntasks_all) : ntasks_all;
-  if (ntasks >= warp_min) {  // grid-uniform: one warp per subtree
+  if (kWide && ntasks >= warp_min) {  // grid-uniform: one warp per subtree
     const uint32_t wpb = blockDim.x >> 5, warp = threadIdx.x >> 5;
     grid_dependency_wait();  // the previous integrate deposited into mom_next
     stamp_begin(stamp);
@@ -764,7 +766,7 @@ __device__ __forceinline__ void m2l_lanes_pass(const SceneDesc *__restrict__ sce
   }
 }
 
-template <bool kCompact>
+template <bool kCompact, bool kWide>
 __global__ void __launch_bounds__(256, 6) k_m2l(const SceneDesc *__restrict__ scenes,
                                              const WorkItem *__restrict__ plist, uint32_t plist_cap,
                                              Counters *__restrict__ ctr, uint32_t list_par,
@@ -789,14 +791,14 @@ __global__ void __launch_bounds__(256, 6) k_m2l(const SceneDesc *__restrict__ sc
   }
   for (uint32_t k = tid; k < kTileCells; k += blockDim.x) {
     sh.slot_info[k] = m2l_slot_info(k);
-    s_slots[k] = m2l_slot_entry(k);
+    if (kWide) s_slots[k] = m2l_slot_entry(k);
   }
   grid_dependency_wait();  // the upward pass built the tree and the parent list
   stamp_begin(stamp);
   const uint32_t count = min(ctr->parents[list_par], plist_cap);
   if (blockIdx.x == 0 && tid == 0) ctr->parents[list_par ^ 1u] = 0u;  // reset for the next step
   __syncthreads();
-  if (count >= lane_min) {  // grid-uniform
+  if (kWide && count >= lane_min) {  // grid-uniform
     m2l_lanes_pass(scenes, plist, count, mom, src, lfield, s_slots);
     stamp_end(stamp);
     grid_dependents_may_launch();
@@ -1059,6 +1061,7 @@ struct L2LShared {
   float centre[127];  // cell_center_lv(c, l) at [2^l - 1 + c], levels 0..6
 };
 
+template <bool kWide>
 __global__ void __launch_bounds__(256) k_l2l_near(const SceneDesc *__restrict__ scenes,
                                                   const WorkItem *__restrict__ plist,
                                                   uint32_t plist_cap,
@@ -1087,7 +1090,7 @@ __global__ void __launch_bounds__(256) k_l2l_near(const SceneDesc *__restrict__ 
   const uint32_t sc = lane < 4u ? (kSrcC >> (4u * lane)) & 15u : lane;
   const uint32_t sd = lane < 4u ? (kSrcD >> (4u * lane)) & 15u : lane;
   __syncthreads();
-  if (count >= lane_min) {  // grid-uniform
+  if (kWide && count >= lane_min) {  // grid-uniform
     l2l_lanes_pass(scenes, plist, count, mom, src, lfield, fields);
     stamp_end(stamp);
     grid_dependents_may_launch();
@@ -1215,6 +1218,11 @@ constexpr uint32_t kL2LLaneAuto = 2048u;
 static uint32_t lane_min(uint32_t mode, uint32_t automatic) {
   return mode == 0u ? kNever : (mode == 1u ? 0u : automatic);
 }
+// The kernels carrying the second path are launched only where it can run:
+// forced on, or automatic in an engine of several scenes (one scene's lists
+// stay below the crossovers; the second path's code costs the per-item path
+// registers and time).
+static bool wide(uint32_t mode, const LaunchCtx &L) { return mode == 1u || (mode == 2u && L.many_scenes); }
 
 void launch_upward(const LaunchCtx &L, uint32_t list_par, uint32_t tasks) {
   const uint32_t grid = tasks < L.tree_ctas ? tasks : L.tree_ctas;
@@ -1222,7 +1230,8 @@ void launch_upward(const LaunchCtx &L, uint32_t list_par, uint32_t tasks) {
   // listed parents.
   uint32_t clear = (L.plist_cap + 2047u) / 2048u;
   clear = clear < 8u ? 8u : (clear > 64u ? 64u : clear);
-  launch_step_kernel(L, k_upward, dim3(grid + clear), dim3(256), 0, L.scenes, L.task_scene,
+  launch_step_kernel(L, wide(L.upward_warps, L) ? k_upward<true> : k_upward<false>, dim3(grid + clear),
+                     dim3(256), 0, L.scenes, L.task_scene,
                      L.task_list, tasks, L.mom, L.mom_next, L.src, L.aux, L.choice, L.fields,
                      L.plist, L.plist_cap, L.plist_prev, L.ctr, list_par, L.tickets, clear,
                      lane_min(L.upward_warps, kUpwardWarpAuto), stamp_rec(L, 0u));
@@ -1233,7 +1242,10 @@ size_t m2l_smem_bytes(bool compact) {
 }
 
 void launch_m2l(const LaunchCtx &L, uint32_t list_par) {
-  launch_step_kernel(L, L.m2l_compact ? k_m2l<true> : k_m2l<false>, dim3(L.m2l_ctas), dim3(256),
+  const bool w = wide(L.m2l_lanes, L);
+  auto kernel = L.m2l_compact ? (w ? k_m2l<true, true> : k_m2l<true, false>)
+                              : (w ? k_m2l<false, true> : k_m2l<false, false>);
+  launch_step_kernel(L, kernel, dim3(L.m2l_ctas), dim3(256),
                      m2l_smem_bytes(L.m2l_compact), L.scenes,
                      (const WorkItem *)L.plist, L.plist_cap, L.ctr, list_par, (const uint4 *)L.mom,
                      (const float4 *)L.src, L.lfield, L.tmaps, lane_min(L.m2l_lanes, kM2LLaneAuto),
@@ -1241,18 +1253,25 @@ void launch_m2l(const LaunchCtx &L, uint32_t list_par) {
 }
 
 void launch_l2l_near(const LaunchCtx &L, uint32_t list_par) {
-  launch_step_kernel(L, k_l2l_near, dim3(L.l2l_ctas), dim3(256), 0, L.scenes, (const WorkItem *)L.plist,
+  launch_step_kernel(L, wide(L.l2l_lanes, L) ? k_l2l_near<true> : k_l2l_near<false>, dim3(L.l2l_ctas),
+                     dim3(256), 0, L.scenes, (const WorkItem *)L.plist,
                      L.plist_cap, (const Counters *)L.ctr, list_par, (const uint4 *)L.mom,
                      (const float4 *)L.src, (const float *)L.lfield, L.fields,
                      lane_min(L.l2l_lanes, kL2LLaneAuto), stamp_rec(L, 2u));
 }
 
 cudaError_t configure_tree_kernels() {
-  cudaError_t e = cudaFuncSetAttribute(k_m2l<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)m2l_smem_bytes(false));
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_m2l<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)m2l_smem_bytes(true));
+  cudaError_t e = cudaSuccess;
+  const std::pair<void (*)(const SceneDesc *, const WorkItem *, uint32_t, Counters *, uint32_t,
+                            const uint4 *, const float4 *, float *, const CUtensorMap *, uint32_t,
+                            unsigned long long *),
+                  bool>
+      m2l[4] = {{k_m2l<false, false>, false}, {k_m2l<false, true>, false}, {k_m2l<true, false>, true},
+                {k_m2l<true, true>, true}};
+  for (const auto &k : m2l)
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k.first, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)m2l_smem_bytes(k.second));
   return e;
 }
 

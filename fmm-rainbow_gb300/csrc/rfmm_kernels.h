@@ -57,6 +57,7 @@ struct LaunchCtx {
   uint32_t m2l_lanes;          // M2L with one lane per target: 0 never, 1 always, 2 long lists
   uint32_t l2l_lanes;          // L2L + near with one lane per target: the same
   uint32_t upward_warps;       // upward with one warp (not one CTA) per subtree: the same
+  bool many_scenes;            // the engine holds more than one scene
   const uint32_t *tile_list;   // active body tiles (null: every tile)
   const uint32_t *task_list;   // active upward tasks (null: every task)
   const uint32_t *scene_list;  // active scenes (null: every scene)

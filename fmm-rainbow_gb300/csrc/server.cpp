@@ -168,6 +168,7 @@ class Server {
   int wait(uint64_t id, uint32_t timeout_ms);
   int result(uint64_t id, void *dst, size_t bytes);
   int stats(rfmm_server_stats *out);
+  int timeline(rfmm_timeline *out);
 
  private:
   void stage_loop(int k);
@@ -180,8 +181,13 @@ class Server {
   uint32_t max_chunk_ = 4;
   cudaStream_t copy_in_[kStageThreads] = {}, copy_out_ = nullptr;
   PinnedRing in_ring_, out_ring_;
+  // Pinned bounce buffers (one largest request each) for inputs and results
+  // that missed the rings: the copies stay asynchronous device transfers
+  // from pinned memory instead of taking the driver's pageable path.
+  uint8_t *bounce_in_[kStageThreads] = {}, *bounce_out_ = nullptr;
   std::vector<Slot> slots_;
   std::mutex m_;
+  std::mutex eng_m_;  // the engine: held by the worker for an iteration, and by timeline()
   std::condition_variable cv_;  // any state change
   std::deque<Request *> queue_;
   std::deque<int> staged_fifo_, drain_fifo_;
@@ -233,7 +239,20 @@ int Server::create(const rfmm_server_config &cfg, Server **out) {
     return st;
   }
   cudaGetDevice(&S->device_);
+  if (cfg.float_mode > 1u) {
+    delete S;
+    return RFMM_ERR_INVALID;
+  }
+  st = S->E_->set_float_mode(cfg.float_mode);
+  if (st == RFMM_OK && cfg.timeline != 0u) st = S->E_->set_timeline(true);
+  // Every step graph a chunk can need, captured now rather than while the
+  // first requests wait.
   S->max_chunk_ = cfg.max_chunk_steps ? cfg.max_chunk_steps : 4u;
+  if (st == RFMM_OK) st = S->E_->prepare_graphs(std::min(S->max_chunk_, 16u));
+  if (st != RFMM_OK) {
+    delete S;
+    return st;
+  }
   // Staging: three quarters for inputs (they wait in the queue), one quarter
   // for results; at least one largest request each.
   const uint64_t staging = cfg.staging_bytes ? cfg.staging_bytes : kDefaultStagingBytes;
@@ -245,6 +264,9 @@ int Server::create(const rfmm_server_config &cfg, Server **out) {
   }
   S->slots_.resize(nslots);
   cudaError_t e = cudaSuccess;
+  for (auto &b : S->bounce_in_)
+    if (e == cudaSuccess) e = cudaHostAlloc((void **)&b, one, cudaHostAllocDefault);
+  if (e == cudaSuccess) e = cudaHostAlloc((void **)&S->bounce_out_, one, cudaHostAllocDefault);
   for (auto &cs : S->copy_in_)
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&S->copy_out_, cudaStreamNonBlocking);
@@ -284,6 +306,9 @@ Server::~Server() {
     cudaStreamSynchronize(copy_out_);
     cudaStreamDestroy(copy_out_);
   }
+  for (auto &b : bounce_in_)
+    if (b != nullptr) cudaFreeHost(b);
+  if (bounce_out_ != nullptr) cudaFreeHost(bounce_out_);
   delete E_;
 }
 
@@ -360,7 +385,12 @@ void Server::stage_loop(int k) {
     const uint32_t buf = E_->scratch_buffer();
     slots_[s].buffer = buf;
     float4 *dst = E_->slot_bodies((uint32_t)s, buf);
-    cudaError_t e = cudaMemcpyAsync(dst, r->in(), 32ull * r->n, cudaMemcpyHostToDevice, copy_in_[k]);
+    const void *from = r->in();
+    if (r->in_ring == nullptr) {  // missed the ring: through this thread's bounce buffer
+      std::memcpy(bounce_in_[k], r->input.data(), 32ull * r->n);
+      from = bounce_in_[k];
+    }
+    cudaError_t e = cudaMemcpyAsync(dst, from, 32ull * r->n, cudaMemcpyHostToDevice, copy_in_[k]);
     if (e == cudaSuccess) e = cudaEventRecord(slots_[s].ready, copy_in_[k]);
     if (e == cudaSuccess) e = cudaEventSynchronize(slots_[s].ready);
     in_ring_.release(r->in_ring);  // the input is on the device (or the copy failed)
@@ -434,6 +464,7 @@ void Server::worker_loop() {
       to_activate.assign(staged_fifo_.begin(), staged_fifo_.end());
       staged_fifo_.clear();
     }
+    std::lock_guard<std::mutex> engine_lock(eng_m_);  // until the end of this iteration
     // Admissions; then one refresh of the active lists covers them and the
     // retirements of the previous iteration.
     double t0 = now_s();
@@ -545,10 +576,13 @@ void Server::drain_loop() {
     r->out_ring = out_ring_.alloc(32ull * r->n);
     if (r->out_ring == nullptr) r->output.resize(32ull * r->n);
     cudaError_t e = cudaStreamWaitEvent(copy_out_, slots_[s].ready, 0);
+    // A result that missed the output ring goes through the bounce buffer.
+    uint8_t *to = r->out_ring != nullptr ? r->out_ring : bounce_out_;
     if (e == cudaSuccess)
-      e = cudaMemcpyAsync(r->out(), E_->slot_bodies((uint32_t)s, slots_[s].buffer), 32ull * r->n,
+      e = cudaMemcpyAsync(to, E_->slot_bodies((uint32_t)s, slots_[s].buffer), 32ull * r->n,
                           cudaMemcpyDeviceToHost, copy_out_);
     if (e == cudaSuccess) e = cudaStreamSynchronize(copy_out_);
+    if (e == cudaSuccess && r->out_ring == nullptr) std::memcpy(r->output.data(), bounce_out_, 32ull * r->n);
     std::lock_guard<std::mutex> lk(m_);
     r->t_done = now_s();
     if (e != cudaSuccess) {
@@ -649,6 +683,12 @@ int Server::stats(rfmm_server_stats *out) {
   return failure_;
 }
 
+int Server::timeline(rfmm_timeline *out) {
+  if (out == nullptr) return RFMM_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(eng_m_);
+  return E_->get_timeline(out);
+}
+
 }  // namespace rfmm
 
 struct rfmm_server {
@@ -715,6 +755,11 @@ int rfmm_server_result(rfmm_server *srv, uint64_t request_id, void *host_dst, si
 int rfmm_server_get_stats(rfmm_server *srv, rfmm_server_stats *out) {
   if (srv == nullptr) return RFMM_ERR_INVALID;
   return srv->impl->stats(out);
+}
+
+int rfmm_server_get_timeline(rfmm_server *srv, rfmm_timeline *out) {
+  if (srv == nullptr) return RFMM_ERR_INVALID;
+  return srv->impl->timeline(out);
 }
 
 }  // extern "C"

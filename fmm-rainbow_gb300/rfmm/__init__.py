@@ -60,7 +60,7 @@ class Params(C.Structure):
 class ServerConfig(C.Structure):
     _fields_ = [("memory_budget_bytes", C.c_uint64), ("max_bodies", C.c_uint32),
                 ("max_slots", C.c_uint32), ("max_chunk_steps", C.c_uint32),
-                ("staging_bytes", C.c_uint64)]
+                ("staging_bytes", C.c_uint64), ("float_mode", C.c_uint32), ("timeline", C.c_uint32)]
 
 
 class ServerStats(C.Structure):
@@ -213,6 +213,7 @@ SIGNATURES = {
     "rfmm_server_wait": (_i, [_vp, C.c_uint64, _u32]),
     "rfmm_server_result": (_i, [_vp, C.c_uint64, _vp, _sz]),
     "rfmm_server_get_stats": (_i, [_vp, C.POINTER(ServerStats)]),
+    "rfmm_server_get_timeline": (_i, [_vp, C.POINTER(Timeline)]),
 }
 KERNEL_KINDS = ("upward", "m2l", "l2l_near", "integrate", "resort", "near_p2p")
 
@@ -622,9 +623,9 @@ class Server:
     """Continuous-batching solve server (the `rfmm_server_*` handle)."""
 
     def __init__(self, max_bodies, memory_budget_bytes=8 << 30, max_slots=0, max_chunk_steps=0,
-                 staging_bytes=0):
+                 staging_bytes=0, float_mode=FLOAT_EXACT, timeline=False):
         cfg = ServerConfig(memory_budget_bytes, max_bodies, max_slots, max_chunk_steps,
-                           staging_bytes)
+                           staging_bytes, float_mode, 1 if timeline else 0)
         self._h = C.c_void_p()
         _check(lib().rfmm_server_create(C.byref(cfg), C.byref(self._h)), "rfmm_server_create")
         self._n = {}
@@ -691,3 +692,9 @@ class Server:
         st = ServerStats()
         _check(lib().rfmm_server_get_stats(self._h, C.byref(st)), "rfmm_server_get_stats")
         return {k: getattr(st, k) for k, _ in ServerStats._fields_}
+
+    def timeline(self) -> dict:
+        """The step kernels' in-graph timeline (server created with timeline=True)."""
+        t = Timeline()
+        _check(lib().rfmm_server_get_timeline(self._h, C.byref(t)), "rfmm_server_get_timeline")
+        return t.as_dict()

@@ -381,6 +381,9 @@ typedef struct rfmm_server_config {
   uint32_t max_chunk_steps;     /* steps between admission points (0 = 4) */
   uint64_t staging_bytes;       /* pinned host memory for request inputs (3/4) and
                                  * results (1/4); 0 = 4 GiB */
+  uint32_t float_mode;          /* RFMM_FLOAT_EXACT (0) or RFMM_FLOAT_FAST for every request */
+  uint32_t timeline;            /* 1: record the step kernels' in-graph timeline
+                                 * (rfmm_server_get_timeline) */
 } rfmm_server_config;
 
 typedef struct rfmm_server_stats {
@@ -407,6 +410,10 @@ typedef struct rfmm_server_stats {
 enum rfmm_request_state { RFMM_REQ_QUEUED = 0, RFMM_REQ_RUNNING = 1, RFMM_REQ_DONE = 2, RFMM_REQ_FAILED = 3 };
 
 int rfmm_server_create(const rfmm_server_config *config, rfmm_server **out);
+/* The step kernels' timeline (the most recent run of each captured graph)
+ * when the server was created with timeline = 1; waits for the worker's
+ * current iteration. */
+int rfmm_server_get_timeline(rfmm_server *server, rfmm_timeline *out);
 int rfmm_server_destroy(rfmm_server *server);
 /* Copies the n bodies (n x 32 B) before it returns (into a pinned staging
  * buffer when one is free); returns RFMM_ERR_BUDGET if n exceeds the slot

@@ -98,3 +98,31 @@ def test_served_resorts_keep_results(rfmm_mod):
             s.upload(p)
             s.step(steps)
             assert np.array_equal(_bits(g), _bits(s.particles())), (len(p), steps)
+
+
+def test_server_fast_float_mode_and_timeline(rfmm_mod):
+    """A server created with the fast float variant gives each request the
+    plain fast solve's result bit for bit, and its timeline records the step
+    kernels."""
+    R = rfmm_mod
+    from rfmm import scenes
+    reqs = [(scenes.make(k, n, 860 + i), st) for i, (k, n, st) in
+            enumerate([("plummer", 40000, 9), ("uniform", 20000, 20), ("clusters4", 60000, 5)])]
+    prm = R.default_params(gravity=1.0, softening=1e-3, dt=5e-4)
+    with R.Server(max_bodies=65536, memory_budget_bytes=1 << 30, max_slots=3, max_chunk_steps=4,
+                  float_mode=R.FLOAT_FAST, timeline=True) as srv:
+        ids = [srv.submit(p, steps, prm) for p, steps in reqs]
+        got = []
+        for rid in ids:
+            srv.wait(rid, 120000)
+            got.append(srv.result(rid))
+        tl = srv.timeline()
+    assert tl["steps"] > 0
+    for kind in ("upward", "m2l", "l2l_near", "integrate"):
+        assert tl["kinds"][kind]["launches"] > 0 and tl["kinds"][kind]["busy_ms"] > 0.0, kind
+    for (p, steps), g in zip(reqs, got):
+        with R.Solver(len(p), prm) as s:
+            s.set_float_mode(R.FLOAT_FAST)
+            s.upload(p)
+            s.step(steps)
+            assert np.array_equal(_bits(g), _bits(s.particles())), (len(p), steps)
