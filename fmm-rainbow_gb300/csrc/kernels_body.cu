@@ -370,8 +370,17 @@ __global__ void __launch_bounds__(256, 6) k_integrate(const SceneDesc *__restric
     __syncthreads();
     return s_next;
   };
-  uint32_t i = dynamic ? grab() : blockIdx.x;
+  // Static schedule: runs of `run` consecutive tiles, interleaved over the
+  // CTAs (CTA c takes runs c, c + G, ...).  Single tiles balance best; with
+  // at least 16 tiles per CTA (many scenes, whose tiles are contiguous) runs
+  // of 4 make the tile's scene change, and its descriptor reload, rarer.
   const uint32_t end = ntiles;
+  const uint32_t run_log2 = end >= 16u * gridDim.x ? 2u : 0u;
+  uint32_t k = 0u;  // this CTA's static tile count so far
+  auto static_tile = [&](uint32_t kk) {
+    return (((kk >> run_log2) * gridDim.x + blockIdx.x) << run_log2) + (kk & ((1u << run_log2) - 1u));
+  };
+  uint32_t i = dynamic ? grab() : static_tile(k);
   uint32_t cur = 0xFFFFFFFFu;
   // The next tile's bodies are loaded one iteration ahead.
   float4 n0 = make_float4(0.f, 0.f, 0.f, 0.f), n1 = n0;
@@ -384,7 +393,7 @@ __global__ void __launch_bounds__(256, 6) k_integrate(const SceneDesc *__restric
     const uint32_t tile = next_tile;
     const uint32_t slot = tile * kTile + threadIdx.x;
     float4 p0 = n0, p1 = n1;
-    const uint32_t ni = dynamic ? grab() : i + gridDim.x;
+    const uint32_t ni = dynamic ? grab() : static_tile(++k);
     if (ni < end) {
       next_tile = tile_list != nullptr ? tile_list[ni] : ni;
       n0 = part[2u * (next_tile * kTile + threadIdx.x)];
