@@ -238,6 +238,9 @@ int Engine::create(const std::vector<SceneSpec> &specs, Engine **out) {
     for (auto &ev : E->ev_)
       if (e == cudaSuccess) e = cudaEventCreate(&ev);
   }
+  if (e == cudaSuccess && E->use_lists_) e = cudaStreamCreateWithFlags(&E->admit_stream_, cudaStreamNonBlocking);
+  if (e == cudaSuccess && E->use_lists_) e = cudaEventCreateWithFlags(&E->admit_ev_, cudaEventDisableTiming);
+  if (e == cudaSuccess && E->use_lists_) e = cudaEventCreateWithFlags(&E->refresh_ev_, cudaEventDisableTiming);
   if (e == cudaSuccess) e = configure_tree_kernels();
   if (e == cudaSuccess) e = fast::configure_tree_kernels();
   // Both variants' integrate grids must fit: the smaller resident count.
@@ -343,6 +346,12 @@ Engine::~Engine() {
       if (m->ev[b] != nullptr) cudaEventDestroy(m->ev[b]);
     }
   }
+  if (admit_stream_ != nullptr) {
+    cudaStreamSynchronize(admit_stream_);
+    cudaStreamDestroy(admit_stream_);
+  }
+  if (admit_ev_ != nullptr) cudaEventDestroy(admit_ev_);
+  if (refresh_ev_ != nullptr) cudaEventDestroy(refresh_ev_);
   if (own_stream_ != nullptr) cudaStreamDestroy(own_stream_);
 }
 
@@ -789,26 +798,32 @@ int Engine::flush_scenes() {
   return RFMM_OK;
 }
 
-int Engine::upload_map(MapBlock &m, const std::vector<uint32_t> &scenes, uint32_t *count) {
+int Engine::upload_map(MapBlock &m, const std::vector<uint32_t> &scenes, uint32_t *count,
+                       cudaStream_t stream, bool counts) {
   if (m.pin[0] == nullptr) {
     for (int b = 0; b < 2; b++) {
-      RF_CK(cudaHostAlloc((void **)&m.pin[b], 4ull * tiles_, cudaHostAllocDefault));
+      RF_CK(cudaHostAlloc((void **)&m.pin[b], 8ull * tiles_, cudaHostAllocDefault));
       RF_CK(cudaEventCreateWithFlags(&m.ev[b], cudaEventDisableTiming));
     }
-    const int st = alloc((void **)&m.dev, 4ull * tiles_);
+    const int st = alloc((void **)&m.dev, 8ull * tiles_);
     if (st != RFMM_OK) return st;
   }
   const uint32_t b = m.next;
   m.next ^= 1u;
   RF_CK(cudaEventSynchronize(m.ev[b]));  // the block's last copy is done
   uint32_t total = 0;
+  for (uint32_t sc : scenes) total += pad_tiles(scenes_[sc].n);
+  uint32_t at = 0;
   for (uint32_t sc : scenes) {
     const SceneDesc &d = scenes_[sc];
-    for (uint32_t t = 0; t < pad_tiles(d.n); t++) m.pin[b][total++] = d.tile_off + t;
+    for (uint32_t t = 0; t < pad_tiles(d.n); t++, at++) {
+      m.pin[b][at] = d.tile_off + t;
+      if (counts) m.pin[b][total + at] = d.n;
+    }
   }
   // The previous use of m.dev is earlier on the same stream.
-  RF_CK(cudaMemcpyAsync(m.dev, m.pin[b], 4ull * total, cudaMemcpyHostToDevice, stream_));
-  RF_CK(cudaEventRecord(m.ev[b], stream_));
+  RF_CK(cudaMemcpyAsync(m.dev, m.pin[b], 4ull * total * (counts ? 2u : 1u), cudaMemcpyHostToDevice, stream));
+  RF_CK(cudaEventRecord(m.ev[b], stream));
   *count = total;
   return RFMM_OK;
 }
@@ -831,32 +846,46 @@ int Engine::activate_many(const std::vector<Admission> &admissions) {
     if (a.n > d.tile_cap * kTile || depth < 4u || depth > d.max_depth) return RFMM_ERR_BUDGET;
   }
   std::vector<uint32_t> slots;
+  std::vector<SceneDesc> descs;
   SceneMask which{};
   for (const Admission &a : adm) {
     const int sd = slot_desc(a.scene, a.n, a.params);
     if (sd != RFMM_OK) return sd;
     slots.push_back(a.scene);
+    descs.push_back(scenes_[a.scene]);
     which.bits[a.scene >> 5] |= 1u << (a.scene & 31u);
   }
-  int st = flush_scenes();
-  if (st != RFMM_OK) return st;
+  // On the admission stream (engines with lists; else the engine stream):
+  // these writes touch only the admitted slots -- their descriptors (the
+  // rest of the table, such as slots retiring at the end of the chunk in
+  // flight, reaches the device with the next refresh_lists), bodies, ids
+  // and cells -- so they may overlap the chunk in flight.  The host buffer
+  // parities already describe the state after the chunks enqueued so far.
+  cudaStream_t as = admit_stream_ != nullptr ? admit_stream_ : stream_;
+  if (as != stream_) RF_CK(cudaStreamWaitEvent(as, refresh_ev_, 0));
+  launch_write_scenes(as, d_scenes_, slots.data(), descs.data(), (uint32_t)slots.size());
   const uint32_t cur = pcur_.load(), scr = cur ^ 1u;
   for (const Admission &a : adm)
     if (a.buffer != scr)  // staged before a resort flipped the buffers
       RF_CK(cudaMemcpyAsync(slot_bodies(a.scene, scr), slot_bodies(a.scene, a.buffer), 32ull * a.n,
-                            cudaMemcpyDeviceToDevice, stream_));
+                            cudaMemcpyDeviceToDevice, as));
   uint32_t total = 0;
-  st = upload_map(admit_map_, slots, &total);
+  int st = upload_map(admit_map_, slots, &total, as);
   if (st != RFMM_OK) return st;
   // Keys of the staged bodies (numbering them in caller order), one sort,
   // cleared trees, one gather with the leaf deposit into the current buffer.
   LaunchCtx L = ctx(mcur_, lpar_, scr);
+  L.stream = as;
   launch_keys(L, sort_.keys[0], sort_.vals[0], d_ids_[scr], 1, total, 0u, nullptr, admit_map_.dev);
-  const int r = radix_sort(stream_, sort_, total * kTile, key_bits_);
+  const int r = radix_sort(as, sort_, total * kTile, key_bits_);
   launch_clear_scenes(L, (uint32_t)scenes_.size(), which, d_mom_[mcur_], d_mom_[mcur_ ^ 1u], d_src_, d_aux_);
   launch_gather(L, sort_.vals[r], d_part_[scr], d_ids_[scr], d_part_[cur], d_ids_[cur], d_mom_[mcur_],
                 total, 0u, nullptr, admit_map_.dev);
   RF_CK(cudaGetLastError());
+  if (as != stream_) {  // the engine stream's next kernels see the admitted slots
+    RF_CK(cudaEventRecord(admit_ev_, as));
+    RF_CK(cudaStreamWaitEvent(stream_, admit_ev_, 0));
+  }
   for (uint32_t sc : slots) uploaded_[sc] = true;
   launches_ += 3u + 3u * ((key_bits_ + 7u) / 8u);
   committed_ = true;
@@ -868,11 +897,13 @@ int Engine::retire_many(const std::vector<uint32_t> &slots) {
   for (uint32_t sc : slots)
     if (sc >= scenes_.size() || scenes_[sc].n == 0u) return RFMM_ERR_INVALID;
   uint32_t total = 0;
-  int st = upload_map(retire_map_, slots, &total);
+  int st = upload_map(retire_map_, slots, &total, stream_, true);
   if (st != RFMM_OK) return st;
   const uint32_t cur = pcur_.load();
   LaunchCtx L = ctx(mcur_, lpar_, cur);
-  launch_unpermute(L, d_ids_[cur], d_part_[cur ^ 1u], 0u, total, retire_map_.dev);
+  // Body counts from the map: an admission overlapping this launch does not
+  // write these slots' descriptors, but the table refresh after it will.
+  launch_unpermute(L, d_ids_[cur], d_part_[cur ^ 1u], 0u, total, retire_map_.dev, retire_map_.dev + total);
   RF_CK(cudaGetLastError());
   launches_ += 1;
   for (uint32_t sc : slots) scenes_[sc].n = 0u;
@@ -881,8 +912,10 @@ int Engine::retire_many(const std::vector<uint32_t> &slots) {
 }
 
 int Engine::refresh_lists() {
-  const int st = flush_scenes();
-  return st != RFMM_OK ? st : rebuild_lists();
+  int st = flush_scenes();
+  if (st == RFMM_OK) st = rebuild_lists();
+  if (st == RFMM_OK && refresh_ev_ != nullptr) RF_CK(cudaEventRecord(refresh_ev_, stream_));
+  return st;
 }
 
 int Engine::commit() {

@@ -192,9 +192,21 @@ class Engine {
     uint32_t next = 0;
   };
   MapBlock admit_map_, retire_map_;
-  // Copies `tiles` of `scenes` (each slot's padded tiles, in order) into the
-  // map's next pinned block and to the device; returns the tile count.
-  int upload_map(MapBlock &m, const std::vector<uint32_t> &scenes, uint32_t *count);
+  // Copies the tiles of `scenes` (each slot's padded tiles, in order) into
+  // the map's next pinned block and to the device on `stream`; with
+  // `counts`, each tile's scene body count follows the tiles (at dev +
+  // count).  Returns the tile count.
+  int upload_map(MapBlock &m, const std::vector<uint32_t> &scenes, uint32_t *count, cudaStream_t stream,
+                 bool counts = false);
+  // Serving admissions run on their own stream, overlapping the chunk in
+  // flight (they touch only the admitted slots' bodies and cells); the engine
+  // stream waits for them before its next kernels.
+  cudaStream_t admit_stream_ = nullptr;
+  cudaEvent_t admit_ev_ = nullptr;
+  // Recorded on the engine stream after each refresh_lists: an admission
+  // waits for it, so the whole-table copy of a refresh never lands on top of
+  // the admitted slots' descriptors.
+  cudaEvent_t refresh_ev_ = nullptr;
   int rebuild_lists();
   int check_device_error();
 

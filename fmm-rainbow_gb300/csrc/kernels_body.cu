@@ -837,13 +837,17 @@ __global__ void __launch_bounds__(256) k_unpermute(const SceneDesc *__restrict__
                                                    const float4 *__restrict__ part,
                                                    const uint32_t *__restrict__ ids,
                                                    float4 *__restrict__ out, uint32_t tile_base,
-                                                   const uint32_t *__restrict__ tile_map) {
+                                                   const uint32_t *__restrict__ tile_map,
+                                                   const uint32_t *__restrict__ tile_count) {
   const uint32_t tile = tile_map != nullptr ? tile_map[blockIdx.x] : tile_base + blockIdx.x;
   const SceneDesc &S = scenes[tile_scene[tile]];
+  // The scene's body count: from the caller when given (a retiring serving
+  // slot's descriptor may already read empty), else from the descriptor.
+  const uint32_t n = tile_count != nullptr ? tile_count[blockIdx.x] : S.n;
   const uint32_t slot = tile * kTile + threadIdx.x;
-  if (slot - S.body_off >= S.n) return;
+  if (slot - S.body_off >= n) return;
   const uint32_t id = ids[slot];
-  if (id >= S.n) return;  // defensive: ids are a permutation of 0..n-1
+  if (id >= n) return;  // defensive: ids are a permutation of 0..n-1
   const uint32_t dst = S.body_off + id;
   out[2u * dst] = part[2u * slot];
   out[2u * dst + 1u] = part[2u * slot + 1u];
@@ -1057,9 +1061,40 @@ void launch_leaf_starts(const LaunchCtx &L, const uint32_t *sorted_keys, uint32_
 }
 
 void launch_unpermute(const LaunchCtx &L, const uint32_t *ids, float4 *out, uint32_t tile_base,
-                      uint32_t tiles, const uint32_t *tile_map) {
+                      uint32_t tiles, const uint32_t *tile_map, const uint32_t *tile_count) {
   k_unpermute<<<tiles, kTile, 0, L.stream>>>(L.scenes, L.tile_scene, L.part, ids, out, tile_base,
-                                             tile_map);
+                                             tile_map, tile_count);
+}
+
+// Scene descriptors written from kernel parameters (a few at a time, on the
+// caller's stream, without touching the other entries of the table).
+struct SceneWrites {
+  static constexpr uint32_t kMax = 16u;
+  uint32_t count;
+  uint32_t index[kMax];
+  SceneDesc desc[kMax];
+};
+
+__global__ void __launch_bounds__(32) k_write_scenes(SceneDesc *__restrict__ scenes,
+                                                     const __grid_constant__ SceneWrites w) {
+  for (uint32_t i = 0; i < w.count; i++) {
+    const uint32_t *src = reinterpret_cast<const uint32_t *>(&w.desc[i]);
+    uint32_t *dst = reinterpret_cast<uint32_t *>(scenes + w.index[i]);
+    for (uint32_t k = threadIdx.x; k < sizeof(SceneDesc) / 4u; k += blockDim.x) dst[k] = src[k];
+  }
+}
+
+void launch_write_scenes(cudaStream_t stream, SceneDesc *scenes, const uint32_t *index,
+                         const SceneDesc *desc, uint32_t count) {
+  for (uint32_t at = 0; at < count; at += SceneWrites::kMax) {
+    SceneWrites w{};
+    w.count = count - at < SceneWrites::kMax ? count - at : SceneWrites::kMax;
+    for (uint32_t i = 0; i < w.count; i++) {
+      w.index[i] = index[at + i];
+      w.desc[i] = desc[at + i];
+    }
+    k_write_scenes<<<1, 32, 0, stream>>>(scenes, w);
+  }
 }
 
 // Zero the moments (both buffers), sources and records of every cell of the

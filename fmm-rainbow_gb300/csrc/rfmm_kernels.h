@@ -135,7 +135,11 @@ void launch_leaf_starts(const LaunchCtx &L, const uint32_t *sorted_keys, uint32_
 // Bodies of tiles [tile_base, tile_base + tiles) (or tile_map[0 ..]) back to
 // caller order: out[body_off + id] = part[slot].
 void launch_unpermute(const LaunchCtx &L, const uint32_t *ids, float4 *out, uint32_t tile_base,
-                      uint32_t tiles, const uint32_t *tile_map = nullptr);
+                      uint32_t tiles, const uint32_t *tile_map = nullptr,
+                      const uint32_t *tile_count = nullptr);
+// Scene descriptors desc[i] into scenes[index[i]] on `stream` (other entries untouched).
+void launch_write_scenes(cudaStream_t stream, SceneDesc *scenes, const uint32_t *index,
+                         const SceneDesc *desc, uint32_t count);
 // Cleared moments (both buffers), sources and records of the scenes in `which`.
 void launch_clear_scenes(const LaunchCtx &L, uint32_t nscenes, const SceneMask &which, uint4 *mom0,
                          uint4 *mom1, float4 *src, float4 *aux);
