@@ -372,7 +372,10 @@ def run_gpu_plain(args, w, torch, rfmm, stream, flush, rank, world, local):
         solver.step(fmm_steps)
 
     tuning = solver.tuning()
-    if not args.no_autotune:  # project autotuner: launch shapes timed on this scene
+    # Project autotuner: launch shapes timed on this scene.  Not in the P2P
+    # mode, whose step is the pair kernel (its trials of 64 steps would take
+    # minutes and the tree-pass shapes do not matter there).
+    if not args.no_autotune and args.near == "reference":
         solver.upload_device(pristine.data_ptr(), pristine.numel())
         tuning = solver.autotune(20)
     for _ in range(args.warmup):

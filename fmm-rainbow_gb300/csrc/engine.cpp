@@ -247,7 +247,11 @@ int Engine::create(const std::vector<SceneSpec> &specs, Engine **out) {
   if (e == cudaSuccess) E->body_limit_ = std::min(body_ctas_per_sm(), fast::body_ctas_per_sm());
   {
     rfmm_tuning t{};
-    t.upward_ctas_per_sm = 6;
+    // Many scenes: the warp-per-subtree upward gains from more CTAs than stay
+    // resident (queued CTAs pick up the tasks as others finish; measured 16
+    // against 6: -14% at 256 scenes); one scene's grid is bounded by its
+    // 512 subtrees either way.
+    t.upward_ctas_per_sm = specs.size() > 1 ? 16 : 6;
     t.m2l_ctas_per_sm = 6;
     t.l2l_ctas_per_sm = 5;
     t.integrate_ctas_per_sm = E->body_limit_;
@@ -500,7 +504,7 @@ int Engine::autotune(uint32_t steps_per_trial, rfmm_tuning *best) {
     for (int knob = 0; knob < 12 && st == RFMM_OK; knob++) {
       std::vector<uint32_t> values;
       switch (knob) {
-        case 0: values = {2, 4, 6, 8}; break;
+        case 0: values = {2, 4, 6, 8, 16}; break;
         case 1: values = {2, 4, 6}; break;
         case 2: values = {2, 4, 5, 8}; break;
         case 3: for (uint32_t v = 1; v <= body_limit_; v++) values.push_back(v); break;
@@ -726,30 +730,6 @@ int Engine::rebuild_lists() {
                           cudaMemcpyHostToDevice, stream_));
   RF_CK(cudaMemcpyAsync(&d_ctr_->tiles_active, counts, sizeof(counts), cudaMemcpyHostToDevice,
                         stream_));
-  return RFMM_OK;
-}
-
-int Engine::commit_scene(uint32_t scene) {
-  const SceneDesc &d = scenes_[scene];
-  const uint32_t tiles = pad_tiles(d.n);
-  LaunchCtx L = ctx(mcur_, lpar_, pcur_);
-  launch_keys(L, sort_.keys[0], sort_.vals[0], nullptr, 0, tiles, d.tile_off);
-  const int r = radix_sort(stream_, sort_, tiles * kTile, 3u * d.key_level);
-  // A rebuilt scene starts from cleared moment, source and record buffers (the
-  // upward pass skips subtrees that are empty in both moment buffers).
-  RF_CK(cudaMemsetAsync(d_mom_[mcur_] + d.cell_off, 0, 16ull * d.cells, stream_));
-  RF_CK(cudaMemsetAsync(d_mom_[mcur_ ^ 1u] + d.cell_off, 0, 16ull * d.cells, stream_));
-  RF_CK(cudaMemsetAsync(d_src_ + d.cell_off, 0, 16ull * d.cells, stream_));
-  RF_CK(cudaMemsetAsync(d_aux_ + d.cell_off, 0, 16ull * d.cells, stream_));
-  launch_gather(L, sort_.vals[r], d_part_[pcur_], d_ids_[pcur_], d_part_[pcur_ ^ 1u],
-                d_ids_[pcur_ ^ 1u], d_mom_[mcur_], tiles, d.tile_off);
-  RF_CK(cudaGetLastError());
-  // The sorted scene lands in the other buffer; copy it back into the current one.
-  RF_CK(cudaMemcpyAsync(d_part_[pcur_] + 2ull * d.body_off, d_part_[pcur_ ^ 1u] + 2ull * d.body_off,
-                        32ull * tiles * kTile, cudaMemcpyDeviceToDevice, stream_));
-  RF_CK(cudaMemcpyAsync(d_ids_[pcur_] + d.body_off, d_ids_[pcur_ ^ 1u] + d.body_off,
-                        4ull * tiles * kTile, cudaMemcpyDeviceToDevice, stream_));
-  launches_ += 2u + 3u * ((3u * d.key_level + 7u) / 8u);
   return RFMM_OK;
 }
 

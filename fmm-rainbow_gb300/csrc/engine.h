@@ -174,7 +174,6 @@ class Engine {
   float4 *d_near4_ = nullptr;     // kNearP2P: per-slot pair sums of the step
   uint32_t *d_starts_ = nullptr;  // per-leaf start slots (leaf sorts)
   int launch_chunk(uint32_t len, bool sort_at_end);
-  int commit_scene(uint32_t scene);
   int slot_desc(uint32_t scene, uint32_t n, const rfmm_params &p);  // fill a free slot's descriptor (host)
   // Serving: the host scene table goes to the device whole (from two pinned
   // blocks used in turn) when slot changes made it stale.

@@ -1129,11 +1129,6 @@ void launch_initialize(const LaunchCtx &L, float4 *part_out, uint32_t tile_base,
   k_initialize<<<tiles, kTile, 0, L.stream>>>(L.scenes, L.tile_scene, part_out, tile_base);
 }
 
-__global__ void k_iota(uint32_t *__restrict__ ids, uint32_t count) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < count) ids[i] = i;
-}
-
 // Bulk upload, one CTA per 256-slot tile: two 16-byte loads and stores per body.
 __global__ void __launch_bounds__(256) k_upload_scenes(const SceneDesc *__restrict__ scenes,
                                                        const uint32_t *__restrict__ tile_scene,
@@ -1155,10 +1150,6 @@ void launch_upload_scenes(const LaunchCtx &L, float4 *part, uint32_t tile_base, 
                           uint32_t scene_base, const UploadSources &src) {
   k_upload_scenes<<<tiles, kTile, 0, L.stream>>>(L.scenes, L.tile_scene, part, tile_base, scene_base,
                                                  src);
-}
-
-void launch_iota(cudaStream_t stream, uint32_t *ids, uint32_t count) {
-  k_iota<<<(count + 255u) / 256u, 256, 0, stream>>>(ids, count);
 }
 
 RFMM_KERNEL_NS_END

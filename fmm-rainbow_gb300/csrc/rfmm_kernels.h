@@ -151,7 +151,6 @@ void launch_upload_scenes(const LaunchCtx &L, float4 *part, uint32_t tile_base, 
 // Self-check of the bounded kernel wait: *status (device) receives
 // kDevErrTmaTimeout when a wait that cannot complete gives up after `polls`.
 void launch_wait_check(cudaStream_t stream, uint32_t polls, uint32_t *status);
-void launch_iota(cudaStream_t stream, uint32_t *ids, uint32_t count);
 uint32_t body_ctas_per_sm();  // resident 256-thread CTAs per SM of the persistent body passes
 // FMM acceleration + potential per body of tiles [tile_base, +tiles), caller order.
 void launch_accel(const LaunchCtx &L, const uint32_t *ids, float4 *out, uint32_t tile_base,
