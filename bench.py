@@ -72,6 +72,8 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="plain workload only")
+    ap.add_argument("--no-served", action="store_true",
+                    help="default line: skip the short served measurement")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--no-extras", action="store_true",
                     help="timed steps only (no timeline, fast-variant, accuracy or render pass): "
@@ -656,6 +658,9 @@ def run_gpu(args, w):
                                                  "plain_back_to_back", "batched_over_plain",
                                                  "clocks", "e2e", "gpu_launches", "roofline",
                                                  "timeline", "tuning")}
+        if (args.workload == "plummer_1m" and not args.no_served and args.near == "reference"
+                and world == 1):
+            line["served"] = served_summary(args, torch, rfmm, local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds, args.near)
     if rank == 0:
@@ -667,7 +672,29 @@ def run_gpu(args, w):
 
 # ------------------------------------------------------------------ serving
 
-def run_gpu_served(args, w):
+def served_summary(args, torch, rfmm, local):
+    """A short served measurement for the default line: 4,000 requests of the
+    served workload's distribution, one rate below saturation (latency) and
+    one above it (throughput), and the same list back to back through plain
+    handles.  A short run's throughput includes the fill and drain of the
+    slots, so it reads below the full sweep's (--workload served)."""
+    w = workloads.WORKLOADS["served"]
+    count, rates = 4000, [1000.0, 3000.0]
+    sweep, plain_value, clocks, pool = served_sweep(args, w, torch, rfmm, local, count, rates, True)
+    top = max(sweep, key=lambda r: r["body_steps_per_s"])
+    return {"value": top["body_steps_per_s"], "unit": "body-steps/s",
+            "requests_per_rate": count, "body_steps_per_rate": pool.body_steps(),
+            "rates": [{k: r[k] for k in ("offered_rate_per_s", "achieved_rate_per_s", "p50_ms",
+                                          "p99_ms", "body_steps_per_s")} for r in sweep],
+            "plain_back_to_back": plain_value,
+            "served_over_plain": top["body_steps_per_s"] / plain_value if plain_value else None,
+            "clocks": clocks,
+            "data": "synthetic (seeded, numpy PCG64): " + w["desc"],
+            "note": "short form of --workload served (10,000 requests per rate, 50-2,000 req/s); "
+                    "the fill and drain of the slots weigh more in a short run"}
+
+
+def served_sweep(args, w, torch, rfmm, local, count, rates, with_plain, timeline=False):
     """Continuous-batching server under Poisson arrivals (open loop), against
     the same request list solved back to back through plain handles.
 
@@ -676,17 +703,14 @@ def run_gpu_served(args, w):
     the scheduled arrival whether or not a submission starts late; a
     collector thread takes the results as they finish.  The achieved
     submission rate and the producers' lag behind the schedule are reported
-    beside the offered rate.
+    beside the offered rate.  Returns (sweep, plain body-steps/s or None,
+    clocks, pool).
     """
     import threading
     import numpy as np
 
-    rank, world, local = dist_env()
-    torch, rfmm, stream, flush = gpu_setup(world, local)
-    count = args.requests or w["requests"]
     pool = workloads.served_pool(w, count)
     params = rfmm.default_params(gravity=w["G"], softening=w["eps"], dt=w["dt"])
-    rates = args.rates or w["rates"]
     producers, collectors = 8, 4
     staging = 24 << 30  # pinned host staging of the server (inputs 18 GiB, results 6 GiB)
     body_steps = pool.body_steps()
@@ -706,7 +730,7 @@ def run_gpu_served(args, w):
     for ri, rate in enumerate(rates):
         srv = rfmm.Server(max_bodies=w["n_max"], memory_budget_bytes=w["budget"],
                           max_chunk_steps=4, staging_bytes=staging, float_mode=fmode,
-                          timeline=args.served_timeline)
+                          timeline=timeline)
         arrivals = np.cumsum(np.random.default_rng(w["seed"] + ri).exponential(1.0 / rate, count))
         ids = [None] * count
         actual = np.zeros(count)
@@ -750,7 +774,7 @@ def run_gpu_served(args, w):
             raise errors[0]
         wall = time.perf_counter() - t0
         st = srv.stats()
-        tl = srv.timeline() if args.served_timeline else None
+        tl = srv.timeline() if timeline else None
         srv.close()
         lag = (actual - (t0 + arrivals)) * 1e3
         sweep.append({"offered_rate_per_s": rate,
@@ -779,7 +803,7 @@ def run_gpu_served(args, w):
     # gets its own handle (created and destroyed outside the timer), then its
     # upload, steps and download are timed on the host clock.
     plain_s = 0.0
-    for i in range(count if not args.no_plain else 0):
+    for i in range(count if with_plain else 0):
         s = rfmm.Solver(int(pool.n[i]), params)
         s.set_float_mode(fmode)
         torch.cuda.synchronize()
@@ -790,6 +814,21 @@ def run_gpu_served(args, w):
         plain_s += time.perf_counter() - t
         s.close()
     plain_value = body_steps / plain_s if plain_s > 0 else None
+    return sweep, plain_value, clocks, pool
+
+
+def run_gpu_served(args, w):
+    import numpy as np
+
+    rank, world, local = dist_env()
+    torch, rfmm, stream, flush = gpu_setup(world, local)
+    count = args.requests or w["requests"]
+    rates = args.rates or w["rates"]
+    sweep, plain_value, clocks, pool = served_sweep(args, w, torch, rfmm, local, count, rates,
+                                                    not args.no_plain, args.served_timeline)
+    body_steps = pool.body_steps()
+    producers, collectors = 8, 4
+    staging = 24 << 30
     top = max(sweep, key=lambda r: r["body_steps_per_s"])
     line = {
         "metric": "body-steps/s", "value": top["body_steps_per_s"], "unit": "body-steps/s",
