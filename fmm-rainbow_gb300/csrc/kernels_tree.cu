@@ -695,17 +695,27 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, i
       : "memory");
 }
 
-// M2L with one lane per target (long parent lists): warp w of the pass takes
-// listed parents 4w .. 4w+3, lane 8q + c handles child c of parent q, and
-// the lane adds the terms of its contributing stencil slots to its own ten
-// sums in the reference's loop order (no partial sum crosses lanes).  Source
-// cells are read through L1: the 8 lanes of a parent read the same cell, so
-// a warp requests at most 4 addresses per slot.  `slots` holds, per slot in
-// loop order, the cell's offset in the 6x6x6 block (3 bits per axis) and the
-// children it is adjacent to (bits 9..16).
-__device__ __forceinline__ uint32_t m2l_slot_entry(uint32_t k) {
-  const uint32_t info = m2l_slot_info(k), t = info & 0xFFu;
-  return (t % 6u) | (((t / 6u) % 6u) << 3) | ((t / 36u) << 6) | ((info >> 8) << 9);
+// M2L with one lane per target (long parent lists): a CTA's 8 warps take 32
+// listed parents at a time, warp c handling child c of each (lane j: parent
+// 32g + j).  The lanes of a warp walk the same 189 contributing stencil slots
+// of child c (the 216 tile cells less the 27 adjacent to it), in the
+// reference's loop order, each adding its terms to its own ten sums (no
+// partial sum crosses lanes).  Source cells are read through L1.  `clist`
+// holds per child the contributing slots' cell offsets in the 6x6x6 block
+// (3 bits per axis), built once per CTA.
+constexpr uint32_t kContrib = 189u;
+
+__device__ __forceinline__ void build_child_slots(uint16_t (*clist)[kContrib]) {
+  if (threadIdx.x < 8u) {
+    const uint32_t c = threadIdx.x;
+    uint32_t n = 0u;
+    for (uint32_t k = 0; k < kTileCells; k++) {
+      const uint32_t info = m2l_slot_info(k);
+      if ((info >> (8u + c)) & 1u) continue;  // adjacent to (or is) child c
+      const uint32_t t = info & 0xFFu;
+      if (n < kContrib) clist[c][n++] = (uint16_t)((t % 6u) | (((t / 6u) % 6u) << 3) | ((t / 36u) << 6));
+    }
+  }
 }
 
 __device__ __forceinline__ void m2l_lanes_pass(const SceneDesc *__restrict__ scenes,
@@ -713,11 +723,12 @@ __device__ __forceinline__ void m2l_lanes_pass(const SceneDesc *__restrict__ sce
                                                const uint4 *__restrict__ mom,
                                                const float4 *__restrict__ src,
                                                float *__restrict__ lfield,
-                                               const uint32_t *__restrict__ slots) {
-  const uint32_t lane = threadIdx.x & 31u, q = lane >> 3, c = lane & 7u;
-  const uint32_t groups = (count + 3u) / 4u, stride = gridDim.x * (blockDim.x >> 5);
-  for (uint32_t g = blockIdx.x + gridDim.x * (threadIdx.x >> 5); g < groups; g += stride) {
-    const uint32_t item = 4u * g + q;
+                                               const uint16_t (*clist)[kContrib]) {
+  const uint32_t lane = threadIdx.x & 31u, c = threadIdx.x >> 5;  // 256 threads: c = 0..7
+  const uint16_t *cl = clist[c];
+  const uint32_t groups = (count + 31u) / 32u;
+  for (uint32_t g = blockIdx.x; g < groups; g += gridDim.x) {
+    const uint32_t item = 32u * g + lane;
     const bool valid = item < count;
     const WorkItem w = valid ? plist[item] : WorkItem{0u, 0u};
     const SceneDesc &S = scenes[w.scene];
@@ -738,18 +749,18 @@ __device__ __forceinline__ void m2l_lanes_pass(const SceneDesc *__restrict__ sce
     if (__any_sync(0xFFFFFFFFu, live)) {
       // Slot k + 1's source is requested while slot k is evaluated.
       auto fetch = [&](uint32_t k, float4 &sv) {
-        const uint32_t e = slots[k];
-        const int x = bx + (int)(e & 7u), y = by + (int)((e >> 3) & 7u), z = bz + (int)((e >> 6) & 7u);
+        const uint32_t e = cl[k];
+        const int x = bx + (int)(e & 7u), y = by + (int)((e >> 3) & 7u), z = bz + (int)(e >> 6);
         sv = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        if (live && !((e >> (9u + c)) & 1u) && (uint32_t)x < dim && (uint32_t)y < dim && (uint32_t)z < dim)
+        if (live && (uint32_t)x < dim && (uint32_t)y < dim && (uint32_t)z < dim)
           sv = __ldg(&src[lvl_base + lin3((uint32_t)x, (uint32_t)y, (uint32_t)z, dim)]);
       };
       float4 next;
       fetch(0u, next);
-      for (uint32_t k = 0; k < kTileCells; k++) {
+      for (uint32_t k = 0; k < kContrib; k++) {
         const float4 sv = next;
-        if (k + 1u < kTileCells) fetch(k + 1u, next);
-        if (sv.w != 0.0f) {  // excluded, absent and empty slots all read w = 0
+        if (k + 1u < kContrib) fetch(k + 1u, next);
+        if (sv.w != 0.0f) {  // absent and empty slots read w = 0
           float out[10];
           pair_field_d(sv, ctx, cty, ctz, eps, out);
 #pragma unroll
@@ -777,7 +788,7 @@ __global__ void __launch_bounds__(256, 6) k_m2l(const SceneDesc *__restrict__ sc
                                              uint32_t lane_min,
                                              unsigned long long *__restrict__ stamp) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  __shared__ uint32_t s_slots[kTileCells];  // the lane path's slot table
+  __shared__ uint16_t s_clist[kWide ? 8 : 1][kContrib];  // the lane path's per-child slot lists
   // The TMA destination must be 128-byte aligned: align the carve-out by hand
   // (the launch reserves 128 spare bytes).
   const uint32_t pad = (128u - (smem_u32(smem_raw) & 127u)) & 127u;
@@ -789,17 +800,15 @@ __global__ void __launch_bounds__(256, 6) k_m2l(const SceneDesc *__restrict__ sc
     sh.stop = 0u;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  for (uint32_t k = tid; k < kTileCells; k += blockDim.x) {
-    sh.slot_info[k] = m2l_slot_info(k);
-    if (kWide) s_slots[k] = m2l_slot_entry(k);
-  }
+  for (uint32_t k = tid; k < kTileCells; k += blockDim.x) sh.slot_info[k] = m2l_slot_info(k);
+  if (kWide) build_child_slots(s_clist);
   grid_dependency_wait();  // the upward pass built the tree and the parent list
   stamp_begin(stamp);
   const uint32_t count = min(ctr->parents[list_par], plist_cap);
   if (blockIdx.x == 0 && tid == 0) ctr->parents[list_par ^ 1u] = 0u;  // reset for the next step
   __syncthreads();
   if (kWide && count >= lane_min) {  // grid-uniform
-    m2l_lanes_pass(scenes, plist, count, mom, src, lfield, s_slots);
+    m2l_lanes_pass(scenes, plist, count, mom, src, lfield, s_clist);
     stamp_end(stamp);
     grid_dependents_may_launch();
     return;
