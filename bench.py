@@ -71,6 +71,8 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=8)
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-baseline-only", action="store_true",
+                    help="print the CPU baseline object of the workload and exit (no GPU use)")
     ap.add_argument("--no-batched", action="store_true", help="plain workload only")
     ap.add_argument("--no-served", action="store_true",
                     help="default line: skip the short served measurement")
@@ -195,6 +197,18 @@ class CpuRuns:
         for st in states:
             st.step(steps)
         return time.perf_counter() - t0
+
+
+def cpu_baseline_child(args):
+    """cpu_baseline in a fresh interpreter that never touches the GPU, so the
+    oracle's host threads do not share the process with CUDA and torch."""
+    cmd = [sys.executable, os.path.abspath(__file__), "--cpu-baseline-only", "--workload", args.workload,
+           "--cpu-seconds", str(args.cpu_seconds), "--near", args.near]
+    try:
+        out = subprocess.run(cmd, capture_output=True, text=True, check=True, timeout=600).stdout
+        return json.loads(out.strip().splitlines()[-1])
+    except (subprocess.SubprocessError, ValueError, IndexError) as e:
+        return {"value": None, "unavailable": "CPU baseline process failed: %s" % type(e).__name__}
 
 
 def cpu_baseline(w, seconds, near="reference", warmup=1):
@@ -662,7 +676,7 @@ def run_gpu(args, w):
                 and world == 1):
             line["served"] = served_summary(args, torch, rfmm, local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds, args.near)
+        line["cpu_baseline"] = cpu_baseline_child(args)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -863,6 +877,9 @@ def run_gpu_served(args, w):
 def main():
     args = parse_args()
     w = workloads.WORKLOADS[args.workload]
+    if args.cpu_baseline_only:
+        print(json.dumps(cpu_baseline(w, args.cpu_seconds, args.near)), flush=True)
+        return 0
     if args.impl == "reference":
         return run_reference(args, w)
     if w["kind"] == "served":
