@@ -523,18 +523,29 @@ __global__ void __launch_bounds__(256, 4) k_near_p2p(const SceneDesc *__restrict
                                                   const uint32_t *__restrict__ choice,
                                                   uint32_t tiles,
                                                   const uint32_t *__restrict__ tile_list,
-                                                  const Counters *__restrict__ ctr,
+                                                  Counters *__restrict__ ctr,
                                                   float4 *__restrict__ near_out,
                                                   unsigned long long *__restrict__ stamp) {
   __shared__ float4 buf[kTile];
   __shared__ SceneDesc S;
   __shared__ uint32_t s_cell[5];  // tid 0's sample cell: key, level, x, y, z
+  __shared__ uint32_t s_next;
   const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   grid_dependency_wait();  // the upward pass resolved this step's sample cells
   stamp_begin(stamp);
   const uint32_t ntiles = tile_list != nullptr ? min(ctr->tiles_active, tiles) : tiles;
+  // Tiles are taken one at a time from a counter (reset by this step's
+  // upward pass): a tile's cost is its bodies times the sources around their
+  // sample cell, which spans two orders of magnitude between sparse and
+  // core leaves, so a static share leaves most SMs idle behind the heaviest.
+  auto grab = [&]() -> uint32_t {
+    __syncthreads();
+    if (tid == 0) s_next = atomicAdd(&ctr->p2p_cursor, 1u);
+    __syncthreads();
+    return s_next;
+  };
   uint32_t cur = 0xFFFFFFFFu;
-  for (uint32_t i = blockIdx.x; i < ntiles; i += gridDim.x) {
+  for (uint32_t i = grab(); i < ntiles; i = grab()) {
     const uint32_t tile = tile_list != nullptr ? tile_list[i] : i;
     const uint32_t sc = tile_scene[tile];
     if (sc != cur) {
@@ -1005,8 +1016,8 @@ static uint32_t near_p2p_grid(const LaunchCtx &L, uint32_t tiles) {
 void launch_near_p2p(const LaunchCtx &L, uint32_t tiles) {
   launch_step_kernel(L, k_near_p2p, dim3(near_p2p_grid(L, tiles)), dim3(kTile), 0, L.scenes,
                      L.tile_scene, (const float4 *)L.pos4, (const uint32_t *)L.starts_out,
-                     (const uint4 *)L.mom, (const uint32_t *)L.choice, tiles, L.tile_list,
-                     (const Counters *)L.ctr, L.near4, stamp_rec(L, 5u));
+                     (const uint4 *)L.mom, (const uint32_t *)L.choice, tiles, L.tile_list, L.ctr,
+                     L.near4, stamp_rec(L, 5u));
 }
 
 void launch_deposit(const LaunchCtx &L, uint4 *moments, uint32_t tiles) {

@@ -276,7 +276,10 @@ __device__ __forceinline__ void clear_previous_fields(const SceneDesc *__restric
   const uint32_t tid = threadIdx.x;
   grid_dependency_wait();  // the previous integrate read the fields
   stamp_begin(stamp);
-  if (blockIdx.x == 0 && tid == 0) ctr->tile_cursor = 0u;  // for this step's integrate
+  if (blockIdx.x == 0 && tid == 0) {  // for this step's integrate and pair sums
+    ctr->tile_cursor = 0u;
+    ctr->p2p_cursor = 0u;
+  }
   const uint32_t prev_n = min(ctr->parents[list_par ^ 1u], plist_cap);
   const uint32_t wpb = blockDim.x >> 5, lane = tid & 31u;
   const uint32_t ch = lane / 3u, part = lane % 3u;  // lanes 0..23: child, float4 of its field

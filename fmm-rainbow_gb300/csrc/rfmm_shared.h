@@ -59,6 +59,7 @@ struct Counters {
   uint32_t tasks_active; // entries of the active upward-task list (when one is used)
   uint32_t scenes_active; // entries of the active scene list (when one is used)
   uint32_t tile_cursor;  // next body tile for dynamically scheduled integrate CTAs
+  uint32_t p2p_cursor;   // next body tile for the near-field pair-sum CTAs
   uint32_t wait_check;   // status word of the bounded-wait self-check
 };
 
