@@ -699,7 +699,8 @@ def served_summary(args, torch, rfmm, local):
     return {"value": top["body_steps_per_s"], "unit": "body-steps/s",
             "requests_per_rate": count, "body_steps_per_rate": pool.body_steps(),
             "rates": [{k: r[k] for k in ("offered_rate_per_s", "achieved_rate_per_s", "p50_ms",
-                                          "p99_ms", "body_steps_per_s")} for r in sweep],
+                                          "p99_ms", "body_steps_per_s", "wall_s", "worker")}
+                      for r in sweep],
             "plain_back_to_back": plain_value,
             "served_over_plain": top["body_steps_per_s"] / plain_value if plain_value else None,
             "clocks": clocks,
