@@ -212,9 +212,17 @@ __device__ __forceinline__ uint32_t body_acceleration(const SceneDesc &S, float 
       const float eps = fmaxf(S.softening, (0.62f * kHalf) * pow2_neg(chosen));
       const float inv_r = inv_sqrt((dx * dx + dy * dy) + dz * dz + eps * eps);
       const float gsm = ax4.x;  // G * f32(count - 1) / f32(N)
+#ifdef RFMM_FAST_FLOAT
+      // One weight for the three components (reassociated: fast variant only).
+      const float w = gsm * ((inv_r * inv_r) * inv_r);
+      ax = ax + dx * w;
+      ay = ay + dy * w;
+      az = az + dz * w;
+#else
       ax = ax + gsm * dx * inv_r * inv_r * inv_r;
       ay = ay + gsm * dy * inv_r * inv_r * inv_r;
       az = az + gsm * dz * inv_r * inv_r * inv_r;
+#endif
     }
 
     if (kPhi) {

@@ -8,7 +8,8 @@ Kernel translation units are compiled with ``-fmad=false`` and IEEE division
 and square root, which is the floating-point contract the kernels rely on to
 match the CPU oracle bit for bit.  The tree and body kernels are compiled a
 second time with ``-DRFMM_FAST_FLOAT`` (namespace ``rfmm::fast``), contraction
-on and approximate division and square root: the fast float variant.
+on, approximate division and square root and subnormals flushed to zero: the
+fast float variant.
 """
 from __future__ import annotations
 
@@ -30,7 +31,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I", CSRC, "-I", INCLUDE,
           "-I", BUILD]
 KERNEL_FLAGS = ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"]
-FAST_FLAGS = ["-DRFMM_FAST_FLOAT", "-fmad=true", "-prec-div=false", "-prec-sqrt=false", "-ftz=false"]
+FAST_FLAGS = ["-DRFMM_FAST_FLOAT", "-fmad=true", "-prec-div=false", "-prec-sqrt=false", "-ftz=true"]
 # Compiled again in the fast float variant (object name, source).
 FAST_SOURCES = ["kernels_tree.cu", "kernels_body.cu"]
 
