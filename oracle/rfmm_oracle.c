@@ -40,11 +40,13 @@
  * so those paths match the GPU bit for bit too.
  *
  * Pinning: the planner is pinned to the reference's own unit tests
- * (src/lib.rs:163-217).  The reference keeps no golden outputs for the
- * compute passes and its WGSL/wgpu harness cannot run in this environment,
- * so the pass restatement is cross-checked against an independent numpy
- * restatement and FP64 physics checks: kernel-output parity is unpinned
- * against executed reference output.
+ * (src/lib.rs:163-217).  The passes are pinned to the reference's own shader
+ * code: oracle/wgsl_transpile.py translates the compute entry points of
+ * src/rainbow_fmm.wgsl into C++, oracle/wgsl_ref_harness.cpp runs them in the
+ * native harness's dispatch order, and this oracle reproduces the digests of
+ * that execution bit for bit (tests/test_reference_golden.py against
+ * tests/golden/reference_wgsl_digests.json).  The float definitions above are
+ * the one thing the two share: WGSL leaves them to the implementation.
  */
 #include <math.h>
 #include <stdint.h>
