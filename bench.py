@@ -35,7 +35,9 @@ sampled during the timed region and `gpu_launches`.
 oracle port: the reference's Rust/WGSL harness needs a Vulkan adapter and a
 Rust toolchain, neither of which exists here) on all host cores, with the
 same protocol as `cpu_baseline`: each bench step resets the scene and runs
-the workload's FMM steps.
+the workload's FMM steps.  Both CPU legs also report `reference_shader`: the
+reference's own WGSL compute passes, translated to C++, on the same cores
+(slower than the port, which therefore stays the conservative baseline).
 """
 from __future__ import annotations
 
@@ -238,6 +240,44 @@ def cpu_baseline(w, seconds, near="reference", warmup=1):
             "host": host_cpu()}
 
 
+def reference_shader_rate(w, seconds=5.0, near="reference"):
+    """The reference's own WGSL compute passes (translated to C++ into
+    oracle/_ref/ by oracle/wgsl_transpile.py, run in the native harness's
+    dispatch order) on all host threads: FMM frames of the workload's first
+    scene from its starting state until `seconds` have passed.  Reported
+    beside the oracle port, which stays the baseline value: the port is the
+    faster of the two, so ratios against it are the conservative ones."""
+    if near != "reference":
+        return {"unavailable": "the reference shader has no P2P near field"}
+    try:
+        import numpy as np
+        from oracle import oracle as O, wgsl_ref as W
+        if not W.available():
+            return {"unavailable": "no translation of the reference shader on this machine "
+                                   "(oracle/_ref/ is generated where the reference checkout is)"}
+        W.build()
+        cores = W.set_threads(0)
+        p = workloads.batch_scenes(w)[0] if w["kind"] == "batched" else workloads.scene(w)
+        n = len(p)
+        depth, cells, scale = O.plan(n)
+        cfg = W.config(n, depth, cells, scale, gravity=w["G"], softening=w["eps"], dt=w["dt"])
+        st = W.RefState(p.view(np.float32).ravel(), cfg)
+        st.frames(1)  # warm-up
+        frames, t0 = 0, time.perf_counter()
+        while frames == 0 or time.perf_counter() - t0 < seconds:
+            st.frames(1)
+            frames += 1
+        el = time.perf_counter() - t0
+        return {"value": n * frames / el, "unit": "body-steps/s", "cores": cores,
+                "kind": "reference",
+                "sample": "%d FMM frame(s) of a %d-body scene of the workload after 1 warm-up "
+                          "frame, %d host threads, %.1f s" % (frames, n, cores, el),
+                "code": "src/rainbow_fmm.wgsl compute passes translated to C++ "
+                        "(oracle/wgsl_transpile.py), native/main.rs dispatch order"}
+    except Exception as e:  # a failed build or run never fails the bench line
+        return {"unavailable": "reference shader timing failed: %s" % type(e).__name__}
+
+
 def run_reference(args, w):
     """The reference arm: the CPU oracle on the same config, same protocol
     as cpu_baseline (each bench step resets the scene and runs the workload's
@@ -280,6 +320,7 @@ def run_reference(args, w):
         "e2e": {"value": value, "unit": "body-steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
+    line["cpu_baseline"]["reference_shader"] = reference_shader_rate(w, near=args.near)
     print(json.dumps(line), flush=True)
     return 0
 
@@ -879,7 +920,9 @@ def main():
     args = parse_args()
     w = workloads.WORKLOADS[args.workload]
     if args.cpu_baseline_only:
-        print(json.dumps(cpu_baseline(w, args.cpu_seconds, args.near)), flush=True)
+        line = cpu_baseline(w, args.cpu_seconds, args.near)
+        line["reference_shader"] = reference_shader_rate(w, near=args.near)
+        print(json.dumps(line), flush=True)
         return 0
     if args.impl == "reference":
         return run_reference(args, w)

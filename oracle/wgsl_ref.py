@@ -5,10 +5,12 @@
 ``wgsl_transpile.py`` into ``oracle/_ref/rainbow_fmm_wgsl.gen.cpp`` and
 compiles it with ``wgsl_ref_harness.cpp`` (the native harness's dispatch
 sequence, native/main.rs) into ``oracle/_ref/libwgsl_ref.so``.  Nothing of
-the reference is stored in the repository; where the checkout is absent
-``available()`` is False.  Only ``tests/golden/make_reference_golden.py``
-and CPU tests use it, to produce and check the golden fixtures that pin the
-oracle and the CUDA path to the reference's own code.
+the reference is stored in the repository: where the checkout is absent
+(the GPU machine), the translation generated earlier into ``oracle/_ref/``
+is compiled if it is there, else ``available()`` is False.  The fixture
+generator and the CPU tests use it to produce and check the golden digests
+that pin the oracle and the CUDA path to the reference's own code;
+``bench.py``'s CPU legs time it beside the oracle port.
 """
 from __future__ import annotations
 
@@ -26,20 +28,30 @@ MATH_DIR = os.path.join(os.path.dirname(HERE), "fmm-rainbow_gb300", "csrc")
 REF_DIR = os.environ.get("RFMM_REFERENCE_DIR", "/root/reference")
 SHADER = os.path.join(REF_DIR, "src", "rainbow_fmm.wgsl")
 
-CXXFLAGS = ["-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
+CXXFLAGS = ["-std=c++17", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-fno-fast-math",
             "-fno-finite-math-only", "-fwrapv", "-Wall", "-Wno-unused-function",
             "-Wno-unused-variable", "-Wno-unused-but-set-variable"]
 
 
-def available() -> bool:
+def shader_available() -> bool:
+    """The reference checkout is present (translation can be regenerated)."""
     return os.path.exists(SHADER)
 
 
-def _compile(shader_text: str, gen_path: str, lib_path: str) -> str:
+def available() -> bool:
+    """The translation can be built: from the checkout, or from a translation
+    generated earlier into oracle/_ref/ (machines without the checkout)."""
+    return shader_available() or os.path.exists(GEN)
+
+
+def _compile(shader_text, gen_path: str, lib_path: str) -> str:
+    """Translate `shader_text` into gen_path (None: use gen_path as it is) and
+    compile it with the harness into lib_path."""
     from . import wgsl_transpile
     os.makedirs(OUT_DIR, exist_ok=True)
-    with open(gen_path, "w") as fh:
-        fh.write(wgsl_transpile.transpile(shader_text))
+    if shader_text is not None:
+        with open(gen_path, "w") as fh:
+            fh.write(wgsl_transpile.transpile(shader_text))
     tmp = lib_path + ".tmp%d" % os.getpid()
     cmd = ["g++", *CXXFLAGS, "-I", HERE, "-I", MATH_DIR, "-include", gen_path,
            os.path.join(HERE, "wgsl_ref_harness.cpp"), "-o", tmp]
@@ -51,16 +63,23 @@ def _compile(shader_text: str, gen_path: str, lib_path: str) -> str:
 
 
 def build(force: bool = False) -> str:
-    """Translate the reference shader and compile the harness (when the checkout is present)."""
+    """Translate the reference shader and compile the harness.  Without the
+    checkout, compile the translation generated earlier into oracle/_ref/."""
     if not available():
         raise FileNotFoundError("reference shader not found: %s" % SHADER)
-    deps = [SHADER, os.path.join(HERE, "wgsl_transpile.py"), os.path.join(HERE, "wgsl_runtime.hpp"),
+    deps = [os.path.join(HERE, "wgsl_transpile.py"), os.path.join(HERE, "wgsl_runtime.hpp"),
             os.path.join(HERE, "wgsl_ref_harness.cpp"), os.path.join(MATH_DIR, "rfmm_math.h")]
+    if shader_available():
+        deps.append(SHADER)
+    else:
+        deps = [GEN] + deps[1:]
     if (not force and os.path.exists(LIB)
             and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps)):
         return LIB
-    with open(SHADER) as fh:
-        return _compile(fh.read(), GEN, LIB)
+    if shader_available():
+        with open(SHADER) as fh:
+            return _compile(fh.read(), GEN, LIB)
+    return _compile(None, GEN, LIB)
 
 
 def build_variant(shader_text: str, tag: str) -> C.CDLL:
@@ -89,7 +108,8 @@ def _bind(L):
     L.wref_seed.argtypes = [vp, P]
     L.wref_solve_fields.argtypes = [vp, vp, vp, P]
     L.wref_frames.argtypes = [vp, vp, vp, P, C.c_uint32]
-    for f in (L.wref_seed, L.wref_solve_fields, L.wref_frames):
+    L.wref_set_threads.argtypes = [C.c_int]
+    for f in (L.wref_seed, L.wref_solve_fields, L.wref_frames, L.wref_set_threads):
         f.restype = C.c_int
     return L
 
@@ -112,6 +132,11 @@ def config(n, depth, cells, scale, dt=0.0009, gravity=0.34, softening=0.012, spe
     c.control_axis_mode[:] = list(control_axis_mode)
     c.control_strength, c.control_radius = control_strength, control_radius
     return c
+
+
+def set_threads(n: int) -> int:
+    """Host threads for the translated dispatches (<= 0: all)."""
+    return lib().wref_set_threads(n)
 
 
 class RefState:

@@ -6,10 +6,10 @@
 //   solve  = clear_cells, deposit, upward (levels depth-1..0), m2l_all,
 //            downward (levels 1..depth), near_all        (main.rs:436-451)
 //   frame  = solve + integrate                           (main.rs:411-421)
-// with the same workgroup counts; every workgroup's invocations run one
-// after another, which the passes allow (no pass reads what another
-// invocation of the same dispatch writes, and the deposit's integer atomics
-// commute).
+// with the same workgroup counts.  A dispatch's invocations may run on
+// several host threads (OpenMP), which the passes allow: no pass reads what
+// another invocation of the same dispatch writes, and the deposit's integer
+// atomics commute, so results do not depend on the thread count.
 //
 // The translated shader (oracle/_ref/rainbow_fmm_wgsl.gen.cpp, written by
 // wgsl_transpile.py) is force-included ahead of this file by the build
@@ -18,6 +18,9 @@
 #include <cstdint>
 #include <cstring>
 #include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 #include "wgsl_runtime.hpp"
 
@@ -82,8 +85,10 @@ const wgsl_entry *entry(const char *name) {
 
 void dispatch(const char *name, uint32_t gx, uint32_t gy) {
   const wgsl_entry *e = entry(name);
-  for (uint32_t y = 0; y < gy; y++)
-    for (uint32_t x = 0; x < gx * e->wg; x++) e->fn(wgsl::make<uint32_t, 3>(x, y, 0u));
+  const int64_t row = (int64_t)gx * e->wg, total = row * gy;
+#pragma omp parallel for schedule(static, 4096) if (total >= 16384)
+  for (int64_t i = 0; i < total; i++)
+    e->fn(wgsl::make<uint32_t, 3>((uint32_t)(i % row), (uint32_t)(i / row), 0u));
 }
 
 uint32_t div_ceil(uint32_t a, uint32_t b) { return (a + b - 1u) / b; }
@@ -126,6 +131,18 @@ void solve(const RefConfig &c, const Plans &P) {
 }  // namespace
 
 extern "C" {
+
+// Host threads for the dispatches (<= 0: all); returns the count in use.
+int wref_set_threads(int n) {
+#ifdef _OPENMP
+  if (n <= 0) n = omp_get_num_procs();
+  omp_set_num_threads(n);
+  return n;
+#else
+  (void)n;
+  return 1;
+#endif
+}
 
 // The reference galaxy (`initialize`) into `particles` (count x 32 bytes).
 int wref_seed(void *particles, const RefConfig *c) {

@@ -14,7 +14,8 @@
 //     mix(a, b, t) = a*(1-t) + b*t; smoothstep = t*t*(3-2t) with
 //     t = clamp((x-lo)/(hi-lo), 0, 1); fract(x) = x - floor(x);
 //   * exp, pow, sin, cos, atan2 are the binary32 functions of rfmm_math.h;
-//   * atomics act on plain memory (invocations run one after another).
+//   * atomic read-modify-writes are host atomics (relaxed; integer sums
+//     commute, so the order of invocations does not change results).
 #pragma once
 
 #include <cmath>
@@ -294,19 +295,18 @@ inline T mod(T a, T b) {
   }
 }
 
-// Atomics on plain memory: invocations run one after another.  Integer sums
-// wrap modulo 2^32 like the device's.
+// Atomics: the harness may run a dispatch's invocations on several host
+// threads, so the read-modify-write forms are real atomic operations.
+// Integer sums wrap modulo 2^32 like the device's.
 template <class T, class U>
 inline T atomicAdd(T *p, U v) {
-  const T old = *p;
-  *p = (T)((uint32_t)old + (uint32_t)(T)v);
-  return old;
+  static_assert(sizeof(T) == 4, "32-bit atomics only");
+  return (T)__atomic_fetch_add(reinterpret_cast<uint32_t *>(p), (uint32_t)(T)v, __ATOMIC_RELAXED);
 }
 template <class T, class U>
 inline T atomicSub(T *p, U v) {
-  const T old = *p;
-  *p = (T)((uint32_t)old - (uint32_t)(T)v);
-  return old;
+  static_assert(sizeof(T) == 4, "32-bit atomics only");
+  return (T)__atomic_fetch_sub(reinterpret_cast<uint32_t *>(p), (uint32_t)(T)v, __ATOMIC_RELAXED);
 }
 template <class T>
 inline T atomicLoad(T *p) { return *p; }

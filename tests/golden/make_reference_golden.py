@@ -105,6 +105,7 @@ def ref_config(n, params):
 def run_case(case):
     import numpy as np
     from oracle import oracle as O, wgsl_ref as W
+    W.set_threads(1)  # one process per case
     n = n_of(case["input"])
     cfg = ref_config(n, case["params"])
     p = make_input(case["input"])
@@ -132,6 +133,7 @@ def run_batch_scene(args):
     import numpy as np
     from oracle import oracle as O, wgsl_ref as W
     from rfmm import workloads
+    W.set_threads(1)
     i, frames, params = args
     p = workloads.batch_scenes(workloads.WORKLOADS[BATCH["workload"]])[i]
     cfg = ref_config(len(p), params)

@@ -76,7 +76,7 @@ def test_oracle_matches_reference_shader_batched_256(oracle_mod):
 
 def _ref_module():
     from oracle import wgsl_ref as W
-    if not W.available():
+    if not W.shader_available():
         pytest.skip("reference checkout absent: the committed digests above stand in for it")
     return W
 
