@@ -409,6 +409,36 @@ def float_variant_pass(args, torch, rfmm, stream, flush, handle, fn, body_steps,
             "timeline": tl_summary}
 
 
+def pipelined_e2e(torch, pair, k, upload, solve, download):
+    """Wall time of `k` end-to-end bench steps through the public C ABI with
+    host buffers, two handles alternating.  `pair` holds two (handle, torch
+    stream) pairs; upload(h) enqueues one bench step's host->device input
+    copy (and the commit's sort), solve(h) its FMM steps, download(h) reads
+    its result into host memory and returns once the bytes are there.  Bench
+    step i runs on handle i % 2: while it computes, the next step's input is
+    copied in on the other handle's stream, and the next solve waits (an
+    event) only for this one's compute, so this step's device->host read
+    overlaps the next solve.  Two solves never run at once (each keeps the
+    L2 to itself); every step's copies stay inside the timed region."""
+    ev = [torch.cuda.Event(), torch.cuda.Event()]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    h0, s0 = pair[0]
+    upload(h0)
+    solve(h0)
+    ev[0].record(s0)
+    for i in range(k):
+        hx, _ = pair[i % 2]
+        if i + 1 < k:
+            hy, sy = pair[(i + 1) % 2]
+            upload(hy)
+            sy.wait_event(ev[i % 2])
+            solve(hy)
+            ev[(i + 1) % 2].record(sy)
+        download(hx)
+    return time.perf_counter() - t0
+
+
 def run_gpu_plain(args, w, torch, rfmm, stream, flush, rank, world, local):
     import numpy as np
     from rfmm import replicas, roofline
@@ -510,9 +540,34 @@ def run_gpu_plain(args, w, torch, rfmm, stream, flush, rank, world, local):
     e2e = None
     if e2e_times:
         e2e_s = statistics.median(e2e_times)  # host wall clock: the median resists scheduler jitter
-        e2e = {"value": world * n * fmm_steps / e2e_s, "unit": "body-steps/s",
+        serial = {"value": world * n * fmm_steps / e2e_s, "ms_per_step": 1e3 * e2e_s,
+                  "timer": "host wall clock (median of %d), one handle: upload, solve and "
+                           "download one after another" % len(e2e_times)}
+        # The same calls on two handles, pipelined (copies of one bench step
+        # overlap the neighbouring steps' compute).
+        other = rfmm.Solver(n, params)
+        other_stream = torch.cuda.Stream()
+        other.set_stream(other_stream.cuda_stream)
+        other.set_tuning(tuning)
+        if args.near == "p2p":
+            other.set_near_mode(rfmm.NEAR_P2P)
+        if args.float == "fast":
+            other.set_float_mode(rfmm.FLOAT_FAST)
+        pair = [(solver, stream), (other, other_stream)]
+        up = lambda h: h.upload_host_ptr(pin_in.data_ptr(), pin_in.numel())
+        sol = lambda h: h.step(fmm_steps)
+        down = lambda h: h.download_host_ptr(rfmm.BUF_PARTICLES, pin_out.data_ptr(), pin_out.numel())
+        pipelined_e2e(torch, pair, 2, up, sol, down)  # warm-up: the second handle's graphs
+        kp = max(2, args.e2e_steps)
+        el = pipelined_e2e(torch, pair, kp, up, sol, down)
+        other.close()
+        e2e = {"value": world * n * fmm_steps * kp / el, "unit": "body-steps/s",
                "h2d_bytes_per_step": n * 32, "d2h_bytes_per_step": n * 32,
-               "ms_per_step": 1e3 * e2e_s, "timer": "host wall clock (median of %d)" % len(e2e_times)}
+               "ms_per_step": 1e3 * el / kp,
+               "timer": "host wall clock over %d bench steps through two handles on two streams "
+                        "(one step's host copies overlap its neighbours' compute; the solves run "
+                        "one at a time)" % kp,
+               "serial": serial}
 
     # Accuracy of the state the bench ends on (outside every timed region):
     # FP64 direct-sum force error on a seeded target sample, FP64 energy.
@@ -661,9 +716,33 @@ def run_gpu_batched(args, w, torch, rfmm, stream, flush, rank, world, local):
     e2e = None
     if e2e_times:
         e2e_s = statistics.median(e2e_times)
-        e2e = {"value": world * bodies * fmm_steps / e2e_s, "unit": "body-steps/s",
+        serial = {"value": world * bodies * fmm_steps / e2e_s, "ms_per_step": 1e3 * e2e_s,
+                  "timer": "host wall clock (median of %d), one batch handle: upload, solve and "
+                           "download one after another" % len(e2e_times)}
+        other = rfmm.Batch(sizes, [params] * len(ps))
+        other_stream = torch.cuda.Stream()
+        other.set_stream(other_stream.cuda_stream)
+        other.set_tuning(batch.tuning())
+        pair = [(batch, stream), (other, other_stream)]
+
+        def up(b):
+            for i, t in enumerate(pin):
+                rfmm._check(rfmm.lib().rfmm_batch_upload(b._h, i, t.data_ptr(), t.numel()), "upload")
+            b.commit()
+
+        sol = lambda b: b.step(fmm_steps)
+        down = lambda b: b.download_all_into(rfmm.BUF_PARTICLES, out_ptrs)
+        pipelined_e2e(torch, pair, 2, up, sol, down)  # warm-up: the second handle's graphs
+        kp = max(2, args.e2e_steps)
+        el = pipelined_e2e(torch, pair, kp, up, sol, down)
+        other.close()
+        e2e = {"value": world * bodies * fmm_steps * kp / el, "unit": "body-steps/s",
                "h2d_bytes_per_step": bodies * 32, "d2h_bytes_per_step": bodies * 32,
-               "ms_per_step": 1e3 * e2e_s, "timer": "host wall clock (median of %d)" % len(e2e_times)}
+               "ms_per_step": 1e3 * el / kp,
+               "timer": "host wall clock over %d bench steps through two batch handles on two "
+                        "streams (one step's host copies overlap its neighbours' compute; the "
+                        "solves run one at a time)" % kp,
+               "serial": serial}
     batch.close()
     return {
         "metric": "body-steps/s", "value": value, "unit": "body-steps/s", "n_gpus": world,
