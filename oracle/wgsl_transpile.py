@@ -594,6 +594,10 @@ class Emitter:
         k = s[0]
         if k == "decl":
             _, kind, name, ty, init = s
+            if kind == "const" and ty is None:
+                # A function-scope abstract constant would need scoped folding;
+                # the translated shader has none, so refuse rather than guess.
+                raise NotImplementedError("wgsl: function-scope untyped const %r" % name)
             if ty is not None:
                 ct = self.ctype(ty)
                 if init is None:
