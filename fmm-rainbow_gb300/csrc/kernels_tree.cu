@@ -94,7 +94,7 @@ __device__ __forceinline__ void upward_task(
     uint32_t *__restrict__ choice, WorkItem *__restrict__ plist, uint32_t plist_cap,
     Counters *__restrict__ ctr, uint32_t list_par, uint32_t *__restrict__ tickets, uint4 *s0,
     uint4 *s1, uint4 *s2, uint4 *s_top, WorkItem *s_items, uint32_t &s_nitems, uint32_t &s_base,
-    uint32_t &s_last) {
+    uint32_t &s_last, bool trigger) {
   const uint32_t tid = threadIdx.x;
   const uint32_t D = S.depth, r = S.sub_level;  // r = D - 3
   uint32_t sx, sy, sz;
@@ -178,6 +178,10 @@ __device__ __forceinline__ void upward_task(
     s_last = last;
   }
   __syncthreads();
+  // The CTA's last task is past its ticket: let the next pass launch, so its
+  // launch overlaps the writes below and the last CTA's top levels (the
+  // next pass still waits for this whole grid before it reads anything).
+  if (trigger) grid_dependents_may_launch();
 
   if (live) {
     // Leaves: source records and the cleared next-deposit leaf.
@@ -601,7 +605,8 @@ __global__ void __launch_bounds__(256, 4) k_upward(const SceneDesc *__restrict__
       load_scene(sS, scenes, scene);
     }
     upward_task(sS, scene, task - sS.task_off, mom, mom_next, src, aux, choice, plist, plist_cap,
-                ctr, list_par, tickets, s0, s1, s2, s_top, s_items, s_nitems, s_base, s_last);
+                ctr, list_par, tickets, s0, s1, s2, s_top, s_items, s_nitems, s_base, s_last,
+                it + ncta >= ntasks);
   }
   stamp_end(stamp);
   grid_dependents_may_launch();
