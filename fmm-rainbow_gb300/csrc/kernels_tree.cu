@@ -755,7 +755,10 @@ __device__ __forceinline__ void m2l_lanes_pass(const SceneDesc *__restrict__ sce
 #pragma unroll
     for (int k = 0; k < 10; k++) acc[k] = 0.0f;
     if (__any_sync(0xFFFFFFFFu, live)) {
-      // Slot k + 1's source is requested while slot k is evaluated.
+      // Two consecutive slots per iteration: their pair terms are
+      // independent chains (the square root and division of one overlap the
+      // other's), and they are added in slot order.  The next two slots'
+      // sources are requested meanwhile.
       auto fetch = [&](uint32_t k, float4 &sv) {
         const uint32_t e = cl[k];
         const int x = bx + (int)(e & 7u), y = by + (int)((e >> 3) & 7u), z = bz + (int)(e >> 6);
@@ -763,17 +766,36 @@ __device__ __forceinline__ void m2l_lanes_pass(const SceneDesc *__restrict__ sce
         if (live && (uint32_t)x < dim && (uint32_t)y < dim && (uint32_t)z < dim)
           sv = __ldg(&src[lvl_base + lin3((uint32_t)x, (uint32_t)y, (uint32_t)z, dim)]);
       };
-      float4 next;
-      fetch(0u, next);
-      for (uint32_t k = 0; k < kContrib; k++) {
-        const float4 sv = next;
-        if (k + 1u < kContrib) fetch(k + 1u, next);
-        if (sv.w != 0.0f) {  // absent and empty slots read w = 0
+      static_assert(kContrib % 2u == 1u, "the loop below ends with one single slot");
+      float4 n0, n1;
+      fetch(0u, n0);
+      fetch(1u, n1);
+      for (uint32_t k = 0; k + 1u < kContrib; k += 2u) {
+        const float4 s0 = n0, s1 = n1;
+        fetch(k + 2u, n0);  // k + 2 <= kContrib - 1
+        if (k + 3u < kContrib) fetch(k + 3u, n1);
+        // Both 1/r chains first, then the terms slot by slot (absent and
+        // empty slots read w = 0 and add nothing).
+        const PairSetup p0 = pair_setup(s0, ctx, cty, ctz, eps);
+        const PairSetup p1 = pair_setup(s1, ctx, cty, ctz, eps);
+        if (s0.w != 0.0f) {
           float out[10];
-          pair_field_d(sv, ctx, cty, ctz, eps, out);
+          pair_terms(p0, out);
 #pragma unroll
           for (int m = 0; m < 10; m++) acc[m] = acc[m] + out[m];
         }
+        if (s1.w != 0.0f) {
+          float out[10];
+          pair_terms(p1, out);
+#pragma unroll
+          for (int m = 0; m < 10; m++) acc[m] = acc[m] + out[m];
+        }
+      }
+      if (n0.w != 0.0f) {  // the last slot (kContrib - 1)
+        float out[10];
+        pair_field_d(n0, ctx, cty, ctz, eps, out);
+#pragma unroll
+        for (int m = 0; m < 10; m++) acc[m] = acc[m] + out[m];
       }
     }
     if (live) {
@@ -785,8 +807,10 @@ __device__ __forceinline__ void m2l_lanes_pass(const SceneDesc *__restrict__ sce
   }
 }
 
+// The instance with the lane path gets up to 64 registers (4 CTAs per SM)
+// for its two-slot chains; the one-scene instance keeps 40 (6 per SM).
 template <bool kCompact, bool kWide>
-__global__ void __launch_bounds__(256, 6) k_m2l(const SceneDesc *__restrict__ scenes,
+__global__ void __launch_bounds__(256, kWide ? 4 : 6) k_m2l(const SceneDesc *__restrict__ scenes,
                                              const WorkItem *__restrict__ plist, uint32_t plist_cap,
                                              Counters *__restrict__ ctr, uint32_t list_par,
                                              const uint4 *__restrict__ mom,

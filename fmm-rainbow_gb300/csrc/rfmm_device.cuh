@@ -165,13 +165,27 @@ __device__ __forceinline__ float inv_sqrt(float x) { return 1.0f / sqrtf(x); }
 
 // pair_field (wgsl:170-203) for a source cell whose centre of mass `src`
 // and gravity-times-mass `gm` were precomputed exactly as the reference
-// computes them per pair (moment_com_read and G * count / N).
-__device__ __forceinline__ void pair_field_d(float4 src, float tx, float ty, float tz, float eps,
-                                             float out[10]) {
-  const float gm = src.w;
-  const float rx = src.x - tx, ry = src.y - ty, rz = src.z - tz;
-  const float r2 = (rx * rx + ry * ry) + rz * rz + eps * eps;
-  const float inv_r = inv_sqrt(r2);
+// computes them per pair (moment_com_read and G * count / N), in two steps:
+// pair_setup forms the offset and 1/r (the long square-root and division
+// chain), pair_terms the ten field terms from them.  Callers that keep two
+// pairs in flight run both setups before either's terms.
+struct PairSetup {
+  float rx, ry, rz, gm, inv_r;
+};
+
+__device__ __forceinline__ PairSetup pair_setup(float4 src, float tx, float ty, float tz, float eps) {
+  PairSetup p;
+  p.gm = src.w;
+  p.rx = src.x - tx;
+  p.ry = src.y - ty;
+  p.rz = src.z - tz;
+  const float r2 = (p.rx * p.rx + p.ry * p.ry) + p.rz * p.rz + eps * eps;
+  p.inv_r = inv_sqrt(r2);
+  return p;
+}
+
+__device__ __forceinline__ void pair_terms(const PairSetup &p, float out[10]) {
+  const float gm = p.gm, rx = p.rx, ry = p.ry, rz = p.rz, inv_r = p.inv_r;
   const float inv_r3 = inv_r * inv_r * inv_r;
   const float inv_r5 = inv_r3 * inv_r * inv_r;
   const float diagonal = -gm * inv_r3;
@@ -186,6 +200,11 @@ __device__ __forceinline__ void pair_field_d(float4 src, float tx, float ty, flo
   out[7] = diagonal + tidal * ry * ry;
   out[8] = tidal * ry * rz;
   out[9] = diagonal + tidal * rz * rz;
+}
+
+__device__ __forceinline__ void pair_field_d(float4 src, float tx, float ty, float tz, float eps,
+                                             float out[10]) {
+  pair_terms(pair_setup(src, tx, ty, tz, eps), out);
 }
 
 // Per-cell terms of integrate's self-leaf and excitation update that depend
