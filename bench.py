@@ -661,6 +661,13 @@ def run_gpu_batched(args, w, torch, rfmm, stream, flush, rank, world, local):
     clocks = clocks_summary(clk)
     value, _, slowest_s = replicas.reduce_throughput(bodies * fmm_steps * args.steps, local_ms * 1e-3)
     ms_per_step = slowest_s * 1e3 / args.steps
+    if args.no_extras and args.workload == "batched_256":
+        batch.close()
+        return {"metric": "body-steps/s", "value": value, "unit": "body-steps/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+                "config": {"workload": "batched_256", "scenes": len(ps), "bodies": bodies,
+                           "fmm_steps_per_bench_step": fmm_steps, "extras": "skipped"},
+                "clocks": clocks, "gpu_launches": launches}
 
     tl, tl_summary = timeline_pass(torch, stream, flush, batch, batched_step, min(args.steps, 3),
                                    fmm_steps, ms_per_step)
