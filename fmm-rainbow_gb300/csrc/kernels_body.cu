@@ -408,6 +408,10 @@ __global__ void __launch_bounds__(256, 6) k_integrate(const SceneDesc *__restric
       n1 = part[2u * (next_tile * kTile + threadIdx.x) + 1u];
     }
     i = ni;
+    // The CTA's last tile: the next step's upward pass may launch now (it
+    // waits for this whole grid before reading anything); its CTAs take SM
+    // slots as this grid's CTAs leave.
+    if (ni >= end) grid_dependents_may_launch();
     const uint32_t sc = tile_scene[tile];
     if (sc != cur) {
       load_scene(S, scenes, sc);
