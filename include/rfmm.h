@@ -103,7 +103,10 @@ int rfmm_get_plan(const rfmm_handle *h, rfmm_plan *out);
 int rfmm_set_params(rfmm_handle *h, const rfmm_params *params);
 
 /* Upload N bodies (N x 32 B, reference Particle layout) from host memory
- * (pinned or pageable) or from device memory. */
+ * (pinned or pageable) or from device memory.  The copy and the leaf sort
+ * are enqueued on the handle's stream; from pinned memory the call returns
+ * before the copy has run, so the source must stay valid until the handle's
+ * next synchronising call (rfmm_download, rfmm_sync). */
 int rfmm_upload_particles(rfmm_handle *h, const void *host_aos, size_t bytes);
 int rfmm_upload_particles_device(rfmm_handle *h, const void *device_aos, size_t bytes);
 
@@ -115,7 +118,8 @@ int rfmm_seed_galaxy(rfmm_handle *h);
  * the field of the current positions. */
 int rfmm_solve_fields(rfmm_handle *h);
 
-/* `steps` full solver frames (native/main.rs:411-421). */
+/* `steps` full solver frames (native/main.rs:411-421), enqueued on the
+ * handle's stream. */
 int rfmm_step(rfmm_handle *h, uint32_t steps);
 
 /* Wait for the handle's queued work; reports kernel error words. */
@@ -123,7 +127,8 @@ int rfmm_sync(rfmm_handle *h);
 
 /* Copy a buffer to host memory (bytes must equal the buffer size:
  * N*32, C*16 or C*48) or to device memory.  Particles come back in the
- * caller's body order. */
+ * caller's body order.  Returns once the bytes are in place (it waits for
+ * the handle's stream), reporting kernel error words like rfmm_sync. */
 int rfmm_download(rfmm_handle *h, int which, void *host_dst, size_t bytes);
 int rfmm_download_device(rfmm_handle *h, int which, void *device_dst, size_t bytes);
 
