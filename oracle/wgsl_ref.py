@@ -155,14 +155,19 @@ class RefState:
                 self.fields.ctypes.data_as(C.c_void_p))
 
     def solve_fields(self):
-        (self.lib or lib()).wref_solve_fields(*self._ptrs(), C.byref(self.cfg))
+        _ok((self.lib or lib()).wref_solve_fields(*self._ptrs(), C.byref(self.cfg)))
 
     def frames(self, k: int):
-        (self.lib or lib()).wref_frames(*self._ptrs(), C.byref(self.cfg), k)
+        _ok((self.lib or lib()).wref_frames(*self._ptrs(), C.byref(self.cfg), k))
 
 
 def seed(cfg: RefConfig, like: np.ndarray | None = None) -> np.ndarray:
     """The reference galaxy of cfg.count bodies (raw 32-byte records)."""
     out = np.zeros(cfg.count * 8, np.float32) if like is None else np.empty_like(like)
-    lib().wref_seed(out.ctypes.data_as(C.c_void_p), C.byref(cfg))
+    _ok(lib().wref_seed(out.ctypes.data_as(C.c_void_p), C.byref(cfg)))
     return out
+
+
+def _ok(status: int) -> None:
+    if status != 0:
+        raise RuntimeError("the translated shader lacks an entry point the harness dispatches")

@@ -83,8 +83,16 @@ const wgsl_entry *entry(const char *name) {
   return nullptr;
 }
 
+// Set when a dispatch names an entry point the translation does not have
+// (the shader changed): the calls below then return -1.
+bool g_missing = false;
+
 void dispatch(const char *name, uint32_t gx, uint32_t gy) {
   const wgsl_entry *e = entry(name);
+  if (e == nullptr) {
+    g_missing = true;
+    return;
+  }
   const int64_t row = (int64_t)gx * e->wg, total = row * gy;
 #pragma omp parallel for schedule(static, 4096) if (total >= 16384)
   for (int64_t i = 0; i < total; i++)
@@ -151,16 +159,18 @@ int wref_seed(void *particles, const RefConfig *c) {
   w_params = P.level[c->depth];
   uint32_t gx, gy;
   particle_grid(c->count, gx, gy);
+  g_missing = false;
   dispatch("initialize", gx, gy);
-  return 0;
+  return g_missing ? -1 : 0;
 }
 
 // One field solve (the harness's digest block): moments and fields.
 int wref_solve_fields(void *particles, void *moments, void *fields, const RefConfig *c) {
   const Plans P = plans(*c);
   bind(particles, moments, fields);
+  g_missing = false;
   solve(*c, P);
-  return 0;
+  return g_missing ? -1 : 0;
 }
 
 // `frames` full frames (solve + integrate).
@@ -170,12 +180,13 @@ int wref_frames(void *particles, void *moments, void *fields, const RefConfig *c
   bind(particles, moments, fields);
   uint32_t gx, gy;
   particle_grid(c->count, gx, gy);
-  for (uint32_t f = 0; f < frames; f++) {
+  g_missing = false;
+  for (uint32_t f = 0; f < frames && !g_missing; f++) {
     solve(*c, P);
     w_tree_params = P.level[c->depth];
     dispatch("integrate", gx, gy);
   }
-  return 0;
+  return g_missing ? -1 : 0;
 }
 
 }  // extern "C"

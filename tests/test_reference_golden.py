@@ -143,3 +143,18 @@ def test_planted_shader_mistake_is_caught(oracle_mod, old, new, where):
     same_p = np.array_equal(ref.particles.view(np.uint32), st.particles.view(np.uint32).ravel())
     assert not (same_f and same_p), "the planted change went unnoticed"
     assert not (same_f if where == "fields" else same_p)
+
+
+def test_missing_entry_point_is_reported(oracle_mod):
+    """A shader whose pass the harness dispatches is gone fails loudly."""
+    W = _ref_module()
+    O = oracle_mod
+    with open(W.SHADER) as fh:
+        text = fh.read()
+    assert text.count("fn near_all(") == 1
+    lib = W.build_variant(text.replace("fn near_all(", "fn near_all_renamed("), "renamed")
+    p = O.initialize(4096)
+    params = O.make_params(4096)
+    cfg = W.config(4096, params.depth, O.lib().oracle_total_cells(params.depth), params.scale)
+    with pytest.raises(RuntimeError):
+        W.RefState(p.view(np.float32).ravel(), cfg, library=lib).solve_fields()
