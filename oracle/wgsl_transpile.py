@@ -439,6 +439,17 @@ def f32_of(x: float) -> float:
     return struct.unpack("<f", struct.pack("<f", x))[0]
 
 
+def int_literal(v: int) -> str:
+    """An abstract integer as C++: int in i32 range (C++ then converts it like
+    WGSL concretises it), u32 above, refused beyond (C++ would widen to 64
+    bits where WGSL cannot)."""
+    if -(1 << 31) <= v < (1 << 31):
+        return "(%d)" % v
+    if 0 <= v < (1 << 32):
+        return "(%du)" % v
+    raise ValueError("wgsl: integer constant %d outside i32/u32" % v)
+
+
 def f32_literal(x: float) -> str:
     v = f32_of(x)
     if v != v or v in (float("inf"), float("-inf")):
@@ -506,7 +517,7 @@ class Emitter:
         if v is not None:
             if v[0] == "afloat":
                 return f32_literal(v[1])
-            return "(%d)" % v[1]
+            return int_literal(v[1])
         k = e[0]
         if k == "lit":
             kind, val = e[1], e[2]
