@@ -59,6 +59,14 @@ CASES = [
     dict(name="tiny_17", input=["scene", "plummer", 17, 1], params=BENCH, frames=3),
     dict(name="fast_speed_8000", input=["scene", "plummer", 8000, 8], frames=2,
          params=dict(gravity=1.0, softening=1e-3, dt=4e-3, speed=2.5)),
+    # Plan overrides (rfmm_params depth / fixed_point_scale), which the shader
+    # takes through its uniform block like the planner's values.
+    dict(name="plummer_20000_depth6", input=["scene", "plummer", 20000, 5], frames=2,
+         params=dict(BENCH, depth=6)),
+    dict(name="clusters_40000_depth4", input=["scene", "clusters", 40000, 9], frames=2,
+         params=dict(BENCH, depth=4)),
+    dict(name="uniform_30000_scale128", input=["scene", "uniform", 30000, 7], frames=2,
+         params=dict(BENCH, scale=128.0)),
 ]
 BATCH = dict(name="batched_256", workload="batched_256", frames=4, params=BENCH)
 
@@ -96,10 +104,14 @@ def n_of(spec):
 
 
 def ref_config(n, params):
+    """The uniform values of a case: the planner's depth and scale unless the
+    case overrides them (keys `depth`, `scale`)."""
     from oracle import oracle as O, wgsl_ref as W
-    depth, cells, scale = O.plan(n)
+    depth, _, scale = O.plan(n)
     kw = dict(params)
-    return W.config(n, depth, cells, scale, **kw)
+    depth = kw.pop("depth", depth)
+    scale = kw.pop("scale", scale)
+    return W.config(n, depth, O.lib().oracle_total_cells(depth), scale, **kw)
 
 
 def run_case(case):

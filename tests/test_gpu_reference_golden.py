@@ -26,7 +26,10 @@ CASES = GOLDEN["cases"]
 
 
 def _params(R, prm):
-    return R.default_params(**dict(prm))
+    kw = dict(prm)
+    if "scale" in kw:  # a plan override: rfmm_params.fixed_point_scale
+        kw["fixed_point_scale"] = kw.pop("scale")
+    return R.default_params(**kw)
 
 
 @pytest.mark.parametrize("name", list(CASES))
