@@ -125,3 +125,35 @@ def test_served_requests_match_reference_shader(rfmm_mod, oracle_mod):
     for name, got in results.items():
         assert O.fnv1a(got) == CASES[name]["frame_particles"], \
             "%s: served result differs from the reference shader's" % name
+
+
+def test_noalloc_solve_matches_reference_shader(rfmm_mod, oracle_mod):
+    """rfmm_solve_fields_noalloc (caller buffers, fixed scratch) against the
+    reference's one-solve digests, for every planner-sized case it takes."""
+    import torch
+    import make_reference_golden as G
+    R, O = rfmm_mod, oracle_mod
+    checked = 0
+    for name, g in CASES.items():
+        n = g["n"]
+        if n > (1 << 17) or "depth" in g["params"] or "scale" in g["params"]:
+            continue
+        p = G.make_input(g["input"])
+        if p is None:
+            with R.Solver(n, _params(R, g["params"])) as s:
+                s.seed_galaxy()
+                p = s.particles()
+        elif O.fnv1a(p) != g["input_particles"]:
+            continue
+        dev = torch.from_numpy(p.view(np.uint8).copy()).cuda()
+        mom = torch.zeros(g["cells"] * 16, dtype=torch.uint8, device="cuda")
+        fld = torch.zeros(g["cells"] * 48, dtype=torch.uint8, device="cuda")
+        stream = torch.cuda.current_stream()
+        R.solve_fields_noalloc(dev.data_ptr(), n, _params(R, g["params"]), mom.data_ptr(),
+                               fld.data_ptr(), stream.cuda_stream)
+        assert R.noalloc_device_error(stream.cuda_stream) == (R.RFMM_OK, 0, 0)
+        torch.cuda.synchronize()
+        assert O.fnv1a(mom.cpu().numpy()) == g["solve_moments"], name
+        assert O.fnv1a(fld.cpu().numpy()) == g["solve_fields"], name
+        checked += 1
+    assert checked >= 8
