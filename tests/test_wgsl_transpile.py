@@ -12,7 +12,6 @@ constructors, and atomics across host threads.
 import ctypes as C
 import os
 import subprocess
-import tempfile
 
 import numpy as np
 import pytest
@@ -104,9 +103,9 @@ extern "C" void run(const char *name, uint32_t invocations) {
 
 
 @pytest.fixture(scope="module")
-def lib():
+def lib(tmp_path_factory):
     from oracle import wgsl_ref, wgsl_transpile
-    d = tempfile.mkdtemp(prefix="wgsl_t_")
+    d = str(tmp_path_factory.mktemp("wgsl_t"))
     src = os.path.join(d, "m.cpp")
     with open(src, "w") as fh:
         fh.write("#include <cstring>\n" + wgsl_transpile.transpile(MODULE) + HARNESS)
